@@ -1,0 +1,90 @@
+/* liblabinius_gpu: the GB300 Labinius opening prover behind a C ABI.
+ *
+ * The boundary is the reference prover's own: `prove(seed, Q, table) -> proof bytes` of
+ * solution/proof_generate/src/main.rs:1692-2009 (prove) and :1252-1416 (the bincode layout
+ * written by encode_into), reached from the `labinius-fast --prove FILE --table FILE
+ * [--modulus Q]` command (main.rs:2050-2090, LABINIUS_SEED in the environment). The proof bytes
+ * are the layout of verifier/proof_verify/src/main.rs:98-124.
+ *
+ * All buffers are caller-owned. Return codes are 0 or one of the negative LF_E_* values.
+ * A context is bound to one CUDA device; calls on one context are serialised. */
+#ifndef LABINIUS_GPU_H
+#define LABINIUS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LF_OK 0
+#define LF_E_ARGS (-1)      /* a null or inconsistent argument */
+#define LF_E_SHAPE (-2)     /* LOG_VARS outside what the prover supports */
+#define LF_E_MODULUS (-3)   /* the modulus fails the checker's gate (main.rs:85-96) or the prover's support */
+#define LF_E_TABLE_LEN (-4) /* table bytes != 2^LOG_VARS / 8 (main.rs:143-153) */
+#define LF_E_CAP (-5)       /* proof buffer smaller than lf_proof_size() */
+#define LF_E_OOM (-6)       /* device memory could not be reserved */
+#define LF_E_CUDA (-7)      /* a CUDA call failed; see lf_last_error() */
+#define LF_E_INTERNAL (-8)  /* a device-side check failed (challenge sampling bound, fold range) */
+#define LF_E_ADMISSION (-9) /* the request does not fit the context's HBM budget */
+
+typedef struct lf_ctx lf_ctx;
+
+typedef struct lf_config {
+  int device;             /* CUDA ordinal */
+  size_t hbm_budget;      /* bytes the context may hold on the device; 0 = no limit */
+} lf_config;
+
+/* Per-phase device times of the last lf_prove* call on a context, in milliseconds
+ * (the reference's labinius-profile line, solution/proof_generate/src/main.rs:1999-2007). */
+typedef struct lf_profile {
+  double upload_ms, key_ms, commit_ms, transcript_ms, partials_ms, switch_ms, row_ms, challenges_ms, fold_ms,
+      download_ms, total_ms;
+} lf_profile;
+
+/* Context lifetime. Replaces the process-wide pool and allocator of the reference prover
+ * (solution/labinius/crates/pcs/src/par.rs, solution/proof_generate/src/main.rs:1427-1569). */
+int lf_ctx_create(const lf_config* cfg, lf_ctx** out);
+void lf_ctx_destroy(lf_ctx* ctx);
+
+/* Size of the proof for modulus q (16 bytes little-endian) at 2^log_vars table bits; 0 if the
+ * shape is unsupported. Replaces ProofLayout::instance (solution/proof_generate/src/main.rs:1252-1310). */
+size_t lf_proof_size(const uint8_t q_le[16], uint32_t log_vars);
+
+/* The checker's modulus gate at this shape (verifier/proof_verify/src/main.rs:85-96):
+ * LF_OK or LF_E_MODULUS. */
+int lf_accept_modulus(const uint8_t q_le[16], uint32_t log_vars);
+
+/* Expand the public matrix A for (q, 2^log_vars) and transform it to the device key; cached on
+ * the context (solution/proof_generate/src/keygen.rs:139-266, build-time key images main.rs:1712-1757). */
+int lf_key_prepare(lf_ctx* ctx, const uint8_t q_le[16], uint32_t log_vars);
+
+/* One proof of the table (host memory, table_bytes = 2^log_vars / 8, little-endian u128 words as
+ * the table file holds them) for seed and modulus q. Writes *proof_len bytes into proof.
+ * Replaces prove() + Output::write (solution/proof_generate/src/main.rs:1692-2009, 1650-1689). */
+int lf_prove(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars, const void* table,
+             size_t table_bytes, uint8_t* proof, size_t proof_cap, size_t* proof_len);
+
+/* The same with the table already resident in device memory (a device pointer of this context's
+ * device). */
+int lf_prove_device(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars,
+                    const void* table_dev, uint8_t* proof, size_t proof_cap, size_t* proof_len);
+
+/* The input table for a seed, written on the device by the table PRG (keyed BLAKE3 XOF,
+ * verifier/table_writer/src/main.rs:14-22): 2^log_vars / 8 bytes into out_dev (device memory). */
+int lf_write_table_device(lf_ctx* ctx, const uint8_t seed[32], uint32_t log_vars, void* out_dev);
+
+/* Device buffers of the context (for hosts that keep tables resident). */
+int lf_device_alloc(lf_ctx* ctx, size_t bytes, void** out_dev);
+int lf_device_free(lf_ctx* ctx, void* dev);
+int lf_memcpy_h2d(lf_ctx* ctx, void* dst_dev, const void* src, size_t bytes);
+
+int lf_last_profile(lf_ctx* ctx, lf_profile* out);
+const char* lf_strerror(int code);
+const char* lf_last_error(lf_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,712 @@
+// Host side of the prover: the C ABI, device buffers, the Fiat-Shamir transcript and the phase
+// pipeline of one proof (solution/proof_generate/src/main.rs:1692-2009; the checker's
+// reference prover verifier/proof_verify/src/reference.rs:137-177 fixes every byte).
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/labinius_gpu.h"
+#include "lf_blake3.cuh"
+#include "lf_internal.h"
+
+using namespace lf;
+
+namespace {
+
+// ---------------------------------------------------------------------------------------------
+// Shape and modulus rules (verifier/proof_verify/src/main.rs:50-96, rq.rs:17-48)
+// ---------------------------------------------------------------------------------------------
+const u128 MIN_MODULUS = 34816965049ull;
+const u128 MAX_MODULUS = (u128)1 << 96;
+
+u128 q_from_le(const uint8_t* b) {
+  u128 q = 0;
+  for (int i = 15; i >= 0; --i) q = (q << 8) | b[i];
+  return q;
+}
+uint32_t modulus_bits(u128 q) {
+  u128 x = q - 1;
+  uint32_t n = 0;
+  while (x) ++n, x >>= 1;
+  return n;
+}
+size_t coefficient_bytes(u128 q) { return (modulus_bits(q) + 7) / 8; }
+
+uint64_t fold_cap(const Shape& s) {  // main.rs:62-64, FOLD_CAP = 108 (recursion/mod.rs:81)
+  return (uint64_t)std::ceil(108.0 * (double)(((uint64_t)1 << s.lp) / 4 * RING_N));
+}
+uint64_t isqrt_u64(uint64_t x) {
+  uint64_t r = (uint64_t)std::sqrt((double)x);
+  while (r * r > x) --r;
+  while ((r + 1) * (r + 1) <= x) ++r;
+  return r;
+}
+bool accept_modulus(u128 q, const Shape& s) {
+  return q >= MIN_MODULUS && q > (u128)2 * isqrt_u64(fold_cap(s)) && q < MAX_MODULUS;
+}
+
+size_t proof_size(u128 q, const Shape& s) {
+  return 4 + 16 + 8 + coefficient_bytes(q) * COLUMNS * RING_N + 8 + 16 * 128 + 8 + 48 * (size_t)s.lp + 24 + 8 +
+         (COLUMNS * 162 + 7) / 8 + 8 + 4 * RING_N * s.ring_elements;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Transcript (solution-arm/labinius/crates/pcs/src/challenge.rs:226-341)
+// ---------------------------------------------------------------------------------------------
+struct Transcript {
+  bk::Hasher h;
+  uint64_t counter = 0;
+  void init(const char* domain) {
+    h.init();
+    counter = 0;
+    absorb_bytes(domain, strlen(domain));
+  }
+  void absorb_bytes(const void* p, size_t n) {
+    h.absorb_u64(n);
+    h.absorb((const uint8_t*)p, n);
+  }
+  void absorb_u64(uint64_t x) { h.absorb_u64(x); }
+  void absorb_b128(const b128* xs, size_t n) {
+    h.absorb_u64(n);
+    for (size_t i = 0; i < n; ++i) {
+      h.absorb_u64(xs[i].lo);
+      h.absorb_u64(xs[i].hi);
+    }
+  }
+  void absorb_f162(const f162* xs, size_t n) {
+    h.absorb_u64(n);
+    for (size_t i = 0; i < n; ++i) {
+      h.absorb_u64(xs[i].w0);
+      h.absorb_u64(xs[i].w1);
+      h.absorb_u64(xs[i].w2);
+    }
+  }
+  bk::Pending derive(const char* label) {
+    bk::Hasher c = h;
+    c.absorb_u64(counter++);
+    c.absorb_u64(strlen(label));
+    c.absorb((const uint8_t*)label, strlen(label));
+    return c.finish();
+  }
+  void fill(const char* label, uint8_t* out, size_t n) { derive(label).root_bytes(0, out, n); }
+  std::vector<b128> sample_b128(const char* label, size_t n) {
+    std::vector<uint8_t> b(16 * n);
+    fill(label, b.data(), b.size());
+    std::vector<b128> o(n);
+    memcpy(o.data(), b.data(), b.size());
+    return o;
+  }
+  std::vector<f162> sample_f162(const char* label, size_t n) {
+    std::vector<uint8_t> b(24 * n);
+    fill(label, b.data(), b.size());
+    std::vector<f162> o(n);
+    memcpy(o.data(), b.data(), b.size());
+    for (auto& x : o) x.w2 &= F162_TOP_MASK;
+    return o;
+  }
+};
+
+std::vector<b128> eq_expand_b128(const std::vector<b128>& r) {  // crossfield.rs:81-137
+  std::vector<b128> t((size_t)1 << r.size());
+  t[0] = {1, 0};
+  for (size_t round = 0; round < r.size(); ++round)
+    for (size_t i = ((size_t)1 << round); i-- > 0;) {
+      b128 hi = b128_mul(t[i], r[round]);
+      t[2 * i + 1] = hi;
+      t[2 * i] = b128_add(t[i], hi);
+    }
+  return t;
+}
+std::vector<f162> eq_expand_f162(const std::vector<f162>& r) {  // crossfield.rs:67-79
+  std::vector<f162> t(1, f162{1, 0, 0});
+  for (auto& ri : r) {
+    std::vector<f162> n;
+    n.reserve(t.size() * 2);
+    for (auto& x : t) {
+      f162 hi = f162_mul(x, ri);
+      n.push_back(f162_add(x, hi));
+      n.push_back(hi);
+    }
+    t.swap(n);
+  }
+  return t;
+}
+
+// pack_f162 (wire/mod.rs:445-452): 162 bits per element, least significant first.
+void pack_f162(const std::vector<f162>& v, uint8_t* out) {
+  size_t bytes = (v.size() * 162 + 7) / 8;
+  memset(out, 0, bytes);
+  size_t bit = 0;
+  auto put = [&](uint64_t x, int n) {
+    for (int i = 0; i < n; ++i, ++bit)
+      if ((x >> i) & 1) out[bit >> 3] |= (uint8_t)(1u << (bit & 7));
+  };
+  for (auto& x : v) put(x.w0, 64), put(x.w1, 64), put(x.w2, 34);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Device buffers
+// ---------------------------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) cap = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+struct KeyCache {
+  bool valid = false;
+  u128 q = 0;
+  uint64_t elements = 0;
+  ModulusPlan mp;
+  DevBuf key;
+};
+
+}  // namespace
+
+struct lf_ctx {
+  int device = 0;
+  int sms = 0;
+  size_t budget = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  std::string err;
+  lf_profile prof{};
+  KeyCache key;
+  bool consts_for_key = false;
+  DevBuf table, stream_buf, partial, sblk, ehi, elo, lo_planes, rhi, vparts, psi, batch, soa, msg, p0, eqt, row,
+      hasher, chal, fold, cvs, cvs_scratch, subtrees, status, phase, scratch_small;
+  uint32_t sign_key[8];
+  std::vector<uint8_t> host_fold;
+  cudaEvent_t ev[16];
+};
+
+namespace {
+
+int fail(lf_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(expr)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (expr);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? LF_E_OOM : LF_E_CUDA,                     \
+                  std::string(#expr) + ": " + cudaGetErrorString(e_));                             \
+  } while (0)
+
+// The phase table of the canonical-embedding test (challenge.rs:525-540):
+// PHASE[p][k] = exp(2 pi i p u_k / 243) over the first 81 units u_k, 88 lanes per row.
+void phase_tables(std::vector<double>& re, std::vector<double>& im) {
+  re.assign(162 * 88, 0.0);
+  im.assign(162 * 88, 0.0);
+  int units[162], n = 0;
+  for (int x = 1; x < 243; ++x)
+    if (x % 3) units[n++] = x;
+  for (int p = 0; p < 162; ++p)
+    for (int k = 0; k < 81; ++k) {
+      int m = (p * units[k]) % 243;
+      volatile double two_pi = 2.0 * M_PI;
+      double angle = two_pi * (double)m;
+      angle = angle / 243.0;
+      re[p * 88 + k] = cos(angle);
+      im[p * 88 + k] = sin(angle);
+    }
+}
+
+int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh) {
+  if (ctx->key.valid && ctx->key.q == q && ctx->key.elements == sh.ring_elements) {
+    if (!ctx->consts_for_key) {
+      upload_prime_consts(ctx->key.mp, ctx->stream);
+      ctx->consts_for_key = true;
+    }
+    return LF_OK;
+  }
+  std::string e;
+  ModulusPlan mp;
+  if (!make_modulus_plan(q, mp, e)) return fail(ctx, LF_E_MODULUS, e);
+  ctx->key.valid = false;
+  uint64_t E = sh.ring_elements;
+  DevBuf ared, leaf;
+  CK(ared.ensure((size_t)mp.nprimes * E * RING_N * 4));
+  CK(leaf.ensure((size_t)mp.nprimes * E * 4 * LEAVES * 4));
+  CK(ctx->key.key.ensure((size_t)mp.nprimes * E * LEAVES * 16 * 2));
+  upload_prime_consts(mp, ctx->stream);
+  launch_matrix_expand(mp, E, ared.as<uint32_t>(), ctx->stream);
+  launch_key_transform(mp, E, ared.as<uint32_t>(), leaf.as<uint32_t>(), ctx->key.key.as<uint16_t>(), ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  ared.release();
+  leaf.release();
+  ctx->key.mp = mp;
+  ctx->key.q = q;
+  ctx->key.elements = E;
+  ctx->key.valid = true;
+  ctx->consts_for_key = true;
+  return LF_OK;
+}
+
+float ev_ms(lf_ctx* ctx, int a, int b) {
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev[a], ctx->ev[b]);
+  return ms;
+}
+
+void put_u64(uint8_t* p, uint64_t x) { memcpy(p, &x, 8); }
+
+// The proof of one table already on the device.
+int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, const uint4* table, uint8_t* proof,
+                 size_t* proof_len) {
+  cudaStream_t st = ctx->stream;
+  const size_t width = coefficient_bytes(q);
+  const size_t commit_bytes = width * COLUMNS * RING_N;
+  const size_t plen = proof_size(q, sh);
+  // Proof layout offsets (main.rs:99-117, bincode fixint).
+  const size_t at_commit = 28;
+  const size_t at_partials = at_commit + commit_bytes + 8;
+  const size_t at_rounds = at_partials + 16 * 128 + 8;
+  const size_t at_opened = at_rounds + 48 * sh.lp;
+  const size_t at_row = at_opened + 24 + 8;
+  const size_t row_bytes = (COLUMNS * 162 + 7) / 8;
+  const size_t at_fold = at_row + row_bytes + 8;
+  const size_t fold_bytes = 4 * RING_N * sh.ring_elements;
+
+  cudaEventRecord(ctx->ev[1], st);
+  int rc = ensure_key(ctx, q, sh);
+  if (rc) return rc;
+  cudaEventRecord(ctx->ev[2], st);
+
+  // ---- commitment (K1 + K2), written after the 112 transcript prefix bytes of the stream ----
+  const int splits = commit_splits(sh.ring_elements);
+  const ModulusPlan& mp = ctx->key.mp;
+  CK(ctx->partial.ensure((size_t)splits * mp.nprimes * COLUMNS * LEAVES * 4 * 4));
+  CK(ctx->stream_buf.ensure(STREAM_PREFIX + commit_bytes + 1024));
+  launch_commit(mp, sh, table, ctx->key.key.as<uint16_t>(), ctx->partial.as<uint32_t>(), splits, st);
+  launch_commit_finish(mp, sh, ctx->partial.as<uint32_t>(), splits, ctx->stream_buf.as<uint8_t>() + STREAM_PREFIX, st);
+  CK(cudaGetLastError());
+  cudaEventRecord(ctx->ev[3], st);
+
+  // ---- transcript (main.rs:166-174): the prefix on the host, the commitment's chunks on the device ----
+  Transcript t;
+  t.init("labinius-fast/v1");
+  t.absorb_bytes(seed, 32);
+  t.absorb_u64((uint64_t)sh.log_vars);
+  t.absorb_u64((uint64_t)COLUMN_LOG);
+  uint8_t qb[16];
+  for (int i = 0; i < 16; ++i) qb[i] = (uint8_t)(q >> (8 * i));
+  t.absorb_bytes(qb, 16);
+  t.absorb_u64(commit_bytes);
+  // Everything so far is the first STREAM_PREFIX bytes of chunk 0.
+  uint8_t prefix[STREAM_PREFIX];
+  {
+    bk::Hasher probe = t.h;
+    if (probe.depth != 0 || probe.chunk.size() != STREAM_PREFIX)
+      return fail(ctx, LF_E_INTERNAL, "unexpected transcript prefix length");
+    // Rebuild the prefix bytes: domain, seed, shapes, modulus, length.
+    size_t o = 0;
+    auto u64 = [&](uint64_t x) { put_u64(prefix + o, x), o += 8; };
+    u64(16);
+    memcpy(prefix + o, "labinius-fast/v1", 16), o += 16;
+    u64(32);
+    memcpy(prefix + o, seed, 32), o += 32;
+    u64((uint64_t)sh.log_vars);
+    u64((uint64_t)COLUMN_LOG);
+    u64(16);
+    memcpy(prefix + o, qb, 16), o += 16;
+    u64(commit_bytes);
+  }
+  CK(cudaMemcpyAsync(ctx->stream_buf.p, prefix, STREAM_PREFIX, cudaMemcpyHostToDevice, st));
+  const uint64_t total = STREAM_PREFIX + commit_bytes;
+  const uint64_t nchunks = (total - 1) / 1024;
+  CK(ctx->cvs.ensure(nchunks * 32 + 32));
+  CK(ctx->cvs_scratch.ensure(2 * nchunks * 32 + 64));
+  CK(ctx->subtrees.ensure(64 * 32));
+  launch_chunk_cvs(ctx->stream_buf.as<uint8_t>(), nchunks, t.h.key, t.h.mode, ctx->cvs.as<uint32_t>(), st);
+  launch_subtrees(ctx->cvs.as<uint32_t>(), ctx->cvs_scratch.as<uint32_t>(), nchunks, t.h.key, t.h.mode,
+                  ctx->subtrees.as<uint32_t>(), st);
+  CK(cudaGetLastError());
+  uint32_t sub[64][8];
+  uint8_t tail[1024];
+  const int depth = __builtin_popcountll(nchunks);
+  const uint64_t tail_len = total - nchunks * 1024;
+  CK(cudaMemcpyAsync(sub, ctx->subtrees.p, depth * 32, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(tail, ctx->stream_buf.as<uint8_t>() + nchunks * 1024, tail_len, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(proof + at_commit, ctx->stream_buf.as<uint8_t>() + STREAM_PREFIX, commit_bytes,
+                     cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  t.h.depth = depth;
+  for (int d = 0; d < depth; ++d) memcpy(t.h.stack[d], sub[d], 32);
+  t.h.chunk.start(t.h.key, nchunks, t.h.mode);
+  t.h.chunk.absorb(tail, tail_len);
+  cudaEventRecord(ctx->ev[4], st);
+
+  // ---- point and partials (main.rs:177-189; crossfield.rs:548-573) ----
+  std::vector<b128> lo = t.sample_b128("r-lo", 7);
+  std::vector<b128> hi = t.sample_b128("r-hi", sh.lp);
+  const int LB = 12, HB = sh.lp - 12;
+  const uint64_t nblocks = 1ull << HB;
+  CK(ctx->rhi.ensure(64 * 16));
+  CK(ctx->elo.ensure(4096 * 16));
+  CK(ctx->ehi.ensure(nblocks * 16));
+  CK(ctx->lo_planes.ensure(4096 / 32 * 128 * 4));
+  CK(ctx->sblk.ensure(nblocks * 128 * 16));
+  CK(ctx->vparts.ensure(256 * 8));
+  CK(cudaMemcpyAsync(ctx->rhi.p, hi.data(), 16 * hi.size(), cudaMemcpyHostToDevice, st));
+  launch_eq_b128(ctx->rhi.as<b128>() + HB, LB, ctx->elo.as<b128>(), st);
+  launch_eq_b128(ctx->rhi.as<b128>(), HB, ctx->ehi.as<b128>(), st);
+  launch_planes_b128(ctx->elo.as<b128>(), 4096, ctx->lo_planes.as<uint32_t>(), st);
+  launch_sblock(table, nblocks, ctx->lo_planes.as<uint32_t>(), ctx->sblk.as<uint8_t>(), st);
+  CK(cudaMemsetAsync(ctx->vparts.p, 0, 256 * 8, st));
+  launch_partials_combine(ctx->ehi.as<b128>(), ctx->sblk.as<uint8_t>(), (int)nblocks,
+                          ctx->vparts.as<unsigned long long>(), st);
+  CK(cudaGetLastError());
+  std::vector<b128> partials(128);
+  CK(cudaMemcpyAsync(partials.data(), ctx->vparts.p, 128 * 16, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  cudaEventRecord(ctx->ev[5], st);
+  b128 claim = {0, 0};
+  {
+    std::vector<b128> e = eq_expand_b128(lo);
+    for (int i = 0; i < 128; ++i) claim = b128_add(claim, b128_mul(partials[i], e[i]));
+  }
+  t.absorb_b128(&claim, 1);
+  t.absorb_b128(partials.data(), 128);
+  std::vector<f162> batch = eq_expand_f162(t.sample_f162("switch-batch", 7));
+
+  // ---- switch rounds (reference.rs:150-161; sumcheck.rs:128-251) ----
+  const uint64_t n = sh.words;
+  CK(ctx->batch.ensure(128 * 24));
+  CK(ctx->psi.ensure(16 * 256 * 24));
+  CK(ctx->soa.ensure(6 * n * 8));
+  CK(ctx->msg.ensure(6 * 8));
+  CK(cudaMemcpyAsync(ctx->batch.p, batch.data(), 128 * 24, cudaMemcpyHostToDevice, st));
+  launch_psi_tables(ctx->batch.as<f162>(), ctx->psi.as<f162>(), st);
+  uint64_t* sb = ctx->soa.as<uint64_t>();
+  Soa A = {sb, sb + n, sb + 2 * n}, P = {sb + 3 * n, sb + 4 * n, sb + 5 * n};
+  launch_switch_init(table, ctx->ehi.as<b128>(), ctx->elo.as<b128>(), LB, ctx->psi.as<f162>(), A, P, n, ctx->sms, st);
+  CK(cudaGetLastError());
+  std::vector<f162> coords, rounds;
+  uint64_t half = n;
+  for (int r = 0; r < sh.lp; ++r) {
+    half >>= 1;
+    CK(cudaMemsetAsync(ctx->msg.p, 0, 48, st));
+    launch_switch_msg(A, P, half, ctx->msg.as<unsigned long long>(), ctx->sms, st);
+    f162 m[2];
+    CK(cudaMemcpyAsync(m, ctx->msg.p, 48, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    t.absorb_f162(m, 2);
+    f162 rr = t.sample_f162("switch-round", 1)[0];
+    rounds.push_back(m[0]);
+    rounds.push_back(m[1]);
+    coords.push_back(rr);
+    launch_switch_fold(A, P, half, rr, ctx->sms, st);
+  }
+  CK(cudaGetLastError());
+  f162 opened;
+  CK(cudaMemcpyAsync(&opened.w0, P.w0, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&opened.w1, P.w1, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&opened.w2, P.w2, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  cudaEventRecord(ctx->ev[6], st);
+  t.absorb_f162(&opened, 1);
+
+  // ---- row evaluation (reference.rs:163-164; main.rs:253-264) ----
+  std::vector<f162> p0(coords.rbegin(), coords.rend() - COLUMN_LOG);
+  CK(ctx->p0.ensure(64 * 24));
+  CK(ctx->eqt.ensure(sh.column_len * 24));
+  CK(ctx->row.ensure(COLUMNS * 24));
+  CK(cudaMemcpyAsync(ctx->p0.p, p0.data(), 24 * p0.size(), cudaMemcpyHostToDevice, st));
+  launch_eq_table_f162(ctx->p0.as<f162>(), sh.rl, ctx->eqt.as<f162>(), st);
+  launch_row_eval(table, sh.rl, ctx->eqt.as<f162>(), ctx->row.as<f162>(), st);
+  CK(cudaGetLastError());
+  std::vector<f162> row(COLUMNS);
+  CK(cudaMemcpyAsync(row.data(), ctx->row.p, COLUMNS * 24, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  cudaEventRecord(ctx->ev[7], st);
+  {  // RowEvaluation::absorb (scheme/commitment.rs:320-331)
+    const char* label = "labinius/row-evaluation";
+    t.absorb_bytes(label, strlen(label));
+    t.absorb_bytes(row.data(), row.size() * 24);
+  }
+
+  // ---- folding challenges (main.rs:281-292) on the device ----
+  CK(ctx->hasher.ensure(sizeof(bk::Hasher)));
+  CK(ctx->chal.ensure(COLUMNS * sizeof(Challenge)));
+  CK(ctx->status.ensure(16));
+  CK(cudaMemcpyAsync(ctx->hasher.p, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(ctx->status.p, 0, 16, st));
+  launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.as<double>(), ctx->phase.as<double>() + 162 * 88,
+                    ctx->chal.as<Challenge>(), COLUMNS, ctx->status.as<int>(), st);
+  t.counter += COLUMNS;
+  CK(cudaGetLastError());
+  cudaEventRecord(ctx->ev[8], st);
+
+  // ---- fold (reference.rs:72-133), straight into the proof's i32 region ----
+  CK(ctx->fold.ensure(fold_bytes));
+  launch_fold(table, sh.rl, sh.ring_elements, ctx->chal.as<Challenge>(), ctx->fold.as<int32_t>(),
+              ctx->status.as<int>(), st);
+  CK(cudaGetLastError());
+  cudaEventRecord(ctx->ev[9], st);
+  CK(cudaMemcpyAsync(proof + at_fold, ctx->fold.p, fold_bytes, cudaMemcpyDeviceToHost, st));
+  int status[4];
+  CK(cudaMemcpyAsync(status, ctx->status.p, 16, cudaMemcpyDeviceToHost, st));
+  cudaEventRecord(ctx->ev[10], st);
+  CK(cudaStreamSynchronize(st));
+  if (status[0] == 1) return fail(ctx, LF_E_INTERNAL, "challenge sampling exceeded its attempt bound");
+  if (status[0] == 2) return fail(ctx, LF_E_INTERNAL, "a fold coefficient does not fit the wire codec");
+
+  // ---- encode (main.rs:98-124) ----
+  uint8_t* o = proof;
+  o[0] = 1, o[1] = o[2] = o[3] = 0;
+  memcpy(o + 4, qb, 16);
+  put_u64(o + 20, commit_bytes);
+  put_u64(o + at_partials - 8, 128);
+  memcpy(o + at_partials, partials.data(), 128 * 16);
+  put_u64(o + at_rounds - 8, (uint64_t)sh.lp);
+  memcpy(o + at_rounds, rounds.data(), 48 * sh.lp);
+  memcpy(o + at_opened, &opened, 24);
+  put_u64(o + at_row - 8, row_bytes);
+  pack_f162(row, o + at_row);
+  put_u64(o + at_fold - 8, fold_bytes);
+  *proof_len = plen;
+
+  ctx->prof.key_ms = ev_ms(ctx, 1, 2);
+  ctx->prof.commit_ms = ev_ms(ctx, 2, 3);
+  ctx->prof.transcript_ms = ev_ms(ctx, 3, 4);
+  ctx->prof.partials_ms = ev_ms(ctx, 4, 5);
+  ctx->prof.switch_ms = ev_ms(ctx, 5, 6);
+  ctx->prof.row_ms = ev_ms(ctx, 6, 7);
+  ctx->prof.challenges_ms = ev_ms(ctx, 7, 8);
+  ctx->prof.fold_ms = ev_ms(ctx, 8, 9);
+  ctx->prof.download_ms = ev_ms(ctx, 9, 10);
+  return LF_OK;
+}
+
+int check_request(lf_ctx* ctx, const uint8_t* q_le, uint32_t log_vars, uint8_t* proof, size_t cap, size_t* len, u128& q,
+                  Shape& sh) {
+  if (!ctx || !q_le || !len) return fail(ctx, LF_E_ARGS, "null argument");
+  if (!sh.set(log_vars) || sh.lp < 12) return fail(ctx, LF_E_SHAPE, "unsupported LOG_VARS");
+  q = q_from_le(q_le);
+  if (!accept_modulus(q, sh)) return fail(ctx, LF_E_MODULUS, "invalid commitment modulus");
+  *len = proof_size(q, sh);
+  if (!proof || cap < *len) return fail(ctx, LF_E_CAP, "proof buffer too small");
+  return LF_OK;
+}
+
+// Table PRG (verifier/table_writer/src/main.rs:14-22): keyed BLAKE3 XOF of the context string.
+__global__ void k_table_prg(bk::Pending root, uint64_t blocks, uint4* out) {
+  uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (b >= blocks) return;
+  uint32_t w[16];
+  root.root_block(b, w);
+  out[4 * b] = make_uint4(w[0], w[1], w[2], w[3]);
+  out[4 * b + 1] = make_uint4(w[4], w[5], w[6], w[7]);
+  out[4 * b + 2] = make_uint4(w[8], w[9], w[10], w[11]);
+  out[4 * b + 3] = make_uint4(w[12], w[13], w[14], w[15]);
+}
+
+}  // namespace
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+extern "C" {
+
+int lf_ctx_create(const lf_config* cfg, lf_ctx** out) {
+  if (!out) return LF_E_ARGS;
+  *out = nullptr;
+  lf_ctx* ctx = new lf_ctx();
+  ctx->device = cfg ? cfg->device : 0;
+  ctx->budget = cfg ? cfg->hbm_budget : 0;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) {
+    delete ctx;
+    return LF_E_CUDA;
+  }
+  cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return LF_E_CUDA;
+  }
+  for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+  {
+    bk::Hasher h;
+    const char* c = "labinius 2026 challenge signs v1";
+    h.init_derive(c, (uint32_t)strlen(c));
+    memcpy(ctx->sign_key, h.key, 32);
+  }
+  std::vector<double> re, im;
+  phase_tables(re, im);
+  if (ctx->phase.ensure(2 * 162 * 88 * 8) != cudaSuccess ||
+      cudaMemcpy(ctx->phase.p, re.data(), 162 * 88 * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->phase.as<double>() + 162 * 88, im.data(), 162 * 88 * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+    lf_ctx_destroy(ctx);
+    return LF_E_CUDA;
+  }
+  *out = ctx;
+  return LF_OK;
+}
+
+void lf_ctx_destroy(lf_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  DevBuf* bufs[] = {&ctx->table, &ctx->stream_buf, &ctx->partial, &ctx->sblk, &ctx->ehi, &ctx->elo, &ctx->lo_planes,
+                    &ctx->rhi, &ctx->vparts, &ctx->psi, &ctx->batch, &ctx->soa, &ctx->msg, &ctx->p0, &ctx->eqt,
+                    &ctx->row, &ctx->hasher, &ctx->chal, &ctx->fold, &ctx->cvs, &ctx->cvs_scratch, &ctx->subtrees,
+                    &ctx->status, &ctx->phase, &ctx->scratch_small, &ctx->key.key};
+  for (DevBuf* b : bufs) b->release();
+  for (auto& ev : ctx->ev) cudaEventDestroy(ev);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+size_t lf_proof_size(const uint8_t q_le[16], uint32_t log_vars) {
+  Shape s;
+  if (!q_le || !s.set(log_vars) || s.lp < 12) return 0;
+  u128 q = q_from_le(q_le);
+  if (q < 2) return 0;
+  return proof_size(q, s);
+}
+
+int lf_accept_modulus(const uint8_t q_le[16], uint32_t log_vars) {
+  Shape s;
+  if (!q_le) return LF_E_ARGS;
+  if (!s.set(log_vars)) return LF_E_SHAPE;
+  return accept_modulus(q_from_le(q_le), s) ? LF_OK : LF_E_MODULUS;
+}
+
+int lf_key_prepare(lf_ctx* ctx, const uint8_t q_le[16], uint32_t log_vars) {
+  if (!ctx || !q_le) return LF_E_ARGS;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  Shape s;
+  if (!s.set(log_vars) || s.lp < 12) return fail(ctx, LF_E_SHAPE, "unsupported LOG_VARS");
+  u128 q = q_from_le(q_le);
+  if (!accept_modulus(q, s)) return fail(ctx, LF_E_MODULUS, "invalid commitment modulus");
+  cudaSetDevice(ctx->device);
+  return ensure_key(ctx, q, s);
+}
+
+int lf_prove_device(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars,
+                    const void* table_dev, uint8_t* proof, size_t proof_cap, size_t* proof_len) {
+  if (!ctx || !seed || !table_dev) return fail(ctx, LF_E_ARGS, "null argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  u128 q;
+  Shape sh;
+  int rc = check_request(ctx, q_le, log_vars, proof, proof_cap, proof_len, q, sh);
+  if (rc) return rc;
+  cudaSetDevice(ctx->device);
+  auto t0 = std::chrono::steady_clock::now();
+  ctx->prof = lf_profile{};
+  cudaEventRecord(ctx->ev[0], ctx->stream);
+  rc = prove_device(ctx, seed, q, sh, reinterpret_cast<const uint4*>(table_dev), proof, proof_len);
+  ctx->prof.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+
+int lf_prove(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars, const void* table,
+             size_t table_bytes, uint8_t* proof, size_t proof_cap, size_t* proof_len) {
+  if (!ctx || !seed || !table) return fail(ctx, LF_E_ARGS, "null argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  u128 q;
+  Shape sh;
+  int rc = check_request(ctx, q_le, log_vars, proof, proof_cap, proof_len, q, sh);
+  if (rc) return rc;
+  if (table_bytes != sh.words * 16) return fail(ctx, LF_E_TABLE_LEN, "witness table has the wrong length");
+  cudaSetDevice(ctx->device);
+  auto t0 = std::chrono::steady_clock::now();
+  ctx->prof = lf_profile{};
+  CK(ctx->table.ensure(table_bytes));
+  cudaEventRecord(ctx->ev[0], ctx->stream);
+  CK(cudaMemcpyAsync(ctx->table.p, table, table_bytes, cudaMemcpyHostToDevice, ctx->stream));
+  rc = prove_device(ctx, seed, q, sh, ctx->table.as<uint4>(), proof, proof_len);
+  ctx->prof.upload_ms = ev_ms(ctx, 0, 1);
+  ctx->prof.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+
+int lf_write_table_device(lf_ctx* ctx, const uint8_t seed[32], uint32_t log_vars, void* out_dev) {
+  if (!ctx || !seed || !out_dev) return LF_E_ARGS;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  Shape s;
+  if (!s.set(log_vars)) return fail(ctx, LF_E_SHAPE, "unsupported LOG_VARS");
+  cudaSetDevice(ctx->device);
+  bk::Hasher h;
+  h.init_keyed(seed);
+  const char* c = "labinius-fast/binary-table/v1";
+  h.absorb((const uint8_t*)c, strlen(c));
+  bk::Pending root = h.finish();
+  uint64_t blocks = (s.words * 16) / 64;
+  k_table_prg<<<(unsigned)((blocks + 255) / 256), 256, 0, ctx->stream>>>(root, blocks, reinterpret_cast<uint4*>(out_dev));
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return LF_OK;
+}
+
+int lf_device_alloc(lf_ctx* ctx, size_t bytes, void** out_dev) {
+  if (!ctx || !out_dev) return LF_E_ARGS;
+  cudaSetDevice(ctx->device);
+  CK(cudaMalloc(out_dev, bytes));
+  return LF_OK;
+}
+int lf_device_free(lf_ctx* ctx, void* dev) {
+  if (!ctx) return LF_E_ARGS;
+  cudaSetDevice(ctx->device);
+  CK(cudaFree(dev));
+  return LF_OK;
+}
+int lf_memcpy_h2d(lf_ctx* ctx, void* dst_dev, const void* src, size_t bytes) {
+  if (!ctx || !dst_dev || !src) return LF_E_ARGS;
+  cudaSetDevice(ctx->device);
+  CK(cudaMemcpy(dst_dev, src, bytes, cudaMemcpyHostToDevice));
+  return LF_OK;
+}
+
+int lf_last_profile(lf_ctx* ctx, lf_profile* out) {
+  if (!ctx || !out) return LF_E_ARGS;
+  *out = ctx->prof;
+  return LF_OK;
+}
+
+const char* lf_strerror(int code) {
+  switch (code) {
+    case LF_OK: return "ok";
+    case LF_E_ARGS: return "invalid argument";
+    case LF_E_SHAPE: return "unsupported shape";
+    case LF_E_MODULUS: return "invalid commitment modulus";
+    case LF_E_TABLE_LEN: return "witness table has the wrong length";
+    case LF_E_CAP: return "proof buffer too small";
+    case LF_E_OOM: return "device memory exhausted";
+    case LF_E_CUDA: return "CUDA error";
+    case LF_E_INTERNAL: return "internal check failed";
+    case LF_E_ADMISSION: return "request exceeds the HBM budget";
+    default: return "unknown error";
+  }
+}
+
+const char* lf_last_error(lf_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+}  // extern "C"

@@ -1,0 +1,137 @@
+// Internal declarations shared by the prover's translation units (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "lf_field.cuh"
+
+namespace lf {
+
+typedef unsigned __int128 u128;
+
+constexpr int RING_N = 648;      // degree of R_Q = Z_Q[X]/(X^648 - X^324 + 1)
+constexpr int LEAVES = 162;      // slots of the transform over Y = X^4
+constexpr int COLUMN_LOG = 10;   // verifier/proof_verify/src/main.rs:37
+constexpr int COLUMNS = 1 << COLUMN_LOG;
+constexpr int MAX_PRIMES = 12;
+constexpr int STREAM_PREFIX = 112;  // transcript bytes before the commitment (see host code)
+
+// The shape of one instance, derived from LOG_VARS (main.rs:32-46).
+struct Shape {
+  int log_vars = 0, lp = 0, rl = 0;
+  size_t words = 0, column_len = 0, ring_elements = 0;
+  bool set(uint32_t l) {
+    if (l < 19 || l > 34) return false;
+    log_vars = (int)l;
+    lp = log_vars - 7;
+    rl = lp - COLUMN_LOG;
+    words = (size_t)1 << lp;
+    column_len = (size_t)1 << rl;
+    ring_elements = column_len / 4;
+    return true;
+  }
+};
+
+// One transform prime p = 1 (mod 486): the 162-point transform of Z_p[Y]/(Y^162 - Y^81 + 1).
+struct PrimePlan {
+  uint32_t p;
+  uint32_t eta;                 // primitive 486th root of unity
+  std::vector<uint32_t> pw;     // eta^i, i < 486
+  // Node exponents (in powers of eta) of the 80 internal radix-3 nodes, level by level:
+  // level 1: 2 nodes (length 81), level 2: 6 (27), level 3: 18 (9), level 4: 54 (3).
+  std::vector<uint32_t> node_e[5];
+  uint32_t leaf_e[LEAVES];      // slot s holds the evaluation at Y = eta^leaf_e[s]
+};
+bool make_plan(uint32_t p, PrimePlan& out);
+
+// Device-side constants of one prime, uploaded once per modulus.
+struct PrimeConst {
+  uint32_t p, bar;                 // bar = floor(2^32 / p)
+  uint32_t om, om_s;               // cube root of unity eta^162 and its Shoup companion
+  uint32_t tw[6][13][2];           // forward twiddles of the 13 nodes inside a sub-block
+  uint32_t tws[6][13][2];          // Shoup companions
+  uint32_t T[6][32];               // fused first two levels on 5 input bits
+  uint32_t itw[80][2];             // inverse twiddles eta^-(e/3), eta^-(2e/3) per internal node
+  uint32_t inv3, iom, iom2;        // 1/3, omega^-1, omega^-2
+  uint32_t w, w5, inv_split;       // eta^81, eta^405, 1/(eta^81 - eta^405)
+  uint32_t fw[80][2];              // forward twiddles per internal node (key transform)
+  uint32_t leaf_root[LEAVES];      // eta^leaf_e[s]
+};
+
+struct ModulusPlan {
+  u128 q = 0;
+  uint32_t width = 0, bits = 0;    // coefficient bytes and bits (rq.rs:40-48)
+  int nprimes = 0;
+  uint32_t primes[MAX_PRIMES];
+  bool exact_lift = false;         // true: CRT gives the integer product, reduced mod q after
+  std::vector<PrimeConst> consts;
+  // Garner constants: inv[i][j] = p_j^-1 mod p_i for j < i
+  uint32_t garner_inv[MAX_PRIMES][MAX_PRIMES];
+};
+bool make_modulus_plan(u128 q, ModulusPlan& mp, std::string& err);
+
+struct ProveProfile {
+  double key_ms, commit_ms, finish_ms, transcript_ms, partials_ms, switch_ms, row_ms, challenges_ms,
+      fold_ms, encode_ms, total_ms;
+};
+
+// Three limb arrays of F162 values (structure of arrays, coalesced per limb).
+struct Soa {
+  uint64_t *w0, *w1, *w2;
+#ifdef __CUDACC__
+  __device__ __forceinline__ f162 get(uint64_t i) const { return {w0[i], w1[i], w2[i]}; }
+  __device__ __forceinline__ void put(uint64_t i, f162 v) const { w0[i] = v.w0, w1[i] = v.w1, w2[i] = v.w2; }
+#endif
+};
+
+// A short challenge (challenge.rs:407-415): sorted positions, sign bits, weight.
+struct Challenge {
+  uint8_t positions[32];
+  uint32_t signs;
+  uint32_t weight;
+};
+
+// ---- launch wrappers (lf_switch.cu) ----
+void launch_eq_b128(const b128* r, int n, b128* out, cudaStream_t s);
+void launch_eq_table_f162(const f162* ps, int n, f162* out, cudaStream_t s);
+void launch_planes_b128(const b128* x, uint64_t n, uint32_t* planes, cudaStream_t s);
+void launch_sblock(const uint4* table, uint64_t nblocks, const uint32_t* lo_planes, uint8_t* sblk, cudaStream_t s);
+void launch_partials_combine(const b128* ehi, const uint8_t* sblk, int nblocks, unsigned long long* v, cudaStream_t s);
+void launch_psi_tables(const f162* batch, f162* tab, cudaStream_t s);
+void launch_switch_init(const uint4* table, const b128* ehi, const b128* elo, int lb, const f162* psi, Soa a, Soa p,
+                        uint64_t n, int sms, cudaStream_t s);
+void launch_switch_msg(Soa a, Soa p, uint64_t half, unsigned long long* msg, int sms, cudaStream_t s);
+void launch_switch_fold(Soa a, Soa p, uint64_t half, f162 r, int sms, cudaStream_t s);
+
+// ---- launch wrappers (lf_open.cu) ----
+void launch_row_eval(const uint4* table, int rl, const f162* eqt, f162* row, cudaStream_t s);
+struct HasherImage;  // a bk::Hasher copied to the device
+void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint32_t sign_key[8], const double* phase_re,
+                       const double* phase_im, Challenge* out, int n, int* status, cudaStream_t s);
+void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Challenge* ch, int32_t* out, int* status,
+                 cudaStream_t s);
+void launch_chunk_cvs(const uint8_t* stream, uint64_t nchunks, const uint32_t key[8], uint32_t mode, uint32_t* cvs,
+                      cudaStream_t s);
+// Reduce nchunks chunk values to the chaining values of the complete subtrees of the stream
+// (largest first, sizes = set bits of nchunks); returns them in out (at most 64 x 8 words).
+void launch_subtrees(uint32_t* cvs, uint32_t* scratch, uint64_t nchunks, const uint32_t key[8], uint32_t mode,
+                     uint32_t* out, cudaStream_t s);
+
+// ---- launch wrappers (lf_commit.cu) ----
+void upload_prime_consts(const ModulusPlan& mp, cudaStream_t s);
+// The public matrix reduced modulo each prime: ared[prime][m][648].
+void launch_matrix_expand(const ModulusPlan& mp, uint64_t elements, uint32_t* ared, cudaStream_t s);
+// Leaf-form key: key[prime][m][162][16] u16.
+void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32_t* ared, uint32_t* leafvals,
+                          uint16_t* key, cudaStream_t s);
+int commit_splits(uint64_t elements);
+void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint16_t* key,
+                   uint32_t* partial, int splits, cudaStream_t s);
+void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t* partial, int splits,
+                          uint8_t* out, cudaStream_t s);
+
+}  // namespace lf

@@ -1,0 +1,378 @@
+// The opening on the GPU: row evaluation, folding challenges, the fold, and the BLAKE3 tree
+// hashing of the transcript's large absorb.
+#include <cstdio>
+
+#include "lf_blake3.cuh"
+#include "lf_internal.h"
+
+namespace lf {
+
+// ---------------------------------------------------------------------------------------------
+// Row evaluation (verifier/proof_verify/src/reference.rs:50-70; eval.rs:173-185):
+// u_j = sum_i eq_table(p0)[i] * lift(W[i + COLUMN_LEN j]). One block per column.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ f162 shfl_xor_f162(f162 v, int m) {
+  v.w0 ^= __shfl_xor_sync(0xffffffffu, v.w0, m);
+  v.w1 ^= __shfl_xor_sync(0xffffffffu, v.w1, m);
+  v.w2 ^= __shfl_xor_sync(0xffffffffu, v.w2, m);
+  return v;
+}
+
+__global__ void __launch_bounds__(256) k_row_eval(const uint4* __restrict__ table, int rl, const f162* __restrict__ eqt,
+                                                  f162* __restrict__ row) {
+  const int col = blockIdx.x;
+  const uint64_t n = 1ull << rl;
+  const uint4* w = table + ((uint64_t)col << rl);
+  f162 acc = {0, 0, 0};
+  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    uint4 x = w[i];
+    b128 b = {(uint64_t)x.x | ((uint64_t)x.y << 32), (uint64_t)x.z | ((uint64_t)x.w << 32)};
+    acc = f162_add(acc, f162_mul_lifted(eqt[i], b));
+  }
+  for (int m = 16; m; m >>= 1) acc = shfl_xor_f162(acc, m);
+  __shared__ f162 part[8];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    f162 s = {0, 0, 0};
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s = f162_add(s, part[i]);
+    row[col] = s;
+  }
+}
+
+void launch_row_eval(const uint4* table, int rl, const f162* eqt, f162* row, cudaStream_t s) {
+  k_row_eval<<<COLUMNS, 256, 0, s>>>(table, rl, eqt, row);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Folding challenges (challenge.rs:343-755). One warp per challenge. The XOF of derivation
+// base + i of the transcript is read as a byte stream; an attempt is a partial Fisher-Yates over
+// the 162 positions driven by little-endian u16 draws, the positions sorted, signed by a keyed
+// hash of the position set, and accepted when every one of the 81 phase lanes keeps
+// re^2 + im^2 <= bound_sq (f64, round-to-nearest, no fused multiply-add).
+// ---------------------------------------------------------------------------------------------
+constexpr int CH_WARPS = 4;
+constexpr int XOF_BUF = 32 * 64;
+constexpr int N162 = 162;
+constexpr int WEIGHT = 28;
+constexpr int PHASE_LANES = 88;
+constexpr uint64_t MAX_ATTEMPTS = 1ull << 22;
+
+struct ChWarp {
+  uint8_t buf[XOF_BUF];
+  uint8_t perm[176];
+  uint32_t root[27];
+};
+
+__device__ __forceinline__ void xof_refill(ChWarp& s, const bk::Pending& root, uint64_t& next_block, int lane) {
+  uint32_t w[16];
+  root.root_block(next_block + lane, w);
+  uint32_t* dst = reinterpret_cast<uint32_t*>(s.buf + 64 * lane);
+#pragma unroll
+  for (int i = 0; i < 16; ++i) dst[i] = w[i];
+  next_block += 32;
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(32 * CH_WARPS) k_challenges(const bk::Hasher* __restrict__ state, uint64_t base,
+                                                              bk::Pending sign_key_node, const double* __restrict__ re,
+                                                              const double* __restrict__ im, double bound_sq,
+                                                              Challenge* __restrict__ out, int n, int* status) {
+  __shared__ ChWarp sw[CH_WARPS];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int ci = blockIdx.x * CH_WARPS + wid;
+  if (ci >= n) return;
+  ChWarp& s = sw[wid];
+  if (lane == 0) {
+    bk::Hasher h = *state;
+    h.absorb_u64(base + (uint64_t)ci);
+    const char label[] = "short-challenge";
+    h.absorb_u64(sizeof(label) - 1);
+    h.absorb((const uint8_t*)label, sizeof(label) - 1);
+    bk::Pending r = h.finish();
+    for (int i = 0; i < 8; ++i) s.root[i] = r.h[i];
+    for (int i = 0; i < 16; ++i) s.root[8 + i] = r.m[i];
+    s.root[24] = (uint32_t)r.t;
+    s.root[25] = r.len;
+    s.root[26] = r.flags;
+  }
+  __syncwarp();
+  bk::Pending root;
+  for (int i = 0; i < 8; ++i) root.h[i] = s.root[i];
+  for (int i = 0; i < 16; ++i) root.m[i] = s.root[8 + i];
+  root.t = s.root[24];
+  root.len = s.root[25];
+  root.flags = s.root[26];
+  uint64_t next_block = 0;
+  int pos = XOF_BUF;
+  auto byte = [&]() -> uint32_t {
+    if (pos == XOF_BUF) {
+      xof_refill(s, root, next_block, lane);
+      pos = 0;
+    }
+    return s.buf[pos++];
+  };
+  for (uint64_t attempt = 0; attempt < MAX_ATTEMPTS; ++attempt) {
+    for (int i = lane; i < N162; i += 32) s.perm[i] = (uint8_t)i;
+    __syncwarp();
+    for (int i = 0; i < WEIGHT; ++i) {
+      const uint32_t nn = (uint32_t)(N162 - i);
+      const uint32_t limit = (65536u / nn) * nn;
+      const uint64_t magic = (1ull << 32) / nn + 1;
+      uint32_t r;
+      do {
+        uint32_t lo = byte();
+        uint32_t hi = byte();
+        r = lo | (hi << 8);
+      } while (r >= limit);
+      uint32_t q = (uint32_t)(((uint64_t)r * magic) >> 32);
+      int j = i + (int)(r - q * nn);
+      if (lane == 0) {
+        uint8_t t = s.perm[i];
+        s.perm[i] = s.perm[j];
+        s.perm[j] = t;
+      }
+      __syncwarp();
+    }
+    // Sorted positions: lane l < 28 places perm[l] by its rank.
+    uint32_t mine = lane < WEIGHT ? s.perm[lane] : 255;
+    int rank = 0;
+    for (int t = 0; t < WEIGHT; ++t) rank += (int)(s.perm[t] < mine);
+    __syncwarp();
+    __shared__ uint8_t sorted[CH_WARPS][32];
+    if (lane < WEIGHT) sorted[wid][rank] = (uint8_t)mine;
+    __syncwarp();
+    // Signs: derive-key hash of (weight as u64 LE || positions), first four bytes LE.
+    uint32_t signs = 0;
+    if (lane == 0) {
+      uint8_t blk[64];
+      for (int i = 0; i < 64; ++i) blk[i] = 0;
+      blk[0] = (uint8_t)WEIGHT;
+      for (int i = 0; i < WEIGHT; ++i) blk[8 + i] = sorted[wid][i];
+      uint32_t m[16], o[16];
+      bk::load_words(blk, m, 16);
+      bk::compress16(sign_key_node.h, m, 0, 8 + WEIGHT, sign_key_node.flags | bk::F_ROOT, o);
+      signs = o[0] & ((1u << WEIGHT) - 1);
+    }
+    signs = __shfl_sync(0xffffffffu, signs, 0);
+    bool over = false;
+    for (int k = lane; k < 81; k += 32) {
+      double vr = 0.0, vi = 0.0;
+      for (int t = 0; t < WEIGHT; ++t) {
+        int b = sorted[wid][t] * PHASE_LANES + k;
+        double pr = re[b], pi = im[b];
+        if ((signs >> t) & 1) pr = -pr, pi = -pi;
+        vr = __dadd_rn(vr, pr);
+        vi = __dadd_rn(vi, pi);
+      }
+      double m2 = __dadd_rn(__dmul_rn(vr, vr), __dmul_rn(vi, vi));
+      over |= m2 > bound_sq;
+    }
+    if (!__any_sync(0xffffffffu, over)) {
+      if (lane < WEIGHT) out[ci].positions[lane] = sorted[wid][lane];
+      else out[ci].positions[lane] = 0;
+      if (lane == 0) {
+        out[ci].signs = signs;
+        out[ci].weight = WEIGHT;
+      }
+      return;
+    }
+    __syncwarp();
+  }
+  if (lane == 0) atomicExch(status, 1);
+}
+
+void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint32_t sign_key[8], const double* phase_re,
+                       const double* phase_im, Challenge* out, int n, int* status, cudaStream_t s) {
+  bk::Pending sk;
+  for (int i = 0; i < 8; ++i) sk.h[i] = sign_key[i];
+  for (int i = 0; i < 16; ++i) sk.m[i] = 0;
+  sk.t = 0;
+  sk.len = 0;
+  sk.flags = bk::F_DERIVE_MAT | bk::F_CHUNK_START | bk::F_CHUNK_END;
+  const double bound_sq = 12.0 * 12.0 + 1e-12;
+  k_challenges<<<(n + CH_WARPS - 1) / CH_WARPS, 32 * CH_WARPS, 0, s>>>(
+      reinterpret_cast<const bk::Hasher*>(hasher_dev), base_counter, sk, phase_re, phase_im, bound_sq, out, n, status);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Fold (reference.rs:72-133): v_m = sum_j c_j W_{j,m} over the integers. A challenge sits in R_648
+// as c(-X^4), so with Y = X^4 each table word k of element m is folded on its own:
+// V_{m,k}(Y) = sum_j sum_t s_{j,t} Y^{pos_{j,t}} W_{j,m,k}(Y), s = sign bit XOR (pos odd), then
+// Y^162 = Y^81 - 1. Bit-sliced: a block handles 8 elements (32 words, one per bit of a u32),
+// thread y owns raw position y (0..288) as a 16-plane two's-complement counter.
+// ---------------------------------------------------------------------------------------------
+constexpr int FOLD_ELEMS = 8;
+constexpr int FOLD_THREADS = 320;
+constexpr int FOLD_BATCH = FOLD_THREADS / 32;  // columns transposed per step, one per warp
+constexpr int RAW_Y = 128 + 161;               // 289 raw positions
+
+__global__ void __launch_bounds__(FOLD_THREADS) k_fold(const uint4* __restrict__ table, int rl,
+                                                      const Challenge* __restrict__ ch, int32_t* __restrict__ out,
+                                                      int* status) {
+  __shared__ uint32_t vec[FOLD_BATCH][128];
+  __shared__ uint8_t cpos[FOLD_BATCH][32];
+  __shared__ uint32_t csign[FOLD_BATCH];
+  __shared__ int32_t raw[32][RAW_Y + 1];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint64_t m0 = (uint64_t)blockIdx.x * FOLD_ELEMS;
+  uint32_t P[16];
+#pragma unroll
+  for (int b = 0; b < 16; ++b) P[b] = 0;
+  for (int j0 = 0; j0 < COLUMNS; j0 += FOLD_BATCH) {
+    const int j = j0 + warp;
+    if (j < COLUMNS) {
+      uint4 v = table[((uint64_t)j << rl) + 4 * m0 + lane];
+      uint32_t keep[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int b = 0; b < 128; ++b) {
+        uint32_t word = b < 32 ? v.x : b < 64 ? v.y : b < 96 ? v.z : v.w;
+        uint32_t m = __ballot_sync(0xffffffffu, (word >> (b & 31)) & 1);
+        if (lane == (b & 31)) keep[b >> 5] = m;
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) vec[warp][32 * i + lane] = keep[i];
+      cpos[warp][lane] = ch[j].positions[lane];
+      if (lane == 0) csign[warp] = ch[j].signs;
+    }
+    __syncthreads();
+    if (tid < RAW_Y) {
+      const int nb = min(FOLD_BATCH, COLUMNS - j0);
+      for (int c = 0; c < nb; ++c) {
+        const uint32_t sg = csign[c];
+        for (int t = 0; t < WEIGHT; ++t) {
+          const int pos = cpos[c][t];
+          const int p = tid - pos;
+          if ((unsigned)p >= 128u) continue;
+          uint32_t x = vec[c][p];
+          if (!x) continue;
+          const bool neg = (((sg >> t) & 1) ^ (pos & 1)) != 0;
+          if (neg) {
+#pragma unroll
+            for (int b = 0; b < 16; ++b) {
+              uint32_t t2 = ~P[b] & x;
+              P[b] ^= x;
+              x = t2;
+              if (!x) break;
+            }
+          } else {
+#pragma unroll
+            for (int b = 0; b < 16; ++b) {
+              uint32_t t2 = P[b] & x;
+              P[b] ^= x;
+              x = t2;
+              if (!x) break;
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (tid < RAW_Y) {
+    for (int l = 0; l < 32; ++l) {
+      int32_t v = 0;
+#pragma unroll
+      for (int b = 0; b < 16; ++b) v |= (int32_t)((P[b] >> l) & 1) << b;
+      v = (v ^ 0x8000) - 0x8000;
+      raw[l][tid] = v;
+    }
+  }
+  __syncthreads();
+  if (tid < 32) {
+    int32_t* r = raw[tid];
+    for (int y = RAW_Y - 1; y >= N162; --y) {
+      int32_t v = r[y];
+      r[y - 81] += v;
+      r[y - N162] -= v;
+    }
+  }
+  __syncthreads();
+  for (int idx = tid; idx < FOLD_ELEMS * 648; idx += FOLD_THREADS) {
+    const int m = idx / 648, c = idx % 648, y = c >> 2, k = c & 3;
+    const int32_t v = raw[4 * m + k][y];
+    if (v < -32768 || v > 32767) atomicExch(status, 2);
+    out[(m0 + m) * 648 + c] = v;
+  }
+}
+
+void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Challenge* ch, int32_t* out, int* status,
+                 cudaStream_t s) {
+  k_fold<<<(unsigned)(ring_elements / FOLD_ELEMS), FOLD_THREADS, 0, s>>>(table, rl, ch, out, status);
+}
+
+// ---------------------------------------------------------------------------------------------
+// BLAKE3 tree hashing of a stream (the transcript's commitment absorb, challenge.rs:152-223).
+// ---------------------------------------------------------------------------------------------
+struct KeyArg {
+  uint32_t k[8];
+};
+
+__global__ void k_chunk_cvs(const uint8_t* __restrict__ stream, uint64_t nchunks, KeyArg key, uint32_t mode,
+                            uint32_t* __restrict__ cvs) {
+  uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (c >= nchunks) return;
+  const uint4* src = reinterpret_cast<const uint4*>(stream + c * 1024);
+  uint32_t h[8];
+  for (int i = 0; i < 8; ++i) h[i] = key.k[i];
+  for (int b = 0; b < 16; ++b) {
+    uint32_t m[16];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      uint4 v = src[4 * b + i];
+      m[4 * i] = v.x, m[4 * i + 1] = v.y, m[4 * i + 2] = v.z, m[4 * i + 3] = v.w;
+    }
+    uint32_t f = mode | (b == 0 ? bk::F_CHUNK_START : 0) | (b == 15 ? bk::F_CHUNK_END : 0);
+    uint32_t o[16];
+    bk::compress16(h, m, c, 64, f, o);
+    for (int i = 0; i < 8; ++i) h[i] = o[i];
+  }
+  for (int i = 0; i < 8; ++i) cvs[c * 8 + i] = h[i];
+}
+
+__global__ void __launch_bounds__(1024) k_subtrees(const uint32_t* __restrict__ cvs, uint32_t* scratch, uint64_t nchunks,
+                                                   KeyArg key, uint32_t mode, uint32_t* __restrict__ out) {
+  uint32_t* bufA = scratch;
+  uint32_t* bufB = scratch + nchunks * 8;
+  uint64_t off = 0;
+  int d = 0;
+  for (int bit = 63; bit >= 0; --bit) {
+    uint64_t size = 1ull << bit;
+    if (!(nchunks & size)) continue;
+    const uint32_t* src = cvs + off * 8;
+    uint32_t* dst = bufA;
+    uint64_t cnt = size;
+    while (cnt > 1) {
+      for (uint64_t i = threadIdx.x; i < cnt / 2; i += blockDim.x) {
+        uint32_t l[8], r[8], o[8];
+        for (int k = 0; k < 8; ++k) l[k] = src[(2 * i) * 8 + k], r[k] = src[(2 * i + 1) * 8 + k];
+        bk::parent(l, r, key.k, mode, o);
+        for (int k = 0; k < 8; ++k) dst[i * 8 + k] = o[k];
+      }
+      __syncthreads();
+      cnt /= 2;
+      src = dst;
+      dst = (dst == bufA) ? bufB : bufA;
+    }
+    if (threadIdx.x < 8) out[d * 8 + threadIdx.x] = src[threadIdx.x];
+    __syncthreads();
+    ++d;
+    off += size;
+  }
+}
+
+void launch_chunk_cvs(const uint8_t* stream, uint64_t nchunks, const uint32_t key[8], uint32_t mode, uint32_t* cvs,
+                      cudaStream_t s) {
+  KeyArg k;
+  for (int i = 0; i < 8; ++i) k.k[i] = key[i];
+  if (nchunks) k_chunk_cvs<<<(unsigned)((nchunks + 127) / 128), 128, 0, s>>>(stream, nchunks, k, mode, cvs);
+}
+
+void launch_subtrees(uint32_t* cvs, uint32_t* scratch, uint64_t nchunks, const uint32_t key[8], uint32_t mode,
+                     uint32_t* out, cudaStream_t s) {
+  KeyArg k;
+  for (int i = 0; i < 8; ++i) k.k[i] = key[i];
+  if (nchunks) k_subtrees<<<1, 1024, 0, s>>>(cvs, scratch, nchunks, k, mode, out);
+}
+
+}  // namespace lf

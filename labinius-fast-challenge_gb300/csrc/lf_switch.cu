@@ -1,0 +1,267 @@
+// The GHASH -> F162 field switch on the GPU: eq tables, the 128 partial evaluations, and the
+// sumcheck rounds (solution-arm/labinius/crates/pcs/src/fields/crossfield.rs:66-170, 548-701;
+// fields/sumcheck.rs:128-251).
+//
+// Partials. v[k] = sum_j bit_k(pi0[j]) eq[j] with eq[j] = E_hi[j >> 12] * E_lo[j & 4095]
+// (eq over the leading and the trailing 12 coordinates of r_hi; r_hi[0] is the most significant
+// index bit, crossfield.rs:126-137). Writing T_h[b'] = sum_jl bit_b'(E_lo[jl]) pi0[h, jl] (a
+// GF(2) product of bit planes, no field multiplication) gives
+// v[k] = sum_h E_hi[h] * S_h[k] with S_h[k] = sum_jl bit_k(pi0[h, jl]) E_lo[jl] = column k of T_h.
+// So the table pass is a 128 x 4096 by 4096 x 128 bit-matrix product per block of 4096 words,
+// done with AND/XOR on 32-bit planes and a final parity, and only 128 * 2^(LP-12) GHASH products
+// remain.
+#include <cstdio>
+
+#include "lf_internal.h"
+
+namespace lf {
+
+// ---------------------------------------------------------------------------------------------
+// eq tables
+// ---------------------------------------------------------------------------------------------
+// eq_expand_b128 (crossfield.rs:81-137): r[0] is the most significant bit of the index.
+__global__ void k_eq_b128(const b128* __restrict__ r, int n, b128* __restrict__ out) {
+  uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (j >= (1ull << n)) return;
+  b128 v = {1, 0};
+  for (int i = 0; i < n; ++i) {
+    b128 f = r[i];
+    if (!((j >> (n - 1 - i)) & 1)) f.lo ^= 1;
+    v = b128_mul(v, f);
+  }
+  out[j] = v;
+}
+
+// eq_table (eval.rs:50-85): variable k is bit k of the index.
+__global__ void k_eq_table_f162(const f162* __restrict__ ps, int n, f162* __restrict__ out) {
+  uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (j >= (1ull << n)) return;
+  f162 v = {1, 0, 0};
+  for (int k = 0; k < n; ++k) {
+    f162 f = ps[k];
+    if (!((j >> k) & 1)) f.w0 ^= 1;
+    v = f162_mul(v, f);
+  }
+  out[j] = v;
+}
+
+// Bit planes of B128 values, word-major: planes[w * 128 + b] holds bit b of entries 32w..32w+31.
+__global__ void k_planes_b128(const b128* __restrict__ x, uint64_t n, uint32_t* __restrict__ planes) {
+  uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (w * 32 >= n) return;
+  b128 v = x[w * 32 + lane];
+  uint32_t keep[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int b = 0; b < 128; ++b) {
+    uint32_t bit = b < 64 ? (uint32_t)(v.lo >> b) & 1 : (uint32_t)(v.hi >> (b - 64)) & 1;
+    uint32_t m = __ballot_sync(0xffffffffu, bit);
+    if (lane == (b & 31)) keep[b >> 5] = m;
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) planes[w * 128 + 32 * i + lane] = keep[i];
+}
+
+// ---------------------------------------------------------------------------------------------
+// S blocks: sblk[h][c] (16 bytes, bit b) = parity sum_jl bit_c(pi0[h, jl]) bit_b(E_lo[jl]).
+// One block of 256 threads per h; 4096 words = 128 plane words of 32 entries.
+// ---------------------------------------------------------------------------------------------
+constexpr int SB_W = 128;  // plane words per block (4096 entries)
+
+__global__ void __launch_bounds__(256, 1) k_sblock(const uint4* __restrict__ table, const uint32_t* __restrict__ lo_planes,
+                                                    uint8_t* __restrict__ sblk) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  uint32_t* sP = smem;                 // [SB_W][128]
+  uint32_t* sL = smem + SB_W * 128;    // [SB_W][128]
+  const int h = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(lo_planes);
+    uint4* dst = reinterpret_cast<uint4*>(sL);
+    for (int i = threadIdx.x; i < SB_W * 32; i += 256) dst[i] = src[i];
+  }
+  const uint4* blk = table + (size_t)h * SB_W * 32;
+  for (int w = warp; w < SB_W; w += 8) {
+    uint4 v = blk[w * 32 + lane];
+    uint32_t keep[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int b = 0; b < 128; ++b) {
+      uint32_t word = b < 32 ? v.x : b < 64 ? v.y : b < 96 ? v.z : v.w;
+      uint32_t m = __ballot_sync(0xffffffffu, (word >> (b & 31)) & 1);
+      if (lane == (b & 31)) keep[b >> 5] = m;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) sP[w * 128 + 32 * i + lane] = keep[i];
+  }
+  __syncthreads();
+  const int cb = threadIdx.x >> 4, bb = threadIdx.x & 15;
+  uint32_t acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0;
+#pragma unroll 2
+  for (int w = 0; w < SB_W; ++w) {
+    const uint4* pp = reinterpret_cast<const uint4*>(sP + w * 128 + 8 * cb);
+    const uint4* lp = reinterpret_cast<const uint4*>(sL + w * 128 + 8 * bb);
+    uint4 p0 = pp[0], p1 = pp[1], l0 = lp[0], l1 = lp[1];
+    uint32_t pv[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+    uint32_t lv[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] ^= pv[i] & lv[j];
+  }
+  uint8_t* out = sblk + (size_t)h * 128 * 16;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    uint32_t byte = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) byte |= (__popc(acc[i][j]) & 1u) << j;
+    out[(8 * cb + i) * 16 + bb] = (uint8_t)byte;
+  }
+}
+
+// v[c] = sum_h E_hi[h] * S_h[c]: block of 128 threads (one per c) over a run of h.
+__global__ void k_partials_combine(const b128* __restrict__ ehi, const uint8_t* __restrict__ sblk, int nblocks, int run,
+                                   unsigned long long* __restrict__ v) {
+  const int c = threadIdx.x;
+  const int h0 = blockIdx.x * run;
+  b128 acc = {0, 0};
+  for (int h = h0; h < min(nblocks, h0 + run); ++h) {
+    const uint64_t* s = reinterpret_cast<const uint64_t*>(sblk + ((size_t)h * 128 + c) * 16);
+    b128 sv = {s[0], s[1]};
+    acc = b128_add(acc, b128_mul(ehi[h], sv));
+  }
+  atomicXor(&v[2 * c], (unsigned long long)acc.lo);
+  atomicXor(&v[2 * c + 1], (unsigned long long)acc.hi);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Switch, first version: a and p materialised (SoA limbs), rounds by field products.
+// ---------------------------------------------------------------------------------------------
+// psi_table (crossfield.rs:150-161): tab[c][m] = sum_{b in m} batch[8c + b].
+__global__ void k_psi_tables(const f162* __restrict__ batch, f162* __restrict__ tab) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= 16 * 256) return;
+  int c = e >> 8, m = e & 255;
+  f162 v = {0, 0, 0};
+  for (int b = 0; b < 8; ++b)
+    if ((m >> b) & 1) v = f162_add(v, batch[8 * c + b]);
+  tab[e] = v;
+}
+
+// a[j] = psi(E_hi[j >> lb] * E_lo[j & mask]), p[j] = lift(pi0[j]).
+__global__ void __launch_bounds__(256) k_switch_init(const uint4* __restrict__ table, const b128* __restrict__ ehi,
+                                                     const b128* __restrict__ elo, int lb, const f162* __restrict__ psi,
+                                                     Soa a, Soa p, uint64_t n) {
+  extern __shared__ __align__(16) uint64_t sm64[];
+  f162* tab = reinterpret_cast<f162*>(sm64);
+  for (int i = threadIdx.x; i < 16 * 256; i += blockDim.x) tab[i] = psi[i];
+  __syncthreads();
+  const uint64_t mask = (1ull << lb) - 1;
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
+    b128 e = b128_mul(ehi[j >> lb], elo[j & mask]);
+    f162 v = {0, 0, 0};
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      uint32_t byte = (uint32_t)((c < 8 ? e.lo >> (8 * c) : e.hi >> (8 * (c - 8))) & 0xff);
+      v = f162_add(v, tab[c * 256 + byte]);
+    }
+    a.put(j, v);
+    uint4 w = table[j];
+    p.put(j, {(uint64_t)w.x | ((uint64_t)w.y << 32), (uint64_t)w.z | ((uint64_t)w.w << 32), 0});
+  }
+}
+
+__device__ __forceinline__ f162 shfl_xor_f162(f162 v, int m) {
+  v.w0 ^= __shfl_xor_sync(0xffffffffu, v.w0, m);
+  v.w1 ^= __shfl_xor_sync(0xffffffffu, v.w1, m);
+  v.w2 ^= __shfl_xor_sync(0xffffffffu, v.w2, m);
+  return v;
+}
+
+// msg = [sum_{j<half} a_j p_j, sum (a_j + a_{j+half})(p_j + p_{j+half})] (sumcheck.rs:128-189)
+__global__ void __launch_bounds__(256) k_switch_msg(Soa a, Soa p, uint64_t half, unsigned long long* __restrict__ msg) {
+  f162 e0 = {0, 0, 0}, ei = {0, 0, 0};
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < half; j += (uint64_t)gridDim.x * blockDim.x) {
+    f162 a0 = a.get(j), a1 = a.get(j + half), p0 = p.get(j), p1 = p.get(j + half);
+    e0 = f162_add(e0, f162_mul(a0, p0));
+    ei = f162_add(ei, f162_mul(f162_add(a0, a1), f162_add(p0, p1)));
+  }
+  for (int m = 16; m; m >>= 1) e0 = shfl_xor_f162(e0, m), ei = shfl_xor_f162(ei, m);
+  __shared__ f162 part[2][8];
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) part[0][warp] = e0, part[1][warp] = ei;
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    f162 s = {0, 0, 0};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s = f162_add(s, part[threadIdx.x][w]);
+    unsigned long long* o = msg + 3 * threadIdx.x;
+    atomicXor(o, (unsigned long long)s.w0);
+    atomicXor(o + 1, (unsigned long long)s.w1);
+    atomicXor(o + 2, (unsigned long long)s.w2);
+  }
+}
+
+// x[j] <- x[j] + r (x[j] + x[j + half]) for j < half, both polynomials (sumcheck.rs:191-245)
+__global__ void __launch_bounds__(256) k_switch_fold(Soa a, Soa p, uint64_t half, f162 r) {
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < half; j += (uint64_t)gridDim.x * blockDim.x) {
+    f162 a0 = a.get(j), a1 = a.get(j + half), p0 = p.get(j), p1 = p.get(j + half);
+    a.put(j, f162_add(a0, f162_mul(r, f162_add(a0, a1))));
+    p.put(j, f162_add(p0, f162_mul(r, f162_add(p0, p1))));
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Launch wrappers
+// ---------------------------------------------------------------------------------------------
+static unsigned grid_for(uint64_t n, int threads, unsigned cap) {
+  uint64_t g = (n + threads - 1) / threads;
+  if (g > cap) g = cap;
+  return (unsigned)(g ? g : 1);
+}
+
+void launch_eq_b128(const b128* r, int n, b128* out, cudaStream_t s) {
+  uint64_t N = 1ull << n;
+  k_eq_b128<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(r, n, out);
+}
+void launch_eq_table_f162(const f162* ps, int n, f162* out, cudaStream_t s) {
+  uint64_t N = 1ull << n;
+  k_eq_table_f162<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(ps, n, out);
+}
+void launch_planes_b128(const b128* x, uint64_t n, uint32_t* planes, cudaStream_t s) {
+  k_planes_b128<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, n, planes);
+}
+void launch_sblock(const uint4* table, uint64_t nblocks, const uint32_t* lo_planes, uint8_t* sblk, cudaStream_t s) {
+  const int smem = 2 * SB_W * 128 * 4;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_sblock, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr = true;
+  }
+  k_sblock<<<(unsigned)nblocks, 256, smem, s>>>(table, lo_planes, sblk);
+}
+void launch_partials_combine(const b128* ehi, const uint8_t* sblk, int nblocks, unsigned long long* v, cudaStream_t s) {
+  int run = 16;
+  k_partials_combine<<<(nblocks + run - 1) / run, 128, 0, s>>>(ehi, sblk, nblocks, run, v);
+}
+void launch_psi_tables(const f162* batch, f162* tab, cudaStream_t s) { k_psi_tables<<<16, 256, 0, s>>>(batch, tab); }
+void launch_switch_init(const uint4* table, const b128* ehi, const b128* elo, int lb, const f162* psi, Soa a, Soa p,
+                        uint64_t n, int sms, cudaStream_t s) {
+  const int smem = 16 * 256 * 24;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_switch_init, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr = true;
+  }
+  k_switch_init<<<grid_for(n, 256, sms * 2), 256, smem, s>>>(table, ehi, elo, lb, psi, a, p, n);
+}
+void launch_switch_msg(Soa a, Soa p, uint64_t half, unsigned long long* msg, int sms, cudaStream_t s) {
+  k_switch_msg<<<grid_for(half, 256, sms * 8), 256, 0, s>>>(a, p, half, msg);
+}
+void launch_switch_fold(Soa a, Soa p, uint64_t half, f162 r, int sms, cudaStream_t s) {
+  k_switch_fold<<<grid_for(half, 256, sms * 8), 256, 0, s>>>(a, p, half, r);
+}
+
+}  // namespace lf

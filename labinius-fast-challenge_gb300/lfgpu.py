@@ -1,0 +1,164 @@
+"""Python binding of liblabinius_gpu (ctypes over include/labinius_gpu.h).
+
+The prover mirrors the reference's `prove(seed, Q, table) -> proof` boundary
+(solution/proof_generate/src/main.rs:1692-2009) with the bincode proof layout of
+verifier/proof_verify/src/main.rs:98-124. There is no CPU path: without the CUDA library or a
+device every call raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liblabinius_gpu.so")
+CLI_PATH = os.path.join(HERE, "_build", "labinius-fast")
+BASELINE_Q = 3889 * 9721 * 17497
+
+LF_OK = 0
+ERRORS = {
+    -1: "LF_E_ARGS", -2: "LF_E_SHAPE", -3: "LF_E_MODULUS", -4: "LF_E_TABLE_LEN", -5: "LF_E_CAP",
+    -6: "LF_E_OOM", -7: "LF_E_CUDA", -8: "LF_E_INTERNAL", -9: "LF_E_ADMISSION",
+}
+EXPORTS = [
+    "lf_ctx_create", "lf_ctx_destroy", "lf_proof_size", "lf_accept_modulus", "lf_key_prepare", "lf_prove",
+    "lf_prove_device", "lf_write_table_device", "lf_device_alloc", "lf_device_free", "lf_memcpy_h2d",
+    "lf_last_profile", "lf_strerror", "lf_last_error",
+]
+
+
+class LfError(RuntimeError):
+    def __init__(self, code, msg=""):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("hbm_budget", ctypes.c_size_t)]
+
+
+class Profile(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in (
+        "upload_ms", "key_ms", "commit_ms", "transcript_ms", "partials_ms", "switch_ms", "row_ms",
+        "challenges_ms", "fold_ms", "download_ms", "total_ms")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """The shared library, loaded once. Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing: run labinius-fast-challenge_gb300/build.py")
+    lib = ctypes.CDLL(path)
+    p, u8p, sz = ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t
+    lib.lf_ctx_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(p)]
+    lib.lf_ctx_destroy.argtypes = [p]
+    lib.lf_ctx_destroy.restype = None
+    lib.lf_proof_size.argtypes = [ctypes.c_char_p, ctypes.c_uint32]
+    lib.lf_proof_size.restype = sz
+    lib.lf_accept_modulus.argtypes = [ctypes.c_char_p, ctypes.c_uint32]
+    lib.lf_key_prepare.argtypes = [p, ctypes.c_char_p, ctypes.c_uint32]
+    lib.lf_prove.argtypes = [p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint32, p, sz, u8p, sz,
+                             ctypes.POINTER(sz)]
+    lib.lf_prove_device.argtypes = [p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint32, p, u8p, sz,
+                                    ctypes.POINTER(sz)]
+    lib.lf_write_table_device.argtypes = [p, ctypes.c_char_p, ctypes.c_uint32, p]
+    lib.lf_device_alloc.argtypes = [p, sz, ctypes.POINTER(p)]
+    lib.lf_device_free.argtypes = [p, p]
+    lib.lf_memcpy_h2d.argtypes = [p, p, p, sz]
+    lib.lf_last_profile.argtypes = [p, ctypes.POINTER(Profile)]
+    lib.lf_strerror.argtypes = [ctypes.c_int]
+    lib.lf_strerror.restype = ctypes.c_char_p
+    lib.lf_last_error.argtypes = [p]
+    lib.lf_last_error.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def q_bytes(q):
+    return int(q).to_bytes(16, "little")
+
+
+def proof_size(q, log_vars):
+    return load().lf_proof_size(q_bytes(q), log_vars)
+
+
+def accept_modulus(q, log_vars):
+    return load().lf_accept_modulus(q_bytes(q), log_vars) == LF_OK
+
+
+class Prover:
+    """One device context (lf_ctx). Not thread-safe across calls; the C side serialises."""
+
+    def __init__(self, device=0, hbm_budget=0):
+        self.lib = load()
+        self.ctx = ctypes.c_void_p()
+        cfg = Config(device, hbm_budget)
+        rc = self.lib.lf_ctx_create(ctypes.byref(cfg), ctypes.byref(self.ctx))
+        if rc != LF_OK:
+            raise LfError(rc, "context creation failed (no CUDA device?)")
+
+    def close(self):
+        if self.ctx:
+            self.lib.lf_ctx_destroy(self.ctx)
+            self.ctx = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != LF_OK:
+            raise LfError(rc, self.lib.lf_last_error(self.ctx).decode())
+
+    def prove(self, seed, table, log_vars, q=BASELINE_Q):
+        """Proof bytes for a host table (bytes, bytearray, memoryview or numpy array)."""
+        mv = memoryview(table).cast("B")
+        cap = proof_size(q, log_vars)
+        out = (ctypes.c_uint8 * max(cap, 1))()
+        n = ctypes.c_size_t()
+        buf = (ctypes.c_uint8 * len(mv)).from_buffer_copy(mv) if mv.readonly else (ctypes.c_uint8 * len(mv)).from_buffer(mv)
+        rc = self.lib.lf_prove(self.ctx, bytes(seed), q_bytes(q), log_vars, ctypes.cast(buf, ctypes.c_void_p),
+                               len(mv), out, cap, ctypes.byref(n))
+        self._check(rc)
+        return bytes(out[: n.value])
+
+    def prove_device(self, seed, table_dev, log_vars, q=BASELINE_Q, out=None):
+        cap = proof_size(q, log_vars)
+        out = out if out is not None else (ctypes.c_uint8 * cap)()
+        n = ctypes.c_size_t()
+        rc = self.lib.lf_prove_device(self.ctx, bytes(seed), q_bytes(q), log_vars, ctypes.c_void_p(table_dev), out,
+                                      cap, ctypes.byref(n))
+        self._check(rc)
+        return out, n.value
+
+    def key_prepare(self, log_vars, q=BASELINE_Q):
+        self._check(self.lib.lf_key_prepare(self.ctx, q_bytes(q), log_vars))
+
+    def alloc(self, nbytes):
+        p = ctypes.c_void_p()
+        self._check(self.lib.lf_device_alloc(self.ctx, nbytes, ctypes.byref(p)))
+        return p.value
+
+    def free(self, dev):
+        self._check(self.lib.lf_device_free(self.ctx, ctypes.c_void_p(dev)))
+
+    def h2d(self, dev, data):
+        mv = memoryview(data).cast("B")
+        buf = (ctypes.c_uint8 * len(mv)).from_buffer_copy(mv)
+        self._check(self.lib.lf_memcpy_h2d(self.ctx, ctypes.c_void_p(dev), buf, len(mv)))
+
+    def write_table_device(self, seed, log_vars, dev):
+        self._check(self.lib.lf_write_table_device(self.ctx, bytes(seed), log_vars, ctypes.c_void_p(dev)))
+
+    def profile(self):
+        p = Profile()
+        self._check(self.lib.lf_last_profile(self.ctx, ctypes.byref(p)))
+        return p.as_dict()

@@ -1,0 +1,53 @@
+"""The C ABI without a GPU: the library builds for sm_103a, loads, exports every entry point the
+header declares, and its host-only entry points agree with the oracle."""
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "labinius_gpu.h")
+
+
+def declared():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(lf_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(gpu_lib):
+    lib = gpu_lib.load()
+    names = declared()
+    assert len(names) >= 14
+    for n in names:
+        assert hasattr(lib, n), n
+    out = subprocess.run(["nm", "-D", "--defined-only", gpu_lib.LIB_PATH], capture_output=True, text=True).stdout
+    for n in names:
+        assert re.search(rf"\bT {n}\b", out), n
+
+
+def test_proof_size_and_gate_match_oracle(gpu_lib, oracle):
+    for log_vars in (19, 20, 22, 31):
+        for q in (3889 * 9721 * 17497, 1 << 36, 55_144_219_393, (1 << 96) - 1):
+            assert gpu_lib.proof_size(q, log_vars) == oracle.proof_size(q, log_vars)
+            assert gpu_lib.accept_modulus(q, log_vars) == oracle.accept_modulus(q, log_vars)
+    assert gpu_lib.proof_size(3889 * 9721 * 17497, 31) == 13_958_612
+    assert not gpu_lib.accept_modulus(34_816_965_048, 31)
+
+
+def test_cli_built_and_usage(gpu_lib):
+    assert os.path.exists(gpu_lib.CLI_PATH)
+    p = subprocess.run([gpu_lib.CLI_PATH], capture_output=True, text=True)
+    assert p.returncode != 0 and "usage" in p.stderr
+
+
+def test_no_device_fails_loudly(gpu_lib):
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            pytest.skip("a device is present")
+    except ImportError:
+        pass
+    with pytest.raises(gpu_lib.LfError):
+        gpu_lib.Prover(0)
