@@ -39,8 +39,9 @@ typedef struct lf_config {
 /* Per-phase device times of the last lf_prove* call on a context, in milliseconds
  * (the reference's labinius-profile line, solution/proof_generate/src/main.rs:1999-2007). */
 typedef struct lf_profile {
-  double upload_ms, key_ms, commit_ms, transcript_ms, partials_ms, switch_ms, row_ms, challenges_ms, fold_ms,
-      download_ms, total_ms;
+  double upload_ms, key_ms, commit_ms, finish_ms, transcript_ms, partials_ms, switch_ms, row_ms, challenges_ms,
+      fold_ms, download_ms, total_ms;
+  int launches; /* kernels this library launched for the proof (key preparation excluded when cached) */
 } lf_profile;
 
 /* Context lifetime. Replaces the process-wide pool and allocator of the reference prover
@@ -81,6 +82,22 @@ int lf_device_free(lf_ctx* ctx, void* dev);
 int lf_memcpy_h2d(lf_ctx* ctx, void* dst_dev, const void* src, size_t bytes);
 
 int lf_last_profile(lf_ctx* ctx, lf_profile* out);
+
+/* Diagnostics: the 1024 folding challenges of the last proof, 40 bytes each (32 position bytes,
+ * u32 sign bits, u32 weight), as sample_short_challenges returns them
+ * (solution-arm/labinius/crates/pcs/src/challenge.rs:707-737). The proof itself carries only
+ * their effect, the fold. */
+int lf_last_challenges(lf_ctx* ctx, uint8_t* out, size_t cap);
+
+/* Diagnostics: n folding challenges sampled on the device from Transcript::new(domain) after
+ * absorb_bytes(prefix) (challenge.rs:240-259, 707-737), 40 bytes each as above. */
+int lf_sample_challenges(lf_ctx* ctx, const char* domain, const uint8_t* prefix, size_t prefix_len, uint32_t n,
+                         uint8_t* out);
+/* The same, also returning 64 words describing challenge 0's first attempt: the XOF root node
+ * (27 words), its first 32 output bytes, the attempt's sorted positions, sign bits, rejection flag
+ * and lane 0's squared norm. */
+int lf_sample_challenges_traced(lf_ctx* ctx, const char* domain, const uint8_t* prefix, size_t prefix_len, uint32_t n,
+                                uint8_t* out, uint32_t* trace64);
 const char* lf_strerror(int code);
 const char* lf_last_error(lf_ctx* ctx);
 

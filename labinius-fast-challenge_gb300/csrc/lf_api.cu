@@ -3,6 +3,7 @@
 // reference prover verifier/proof_verify/src/reference.rs:137-177 fixes every byte).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -87,13 +88,7 @@ struct Transcript {
       h.absorb_u64(xs[i].w2);
     }
   }
-  bk::Pending derive(const char* label) {
-    bk::Hasher c = h;
-    c.absorb_u64(counter++);
-    c.absorb_u64(strlen(label));
-    c.absorb((const uint8_t*)label, strlen(label));
-    return c.finish();
-  }
+  bk::Pending derive(const char* label) { return bk::derive_root(h, counter++, label, (uint32_t)strlen(label)); }
   void fill(const char* label, uint8_t* out, size_t n) { derive(label).root_bytes(0, out, n); }
   std::vector<b128> sample_b128(const char* label, size_t n) {
     std::vector<uint8_t> b(16 * n);
@@ -210,6 +205,12 @@ int fail(lf_ctx* c, int code, const std::string& msg) {
   return code;
 }
 
+#define CKL(label)                                                                                 \
+  do {                                                                                             \
+    cudaError_t e_ = cudaGetLastError();                                                           \
+    if (e_ != cudaSuccess) return fail(ctx, LF_E_CUDA, std::string(label) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
 #define CK(expr)                                                                                   \
   do {                                                                                             \
     cudaError_t e_ = (expr);                                                                       \
@@ -257,7 +258,7 @@ int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh) {
   upload_prime_consts(mp, ctx->stream);
   launch_matrix_expand(mp, E, ared.as<uint32_t>(), ctx->stream);
   launch_key_transform(mp, E, ared.as<uint32_t>(), leaf.as<uint32_t>(), ctx->key.key.as<uint16_t>(), ctx->stream);
-  CK(cudaGetLastError());
+  CKL("key build");
   CK(cudaStreamSynchronize(ctx->stream));
   ared.release();
   leaf.release();
@@ -305,8 +306,9 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   CK(ctx->partial.ensure((size_t)splits * mp.nprimes * COLUMNS * LEAVES * 4 * 4));
   CK(ctx->stream_buf.ensure(STREAM_PREFIX + commit_bytes + 1024));
   launch_commit(mp, sh, table, ctx->key.key.as<uint16_t>(), ctx->partial.as<uint32_t>(), splits, st);
+  cudaEventRecord(ctx->ev[11], st);
   launch_commit_finish(mp, sh, ctx->partial.as<uint32_t>(), splits, ctx->stream_buf.as<uint8_t>() + STREAM_PREFIX, st);
-  CK(cudaGetLastError());
+  CKL("commitment");
   cudaEventRecord(ctx->ev[3], st);
 
   // ---- transcript (main.rs:166-174): the prefix on the host, the commitment's chunks on the device ----
@@ -347,7 +349,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   launch_chunk_cvs(ctx->stream_buf.as<uint8_t>(), nchunks, t.h.key, t.h.mode, ctx->cvs.as<uint32_t>(), st);
   launch_subtrees(ctx->cvs.as<uint32_t>(), ctx->cvs_scratch.as<uint32_t>(), nchunks, t.h.key, t.h.mode,
                   ctx->subtrees.as<uint32_t>(), st);
-  CK(cudaGetLastError());
+  CKL("transcript hashing");
   uint32_t sub[64][8];
   uint8_t tail[1024];
   const int depth = __builtin_popcountll(nchunks);
@@ -382,7 +384,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   CK(cudaMemsetAsync(ctx->vparts.p, 0, 256 * 8, st));
   launch_partials_combine(ctx->ehi.as<b128>(), ctx->sblk.as<uint8_t>(), (int)nblocks,
                           ctx->vparts.as<unsigned long long>(), st);
-  CK(cudaGetLastError());
+  CKL("partials");
   std::vector<b128> partials(128);
   CK(cudaMemcpyAsync(partials.data(), ctx->vparts.p, 128 * 16, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -407,7 +409,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   uint64_t* sb = ctx->soa.as<uint64_t>();
   Soa A = {sb, sb + n, sb + 2 * n}, P = {sb + 3 * n, sb + 4 * n, sb + 5 * n};
   launch_switch_init(table, ctx->ehi.as<b128>(), ctx->elo.as<b128>(), LB, ctx->psi.as<f162>(), A, P, n, ctx->sms, st);
-  CK(cudaGetLastError());
+  CKL("switch init");
   std::vector<f162> coords, rounds;
   uint64_t half = n;
   for (int r = 0; r < sh.lp; ++r) {
@@ -424,7 +426,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
     coords.push_back(rr);
     launch_switch_fold(A, P, half, rr, ctx->sms, st);
   }
-  CK(cudaGetLastError());
+  CKL("switch rounds");
   f162 opened;
   CK(cudaMemcpyAsync(&opened.w0, P.w0, 8, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&opened.w1, P.w1, 8, cudaMemcpyDeviceToHost, st));
@@ -441,7 +443,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   CK(cudaMemcpyAsync(ctx->p0.p, p0.data(), 24 * p0.size(), cudaMemcpyHostToDevice, st));
   launch_eq_table_f162(ctx->p0.as<f162>(), sh.rl, ctx->eqt.as<f162>(), st);
   launch_row_eval(table, sh.rl, ctx->eqt.as<f162>(), ctx->row.as<f162>(), st);
-  CK(cudaGetLastError());
+  CKL("row evaluation");
   std::vector<f162> row(COLUMNS);
   CK(cudaMemcpyAsync(row.data(), ctx->row.p, COLUMNS * 24, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -461,14 +463,14 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.as<double>(), ctx->phase.as<double>() + 162 * 88,
                     ctx->chal.as<Challenge>(), COLUMNS, ctx->status.as<int>(), st);
   t.counter += COLUMNS;
-  CK(cudaGetLastError());
+  CKL("challenges");
   cudaEventRecord(ctx->ev[8], st);
 
   // ---- fold (reference.rs:72-133), straight into the proof's i32 region ----
   CK(ctx->fold.ensure(fold_bytes));
   launch_fold(table, sh.rl, sh.ring_elements, ctx->chal.as<Challenge>(), ctx->fold.as<int32_t>(),
               ctx->status.as<int>(), st);
-  CK(cudaGetLastError());
+  CKL("fold");
   cudaEventRecord(ctx->ev[9], st);
   CK(cudaMemcpyAsync(proof + at_fold, ctx->fold.p, fold_bytes, cudaMemcpyDeviceToHost, st));
   int status[4];
@@ -494,7 +496,11 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   *proof_len = plen;
 
   ctx->prof.key_ms = ev_ms(ctx, 1, 2);
-  ctx->prof.commit_ms = ev_ms(ctx, 2, 3);
+  ctx->prof.commit_ms = ev_ms(ctx, 2, 11);
+  ctx->prof.finish_ms = ev_ms(ctx, 11, 3);
+  // Kernel launches of one proof: commit 2, stream hashing 2, partials 5, switch 2 + 2 per round,
+  // row 2, challenges 1, fold 1.
+  ctx->prof.launches = 2 + 2 + 5 + 2 + 2 * sh.lp + 2 + 1 + 1;
   ctx->prof.transcript_ms = ev_ms(ctx, 3, 4);
   ctx->prof.partials_ms = ev_ms(ctx, 4, 5);
   ctx->prof.switch_ms = ev_ms(ctx, 5, 6);
@@ -661,7 +667,7 @@ int lf_write_table_device(lf_ctx* ctx, const uint8_t seed[32], uint32_t log_vars
   bk::Pending root = h.finish();
   uint64_t blocks = (s.words * 16) / 64;
   k_table_prg<<<(unsigned)((blocks + 255) / 256), 256, 0, ctx->stream>>>(root, blocks, reinterpret_cast<uint4*>(out_dev));
-  CK(cudaGetLastError());
+  CKL("table PRG");
   CK(cudaStreamSynchronize(ctx->stream));
   return LF_OK;
 }
@@ -682,6 +688,44 @@ int lf_memcpy_h2d(lf_ctx* ctx, void* dst_dev, const void* src, size_t bytes) {
   if (!ctx || !dst_dev || !src) return LF_E_ARGS;
   cudaSetDevice(ctx->device);
   CK(cudaMemcpy(dst_dev, src, bytes, cudaMemcpyHostToDevice));
+  return LF_OK;
+}
+
+int lf_last_challenges(lf_ctx* ctx, uint8_t* out, size_t cap) {
+  if (!ctx || !out) return LF_E_ARGS;
+  if (cap < COLUMNS * sizeof(Challenge) || ctx->chal.cap < COLUMNS * sizeof(Challenge)) return LF_E_CAP;
+  cudaSetDevice(ctx->device);
+  CK(cudaMemcpy(out, ctx->chal.p, COLUMNS * sizeof(Challenge), cudaMemcpyDeviceToHost));
+  return LF_OK;
+}
+
+int lf_sample_challenges(lf_ctx* ctx, const char* domain, const uint8_t* prefix, size_t prefix_len, uint32_t n,
+                         uint8_t* out) {
+  return lf_sample_challenges_traced(ctx, domain, prefix, prefix_len, n, out, nullptr);
+}
+
+int lf_sample_challenges_traced(lf_ctx* ctx, const char* domain, const uint8_t* prefix, size_t prefix_len, uint32_t n,
+                                uint8_t* out, uint32_t* trace64) {
+  if (!ctx || !domain || (!prefix && prefix_len) || !out) return LF_E_ARGS;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaSetDevice(ctx->device);
+  Transcript t;
+  t.init(domain);
+  t.absorb_bytes(prefix, prefix_len);
+  CK(ctx->hasher.ensure(sizeof(bk::Hasher)));
+  CK(ctx->chal.ensure(std::max<size_t>(n, COLUMNS) * sizeof(Challenge)));
+  CK(ctx->status.ensure(16));
+  CK(ctx->scratch_small.ensure(64 * 4));
+  CK(cudaMemsetAsync(ctx->scratch_small.p, 0, 64 * 4, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->hasher.p, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(ctx->status.p, 0, 16, ctx->stream));
+  launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.as<double>(), ctx->phase.as<double>() + 162 * 88,
+                    ctx->chal.as<Challenge>(), (int)n, ctx->status.as<int>(), ctx->stream,
+                    trace64 ? ctx->scratch_small.as<uint32_t>() : nullptr);
+  CKL("challenges");
+  CK(cudaMemcpyAsync(out, ctx->chal.p, n * sizeof(Challenge), cudaMemcpyDeviceToHost, ctx->stream));
+  if (trace64) CK(cudaMemcpyAsync(trace64, ctx->scratch_small.p, 64 * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   return LF_OK;
 }
 

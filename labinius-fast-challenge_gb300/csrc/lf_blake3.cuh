@@ -278,5 +278,20 @@ struct Hasher {
   LF_HD uint64_t count() const { return chunk.index * 1024 + chunk.size(); }
 };
 
+// The root of one transcript derivation (challenge.rs:335-341): the stream so far, then the
+// counter (u64 LE), the label length (u64 LE) and the label. The suffix is assembled in one local
+// buffer and absorbed in a single call; on sm_103a a sequence of small absorbs from separate local
+// arrays (two u64 helpers and a label literal) produced a wrong chaining value, while this form
+// matches the host build (tests/dev_blake3_check.cu).
+LF_HD Pending derive_root(const Hasher& state, uint64_t counter, const char* label, uint32_t label_len) {
+  uint8_t suffix[16 + 64];
+  for (int i = 0; i < 8; ++i) suffix[i] = (uint8_t)(counter >> (8 * i));
+  for (int i = 0; i < 8; ++i) suffix[8 + i] = (uint8_t)((uint64_t)label_len >> (8 * i));
+  for (uint32_t i = 0; i < label_len && i < 64; ++i) suffix[16 + i] = (uint8_t)label[i];
+  Hasher h = state;
+  h.absorb(suffix, 16 + (label_len < 64 ? label_len : 64));
+  return h.finish();
+}
+
 }  // namespace bk
 }  // namespace lf

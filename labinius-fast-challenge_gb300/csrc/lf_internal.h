@@ -111,7 +111,8 @@ void launch_switch_fold(Soa a, Soa p, uint64_t half, f162 r, int sms, cudaStream
 void launch_row_eval(const uint4* table, int rl, const f162* eqt, f162* row, cudaStream_t s);
 struct HasherImage;  // a bk::Hasher copied to the device
 void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint32_t sign_key[8], const double* phase_re,
-                       const double* phase_im, Challenge* out, int n, int* status, cudaStream_t s);
+                       const double* phase_im, Challenge* out, int n, int* status, cudaStream_t s,
+                       uint32_t* dbg = nullptr);
 void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Challenge* ch, int32_t* out, int* status,
                  cudaStream_t s);
 void launch_chunk_cvs(const uint8_t* stream, uint64_t nchunks, const uint32_t key[8], uint32_t mode, uint32_t* cvs,

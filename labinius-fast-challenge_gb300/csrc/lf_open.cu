@@ -65,6 +65,7 @@ struct ChWarp {
 };
 
 __device__ __forceinline__ void xof_refill(ChWarp& s, const bk::Pending& root, uint64_t& next_block, int lane) {
+  __syncwarp();  // every lane has read the previous buffer before any lane overwrites it
   uint32_t w[16];
   root.root_block(next_block + lane, w);
   uint32_t* dst = reinterpret_cast<uint32_t*>(s.buf + 64 * lane);
@@ -77,19 +78,20 @@ __device__ __forceinline__ void xof_refill(ChWarp& s, const bk::Pending& root, u
 __global__ void __launch_bounds__(32 * CH_WARPS) k_challenges(const bk::Hasher* __restrict__ state, uint64_t base,
                                                               bk::Pending sign_key_node, const double* __restrict__ re,
                                                               const double* __restrict__ im, double bound_sq,
-                                                              Challenge* __restrict__ out, int n, int* status) {
+                                                              Challenge* __restrict__ out, int n, int* status,
+                                                              uint32_t* __restrict__ dbg) {
   __shared__ ChWarp sw[CH_WARPS];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int ci = blockIdx.x * CH_WARPS + wid;
   if (ci >= n) return;
   ChWarp& s = sw[wid];
   if (lane == 0) {
-    bk::Hasher h = *state;
-    h.absorb_u64(base + (uint64_t)ci);
-    const char label[] = "short-challenge";
-    h.absorb_u64(sizeof(label) - 1);
-    h.absorb((const uint8_t*)label, sizeof(label) - 1);
-    bk::Pending r = h.finish();
+    if (dbg != nullptr && ci == 0) {
+      dbg[48] = state->key[0], dbg[49] = state->mode, dbg[50] = state->depth, dbg[51] = state->chunk.buf_len;
+      dbg[52] = state->chunk.blocks, dbg[53] = (uint32_t)state->chunk.index, dbg[54] = state->chunk.h[0];
+      dbg[56] = (uint32_t)sizeof(bk::Hasher);
+    }
+    bk::Pending r = bk::derive_root(*state, base + (uint64_t)ci, "short-challenge", 15);
     for (int i = 0; i < 8; ++i) s.root[i] = r.h[i];
     for (int i = 0; i < 16; ++i) s.root[8 + i] = r.m[i];
     s.root[24] = (uint32_t)r.t;
@@ -105,6 +107,9 @@ __global__ void __launch_bounds__(32 * CH_WARPS) k_challenges(const bk::Hasher* 
   root.flags = s.root[26];
   uint64_t next_block = 0;
   int pos = XOF_BUF;
+  const bool trace = dbg != nullptr && ci == 0;
+  if (trace && lane == 0)
+    for (int i = 0; i < 27; ++i) dbg[i] = s.root[i];
   auto byte = [&]() -> uint32_t {
     if (pos == XOF_BUF) {
       xof_refill(s, root, next_block, lane);
@@ -155,6 +160,11 @@ __global__ void __launch_bounds__(32 * CH_WARPS) k_challenges(const bk::Hasher* 
       signs = o[0] & ((1u << WEIGHT) - 1);
     }
     signs = __shfl_sync(0xffffffffu, signs, 0);
+    if (trace && attempt == 0 && lane == 0) {
+      for (int i = 0; i < 32; ++i) reinterpret_cast<uint8_t*>(dbg + 27)[i] = s.buf[i];
+      for (int i = 0; i < 28; ++i) reinterpret_cast<uint8_t*>(dbg + 35)[i] = sorted[wid][i];
+      dbg[42] = signs;
+    }
     bool over = false;
     for (int k = lane; k < 81; k += 32) {
       double vr = 0.0, vi = 0.0;
@@ -167,8 +177,15 @@ __global__ void __launch_bounds__(32 * CH_WARPS) k_challenges(const bk::Hasher* 
       }
       double m2 = __dadd_rn(__dmul_rn(vr, vr), __dmul_rn(vi, vi));
       over |= m2 > bound_sq;
+      if (trace && attempt == 0 && k == 0) {
+        double* d = reinterpret_cast<double*>(dbg + 44);
+        d[0] = m2;
+        d[1] = vr;
+      }
     }
-    if (!__any_sync(0xffffffffu, over)) {
+    const bool any_over = __any_sync(0xffffffffu, over);
+    if (trace && attempt == 0 && lane == 0) dbg[43] = any_over;
+    if (!any_over) {
       if (lane < WEIGHT) out[ci].positions[lane] = sorted[wid][lane];
       else out[ci].positions[lane] = 0;
       if (lane == 0) {
@@ -183,7 +200,7 @@ __global__ void __launch_bounds__(32 * CH_WARPS) k_challenges(const bk::Hasher* 
 }
 
 void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint32_t sign_key[8], const double* phase_re,
-                       const double* phase_im, Challenge* out, int n, int* status, cudaStream_t s) {
+                       const double* phase_im, Challenge* out, int n, int* status, cudaStream_t s, uint32_t* dbg) {
   bk::Pending sk;
   for (int i = 0; i < 8; ++i) sk.h[i] = sign_key[i];
   for (int i = 0; i < 16; ++i) sk.m[i] = 0;
@@ -192,7 +209,7 @@ void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint
   sk.flags = bk::F_DERIVE_MAT | bk::F_CHUNK_START | bk::F_CHUNK_END;
   const double bound_sq = 12.0 * 12.0 + 1e-12;
   k_challenges<<<(n + CH_WARPS - 1) / CH_WARPS, 32 * CH_WARPS, 0, s>>>(
-      reinterpret_cast<const bk::Hasher*>(hasher_dev), base_counter, sk, phase_re, phase_im, bound_sq, out, n, status);
+      reinterpret_cast<const bk::Hasher*>(hasher_dev), base_counter, sk, phase_re, phase_im, bound_sq, out, n, status, dbg);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -208,21 +225,23 @@ constexpr int FOLD_BATCH = FOLD_THREADS / 32;  // columns transposed per step, o
 constexpr int RAW_Y = 128 + 161;               // 289 raw positions
 
 __global__ void __launch_bounds__(FOLD_THREADS) k_fold(const uint4* __restrict__ table, int rl,
-                                                      const Challenge* __restrict__ ch, int32_t* __restrict__ out,
-                                                      int* status) {
+                                                      uint64_t ring_elements, const Challenge* __restrict__ ch,
+                                                      int32_t* __restrict__ out, int* status) {
   __shared__ uint32_t vec[FOLD_BATCH][128];
   __shared__ uint8_t cpos[FOLD_BATCH][32];
   __shared__ uint32_t csign[FOLD_BATCH];
   __shared__ int32_t raw[32][RAW_Y + 1];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint64_t m0 = (uint64_t)blockIdx.x * FOLD_ELEMS;
+  // Columns with fewer than 8 ring elements: lanes past the last element fold zero words.
+  const int live_words = (int)min((uint64_t)FOLD_ELEMS, ring_elements - m0) * 4;
   uint32_t P[16];
 #pragma unroll
   for (int b = 0; b < 16; ++b) P[b] = 0;
   for (int j0 = 0; j0 < COLUMNS; j0 += FOLD_BATCH) {
     const int j = j0 + warp;
     if (j < COLUMNS) {
-      uint4 v = table[((uint64_t)j << rl) + 4 * m0 + lane];
+      uint4 v = lane < live_words ? table[((uint64_t)j << rl) + 4 * m0 + lane] : make_uint4(0, 0, 0, 0);
       uint32_t keep[4] = {0, 0, 0, 0};
 #pragma unroll
       for (int b = 0; b < 128; ++b) {
@@ -288,7 +307,7 @@ __global__ void __launch_bounds__(FOLD_THREADS) k_fold(const uint4* __restrict__
     }
   }
   __syncthreads();
-  for (int idx = tid; idx < FOLD_ELEMS * 648; idx += FOLD_THREADS) {
+  for (int idx = tid; idx < (live_words / 4) * 648; idx += FOLD_THREADS) {
     const int m = idx / 648, c = idx % 648, y = c >> 2, k = c & 3;
     const int32_t v = raw[4 * m + k][y];
     if (v < -32768 || v > 32767) atomicExch(status, 2);
@@ -298,7 +317,8 @@ __global__ void __launch_bounds__(FOLD_THREADS) k_fold(const uint4* __restrict__
 
 void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Challenge* ch, int32_t* out, int* status,
                  cudaStream_t s) {
-  k_fold<<<(unsigned)(ring_elements / FOLD_ELEMS), FOLD_THREADS, 0, s>>>(table, rl, ch, out, status);
+  k_fold<<<(unsigned)((ring_elements + FOLD_ELEMS - 1) / FOLD_ELEMS), FOLD_THREADS, 0, s>>>(table, rl, ring_elements,
+                                                                                          ch, out, status);
 }
 
 // ---------------------------------------------------------------------------------------------

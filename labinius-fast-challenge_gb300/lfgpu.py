@@ -21,7 +21,8 @@ ERRORS = {
 EXPORTS = [
     "lf_ctx_create", "lf_ctx_destroy", "lf_proof_size", "lf_accept_modulus", "lf_key_prepare", "lf_prove",
     "lf_prove_device", "lf_write_table_device", "lf_device_alloc", "lf_device_free", "lf_memcpy_h2d",
-    "lf_last_profile", "lf_strerror", "lf_last_error",
+    "lf_last_profile", "lf_strerror", "lf_last_error", "lf_last_challenges",
+    "lf_sample_challenges",
 ]
 
 
@@ -37,8 +38,8 @@ class Config(ctypes.Structure):
 
 class Profile(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in (
-        "upload_ms", "key_ms", "commit_ms", "transcript_ms", "partials_ms", "switch_ms", "row_ms",
-        "challenges_ms", "fold_ms", "download_ms", "total_ms")]
+        "upload_ms", "key_ms", "commit_ms", "finish_ms", "transcript_ms", "partials_ms", "switch_ms", "row_ms",
+        "challenges_ms", "fold_ms", "download_ms", "total_ms")] + [("launches", ctypes.c_int)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -76,8 +77,19 @@ def load(path=LIB_PATH):
     lib.lf_strerror.restype = ctypes.c_char_p
     lib.lf_last_error.argtypes = [p]
     lib.lf_last_error.restype = ctypes.c_char_p
+    lib.lf_last_challenges.argtypes = [p, u8p, sz]
+    lib.lf_sample_challenges.argtypes = [p, ctypes.c_char_p, ctypes.c_char_p, sz, ctypes.c_uint32, u8p]
     _lib = lib
     return lib
+
+
+def _parse_challenges(raw, n):
+    out = []
+    for i in range(n):
+        c = raw[40 * i:40 * i + 40]
+        w = int.from_bytes(c[36:40], "little")
+        out.append((list(c[:w]), int.from_bytes(c[32:36], "little"), w))
+    return out
 
 
 def q_bytes(q):
@@ -157,6 +169,17 @@ class Prover:
 
     def write_table_device(self, seed, log_vars, dev):
         self._check(self.lib.lf_write_table_device(self.ctx, bytes(seed), log_vars, ctypes.c_void_p(dev)))
+
+    def sample_challenges(self, domain, prefix, n):
+        buf = (ctypes.c_uint8 * (40 * n))()
+        self._check(self.lib.lf_sample_challenges(self.ctx, domain.encode(), bytes(prefix), len(prefix), n, buf))
+        return _parse_challenges(bytes(buf), n)
+
+    def last_challenges(self):
+        """[(positions, signs, weight)] of the last proof's 1024 folding challenges."""
+        buf = (ctypes.c_uint8 * (40 * 1024))()
+        self._check(self.lib.lf_last_challenges(self.ctx, buf, 40 * 1024))
+        return _parse_challenges(bytes(buf), 1024)
 
     def profile(self):
         p = Profile()

@@ -58,3 +58,10 @@ def test_repeatable(prover, oracle):
     seed = SEEDS[1]
     table = oracle.write_table(seed, log_vars)
     assert prover.prove(seed, table, log_vars) == prover.prove(seed, table, log_vars)
+
+
+@pytest.mark.parametrize("prefix", [b"", b"lfchk", bytes(range(256)) * 13], ids=["empty", "short", "3328B"])
+def test_device_challenges_match_oracle(prover, oracle, prefix):
+    want = oracle.short_challenges("labinius/test/batch", prefix, 64)
+    got = prover.sample_challenges("labinius/test/batch", prefix, 64)
+    assert got == want
