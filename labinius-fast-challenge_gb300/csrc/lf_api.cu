@@ -499,8 +499,8 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   ctx->prof.commit_ms = ev_ms(ctx, 2, 11);
   ctx->prof.finish_ms = ev_ms(ctx, 11, 3);
   // Kernel launches of one proof: commit 2, stream hashing 2, partials 5, switch 2 + 2 per round,
-  // row 2, challenges 1, fold 1.
-  ctx->prof.launches = 2 + 2 + 5 + 2 + 2 * sh.lp + 2 + 1 + 1;
+  // row 2, challenges 1, fold 2.
+  ctx->prof.launches = 2 + 2 + 5 + 2 + 2 * sh.lp + 2 + 1 + 2;
   ctx->prof.transcript_ms = ev_ms(ctx, 3, 4);
   ctx->prof.partials_ms = ev_ms(ctx, 4, 5);
   ctx->prof.switch_ms = ev_ms(ctx, 5, 6);

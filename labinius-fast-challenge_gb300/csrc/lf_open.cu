@@ -315,10 +315,177 @@ __global__ void __launch_bounds__(FOLD_THREADS) k_fold(const uint4* __restrict__
   }
 }
 
+// Fold, carry-save version. A block folds 16 elements (64 table words: two 32-bit bit-slices per
+// thread) over a share of the columns; thread y owns raw position y. Per column the 128 bit
+// vectors of the 64 words sit in shared memory zero-padded to positions -161..288, so term t of
+// a challenge contributes vec[y - pos_t] with no range test. A negative term contributes the
+// complemented vector: sum_t s_t x_t = sum_{t+} x_t + sum_{t-} ~x_t - (number of negative terms),
+// and that count does not depend on y or on the lane, so it is subtracted once at the end.
+// The inputs (28 per column, 8 columns per step = 14 groups of 16) go through Harley-Seal
+// carry-save adders into a 16-plane counter. Shares of columns are summed with atomicAdd.
+constexpr int F2_BATCH = 8;                 // columns per step, one transposing warp each
+constexpr int F2_THREADS = 320;
+constexpr int F2_PAD = 161;                 // vec index = p + 161, p in [-161, 288]
+constexpr int F2_VEC = 450;
+constexpr int F2_INPUTS = F2_BATCH * WEIGHT;  // 224 = 14 x 16
+
+__device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t u = a ^ b;
+  h = (a & b) | (u & c);
+  l = u ^ c;
+}
+
+__global__ void __launch_bounds__(F2_THREADS) k_fold2(const uint4* __restrict__ table, int rl, uint64_t ring_elements,
+                                                     const Challenge* __restrict__ ch, int col_share,
+                                                     int32_t* __restrict__ out) {
+  extern __shared__ __align__(16) uint8_t f2smem[];
+  uint2* vec = reinterpret_cast<uint2*>(f2smem);                                      // [F2_BATCH][F2_VEC]
+  int* toff = reinterpret_cast<int*>(f2smem + F2_BATCH * F2_VEC * 8);                  // [F2_INPUTS]
+  uint32_t* tmask = reinterpret_cast<uint32_t*>(toff + F2_INPUTS);                     // [F2_INPUTS]
+  __shared__ int neg_total;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint64_t m0 = (uint64_t)blockIdx.x * 16;
+  const int live = (int)min((uint64_t)16, ring_elements - m0) * 4;  // live words of the 64
+  const int c_begin = blockIdx.y * col_share, c_end = min(COLUMNS, c_begin + col_share);
+  for (int i = tid; i < F2_BATCH * F2_VEC; i += F2_THREADS) vec[i] = make_uint2(0, 0);
+  if (tid == 0) neg_total = 0;
+  uint32_t ones[2] = {0, 0}, twos[2] = {0, 0}, fours[2] = {0, 0}, eights[2] = {0, 0};
+  uint32_t P[2][12];
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
+#pragma unroll
+    for (int b = 0; b < 12; ++b) P[h][b] = 0;
+  __syncthreads();
+  for (int j0 = c_begin; j0 < c_end; j0 += F2_BATCH) {
+    const int nb = min(F2_BATCH, c_end - j0);
+    if (warp < nb) {
+      const int j = j0 + warp;
+      const uint4* w = table + ((uint64_t)j << rl) + 4 * m0;
+      uint4 v0 = lane < live ? w[lane] : make_uint4(0, 0, 0, 0);
+      uint4 v1 = lane + 32 < live ? w[lane + 32] : make_uint4(0, 0, 0, 0);
+      uint32_t keep0[4] = {0, 0, 0, 0}, keep1[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int b = 0; b < 128; ++b) {
+        const uint32_t a0 = b < 32 ? v0.x : b < 64 ? v0.y : b < 96 ? v0.z : v0.w;
+        const uint32_t a1 = b < 32 ? v1.x : b < 64 ? v1.y : b < 96 ? v1.z : v1.w;
+        const uint32_t m0b = __ballot_sync(0xffffffffu, (a0 >> (b & 31)) & 1);
+        const uint32_t m1b = __ballot_sync(0xffffffffu, (a1 >> (b & 31)) & 1);
+        if (lane == (b & 31)) keep0[b >> 5] = m0b, keep1[b >> 5] = m1b;
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) vec[warp * F2_VEC + F2_PAD + 32 * i + lane] = make_uint2(keep0[i], keep1[i]);
+      if (lane < WEIGHT) {
+        const int pos = ch[j].positions[lane];
+        const bool neg = (((ch[j].signs >> lane) & 1) ^ (pos & 1)) != 0;
+        toff[warp * WEIGHT + lane] = warp * F2_VEC + F2_PAD - pos;
+        tmask[warp * WEIGHT + lane] = neg ? 0xffffffffu : 0u;
+        const unsigned nn = __ballot_sync(0x0fffffffu, neg);
+        if (lane == 0) atomicAdd(&neg_total, __popc(nn));
+      }
+    } else if (warp < F2_BATCH) {
+      // columns past the end of the share: zero vectors, no negative terms
+#pragma unroll
+      for (int i = 0; i < 4; ++i) vec[warp * F2_VEC + F2_PAD + 32 * i + lane] = make_uint2(0, 0);
+      if (lane < WEIGHT) {
+        toff[warp * WEIGHT + lane] = warp * F2_VEC + F2_PAD;
+        tmask[warp * WEIGHT + lane] = 0u;
+      }
+    }
+    __syncthreads();
+    if (tid < RAW_Y) {
+#pragma unroll 1
+      for (int g = 0; g < F2_INPUTS / 16; ++g) {
+        uint32_t x[2][16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int k = 16 * g + i;
+          const uint2 v = vec[toff[k] + tid];
+          const uint32_t m = tmask[k];
+          x[0][i] = v.x ^ m, x[1][i] = v.y ^ m;
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, sixteens;
+          csa(twosA, ones[h], ones[h], x[h][0], x[h][1]);
+          csa(twosB, ones[h], ones[h], x[h][2], x[h][3]);
+          csa(foursA, twos[h], twos[h], twosA, twosB);
+          csa(twosA, ones[h], ones[h], x[h][4], x[h][5]);
+          csa(twosB, ones[h], ones[h], x[h][6], x[h][7]);
+          csa(foursB, twos[h], twos[h], twosA, twosB);
+          csa(eightsA, fours[h], fours[h], foursA, foursB);
+          csa(twosA, ones[h], ones[h], x[h][8], x[h][9]);
+          csa(twosB, ones[h], ones[h], x[h][10], x[h][11]);
+          csa(foursA, twos[h], twos[h], twosA, twosB);
+          csa(twosA, ones[h], ones[h], x[h][12], x[h][13]);
+          csa(twosB, ones[h], ones[h], x[h][14], x[h][15]);
+          csa(foursB, twos[h], twos[h], twosA, twosB);
+          csa(eightsB, fours[h], fours[h], foursA, foursB);
+          csa(sixteens, eights[h], eights[h], eightsA, eightsB);
+          uint32_t c = sixteens;
+#pragma unroll
+          for (int b = 0; b < 12; ++b) {
+            const uint32_t t = P[h][b] & c;
+            P[h][b] ^= c;
+            c = t;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // Un-slice: raw[lane][y] for the 64 words, then the ring reduction Y^162 = Y^81 - 1 per word.
+  int32_t* raw = reinterpret_cast<int32_t*>(f2smem);  // [64][RAW_Y + 1], reuses the vectors' space
+  const int ntot = neg_total;
+  if (tid < RAW_Y) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+      for (int l = 0; l < 32; ++l) {
+        int32_t v = (int32_t)((ones[h] >> l) & 1) | ((int32_t)((twos[h] >> l) & 1) << 1) |
+                    ((int32_t)((fours[h] >> l) & 1) << 2) | ((int32_t)((eights[h] >> l) & 1) << 3);
+#pragma unroll
+        for (int b = 0; b < 12; ++b) v |= (int32_t)((P[h][b] >> l) & 1) << (b + 4);
+        raw[(32 * h + l) * (RAW_Y + 1) + tid] = v - ntot;
+      }
+  }
+  __syncthreads();
+  if (tid < 64) {
+    int32_t* r = raw + tid * (RAW_Y + 1);
+    for (int y = RAW_Y - 1; y >= N162; --y) {
+      const int32_t v = r[y];
+      r[y - 81] += v;
+      r[y - N162] -= v;
+    }
+  }
+  __syncthreads();
+  for (int idx = tid; idx < (live / 4) * 648; idx += F2_THREADS) {
+    const int m = idx / 648, c = idx % 648, y = c >> 2, k = c & 3;
+    atomicAdd(&out[(m0 + m) * 648 + c], raw[(4 * m + k) * (RAW_Y + 1) + y]);
+  }
+}
+
+__global__ void k_fold_range(const int32_t* __restrict__ out, uint64_t n, int* status) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    if (out[i] < -32768 || out[i] > 32767) atomicExch(status, 2);
+}
+
 void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Challenge* ch, int32_t* out, int* status,
                  cudaStream_t s) {
-  k_fold<<<(unsigned)((ring_elements + FOLD_ELEMS - 1) / FOLD_ELEMS), FOLD_THREADS, 0, s>>>(table, rl, ring_elements,
-                                                                                          ch, out, status);
+  const int smem_vec = F2_BATCH * F2_VEC * 8 + 2 * F2_INPUTS * 4;
+  const int smem_raw = 64 * (RAW_Y + 1) * 4;
+  const int smem = smem_vec > smem_raw ? smem_vec : smem_raw;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_fold2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr = true;
+  }
+  const unsigned blocks = (unsigned)((ring_elements + 15) / 16);
+  // Enough blocks to cover the SMs: split the columns when there are few element blocks.
+  int shares = 1;
+  while (blocks * shares < 2 * 152 && shares < 64) shares *= 2;
+  const int col_share = COLUMNS / shares;
+  cudaMemsetAsync(out, 0, ring_elements * 648 * 4, s);
+  k_fold2<<<dim3(blocks, shares), F2_THREADS, smem, s>>>(table, rl, ring_elements, ch, col_share, out);
+  k_fold_range<<<256, 256, 0, s>>>(out, ring_elements * 648, status);
 }
 
 // ---------------------------------------------------------------------------------------------

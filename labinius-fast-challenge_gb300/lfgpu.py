@@ -140,7 +140,7 @@ class Prover:
         rc = self.lib.lf_prove(self.ctx, bytes(seed), q_bytes(q), log_vars, ctypes.cast(buf, ctypes.c_void_p),
                                len(mv), out, cap, ctypes.byref(n))
         self._check(rc)
-        return bytes(out[: n.value])
+        return ctypes.string_at(out, n.value)
 
     def prove_device(self, seed, table_dev, log_vars, q=BASELINE_Q, out=None):
         cap = proof_size(q, log_vars)
