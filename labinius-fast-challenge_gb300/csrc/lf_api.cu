@@ -192,7 +192,7 @@ struct lf_ctx {
   KeyCache key;
   bool consts_for_key = false;
   DevBuf table, stream_buf, partial, sblk, ehi, elo, lo_planes, rhi, vparts, psi, batch, soa, msg, p0, eqt, row,
-      hasher, chal, fold, cvs, cvs_scratch, subtrees, status, phase, scratch_small;
+      hasher, chal, fold, cvs, cvs_scratch, subtrees, status, phase, scratch_small, wbuf, rbuf;
   uint32_t sign_key[8];
   std::vector<uint8_t> host_fold;
   cudaEvent_t ev[16];
@@ -399,20 +399,68 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   std::vector<f162> batch = eq_expand_f162(t.sample_f162("switch-batch", 7));
 
   // ---- switch rounds (reference.rs:150-161; sumcheck.rs:128-251) ----
-  const uint64_t n = sh.words;
-  CK(ctx->batch.ensure(128 * 24));
+  // Rounds r < HB from the partials' blocks folded bottom-up (no table read), then one table
+  // pass materialises the folded polynomial on the trailing 12 variables, and the last 12 rounds
+  // run on those 4096 entries.
+  const uint64_t nsmall = 4096;
+  const uint64_t xmax = 1ull << HB;
+  CK(ctx->batch.ensure(2 * 128 * 24));
   CK(ctx->psi.ensure(16 * 256 * 24));
-  CK(ctx->soa.ensure(6 * n * 8));
+  CK(ctx->soa.ensure(6 * nsmall * 8));
   CK(ctx->msg.ensure(6 * 8));
-  CK(cudaMemcpyAsync(ctx->batch.p, batch.data(), 128 * 24, cudaMemcpyHostToDevice, st));
-  launch_psi_tables(ctx->batch.as<f162>(), ctx->psi.as<f162>(), st);
-  uint64_t* sb = ctx->soa.as<uint64_t>();
-  Soa A = {sb, sb + n, sb + 2 * n}, P = {sb + 3 * n, sb + 4 * n, sb + 5 * n};
-  launch_switch_init(table, ctx->ehi.as<b128>(), ctx->elo.as<b128>(), LB, ctx->psi.as<f162>(), A, P, n, ctx->sms, st);
-  CKL("switch init");
+  CK(ctx->wbuf.ensure(2 * xmax * 24 + 48));
+  CK(ctx->rbuf.ensure((xmax > 2 ? xmax : 2) * 128 * 16));
+  f162* G[2] = {ctx->batch.as<f162>(), ctx->batch.as<f162>() + 128};
+  f162* W[2] = {ctx->wbuf.as<f162>(), ctx->wbuf.as<f162>() + xmax + 1};
+  const f162 one = {1, 0, 0};
+  CK(cudaMemcpyAsync(G[0], batch.data(), 128 * 24, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(W[0], &one, 24, cudaMemcpyHostToDevice, st));
+  // R_k for k = 1 .. HB - 1 (R_0 is the block array itself).
+  std::vector<const b128*> R(HB > 0 ? HB : 1);
+  if (HB > 0) R[0] = ctx->sblk.as<b128>();
+  {
+    size_t off = 0;
+    for (int k = 0; k + 1 < HB; ++k) {
+      const uint64_t nout = 1ull << (HB - k - 1);
+      b128* dst = ctx->rbuf.as<b128>() + off;
+      launch_rblock_level(R[k], nout, hi[HB - 1 - k], dst, st);
+      R[k + 1] = dst;
+      off += nout * 128;
+    }
+  }
+  int launches = HB > 1 ? HB - 1 : 0;
   std::vector<f162> coords, rounds;
-  uint64_t half = n;
-  for (int r = 0; r < sh.lp; ++r) {
+  int cur = 0;
+  for (int r = 0; r < HB; ++r) {
+    const uint64_t X = 1ull << r;
+    launch_psi_tables(G[cur], ctx->psi.as<f162>(), st);
+    CK(cudaMemsetAsync(ctx->msg.p, 0, 48, st));
+    launch_switch_round_blocks(R[HB - 1 - r], X, hi[r], ctx->psi.as<f162>(), W[cur],
+                               ctx->msg.as<unsigned long long>(), ctx->sms, st);
+    f162 m[2];
+    CK(cudaMemcpyAsync(m, ctx->msg.p, 48, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    t.absorb_f162(m, 2);
+    f162 rr = t.sample_f162("switch-round", 1)[0];
+    rounds.push_back(m[0]);
+    rounds.push_back(m[1]);
+    coords.push_back(rr);
+    launch_g_update(G[cur], hi[r], rr, G[cur ^ 1], st);
+    launch_w_update(W[cur], X, rr, W[cur ^ 1], st);
+    cur ^= 1;
+    launches += 4;
+  }
+  CKL("switch rounds on blocks");
+  uint64_t* sb = ctx->soa.as<uint64_t>();
+  Soa A = {sb, sb + nsmall, sb + 2 * nsmall}, P = {sb + 3 * nsmall, sb + 4 * nsmall, sb + 5 * nsmall};
+  launch_psi_tables(G[cur], ctx->psi.as<f162>(), st);
+  launch_phi_apply(ctx->elo.as<b128>(), nsmall, ctx->psi.as<f162>(), A, st);
+  CK(cudaMemsetAsync(P.w0, 0, 3 * nsmall * 8, st));
+  launch_materialize(table, W[cur], xmax, P, st);
+  launches += 3;
+  CKL("switch materialisation");
+  uint64_t half = nsmall;
+  for (int r = HB; r < sh.lp; ++r) {
     half >>= 1;
     CK(cudaMemsetAsync(ctx->msg.p, 0, 48, st));
     launch_switch_msg(A, P, half, ctx->msg.as<unsigned long long>(), ctx->sms, st);
@@ -425,6 +473,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
     rounds.push_back(m[1]);
     coords.push_back(rr);
     launch_switch_fold(A, P, half, rr, ctx->sms, st);
+    launches += 2;
   }
   CKL("switch rounds");
   f162 opened;
@@ -498,9 +547,9 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   ctx->prof.key_ms = ev_ms(ctx, 1, 2);
   ctx->prof.commit_ms = ev_ms(ctx, 2, 11);
   ctx->prof.finish_ms = ev_ms(ctx, 11, 3);
-  // Kernel launches of one proof: commit 2, stream hashing 2, partials 5, switch 2 + 2 per round,
+  // Kernel launches of one proof: commit 2, stream hashing 2, partials 5, switch (counted above),
   // row 2, challenges 1, fold 2.
-  ctx->prof.launches = 2 + 2 + 5 + 2 + 2 * sh.lp + 2 + 1 + 2;
+  ctx->prof.launches = 2 + 2 + 5 + launches + 2 + 1 + 2;
   ctx->prof.transcript_ms = ev_ms(ctx, 3, 4);
   ctx->prof.partials_ms = ev_ms(ctx, 4, 5);
   ctx->prof.switch_ms = ev_ms(ctx, 5, 6);
@@ -583,7 +632,7 @@ void lf_ctx_destroy(lf_ctx* ctx) {
   DevBuf* bufs[] = {&ctx->table, &ctx->stream_buf, &ctx->partial, &ctx->sblk, &ctx->ehi, &ctx->elo, &ctx->lo_planes,
                     &ctx->rhi, &ctx->vparts, &ctx->psi, &ctx->batch, &ctx->soa, &ctx->msg, &ctx->p0, &ctx->eqt,
                     &ctx->row, &ctx->hasher, &ctx->chal, &ctx->fold, &ctx->cvs, &ctx->cvs_scratch, &ctx->subtrees,
-                    &ctx->status, &ctx->phase, &ctx->scratch_small, &ctx->key.key};
+                    &ctx->status, &ctx->phase, &ctx->scratch_small, &ctx->wbuf, &ctx->rbuf, &ctx->key.key};
   for (DevBuf* b : bufs) b->release();
   for (auto& ev : ctx->ev) cudaEventDestroy(ev);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -138,7 +138,7 @@ __global__ void k_partials_combine(const b128* __restrict__ ehi, const uint8_t* 
 }
 
 // ---------------------------------------------------------------------------------------------
-// Switch, first version: a and p materialised (SoA limbs), rounds by field products.
+// Switch rounds on materialised a and p (SoA limbs): the last 12 rounds, 4096 entries.
 // ---------------------------------------------------------------------------------------------
 // psi_table (crossfield.rs:150-161): tab[c][m] = sum_{b in m} batch[8c + b].
 __global__ void k_psi_tables(const f162* __restrict__ batch, f162* __restrict__ tab) {
@@ -149,29 +149,6 @@ __global__ void k_psi_tables(const f162* __restrict__ batch, f162* __restrict__ 
   for (int b = 0; b < 8; ++b)
     if ((m >> b) & 1) v = f162_add(v, batch[8 * c + b]);
   tab[e] = v;
-}
-
-// a[j] = psi(E_hi[j >> lb] * E_lo[j & mask]), p[j] = lift(pi0[j]).
-__global__ void __launch_bounds__(256) k_switch_init(const uint4* __restrict__ table, const b128* __restrict__ ehi,
-                                                     const b128* __restrict__ elo, int lb, const f162* __restrict__ psi,
-                                                     Soa a, Soa p, uint64_t n) {
-  extern __shared__ __align__(16) uint64_t sm64[];
-  f162* tab = reinterpret_cast<f162*>(sm64);
-  for (int i = threadIdx.x; i < 16 * 256; i += blockDim.x) tab[i] = psi[i];
-  __syncthreads();
-  const uint64_t mask = (1ull << lb) - 1;
-  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
-    b128 e = b128_mul(ehi[j >> lb], elo[j & mask]);
-    f162 v = {0, 0, 0};
-#pragma unroll
-    for (int c = 0; c < 16; ++c) {
-      uint32_t byte = (uint32_t)((c < 8 ? e.lo >> (8 * c) : e.hi >> (8 * (c - 8))) & 0xff);
-      v = f162_add(v, tab[c * 256 + byte]);
-    }
-    a.put(j, v);
-    uint4 w = table[j];
-    p.put(j, {(uint64_t)w.x | ((uint64_t)w.y << 32), (uint64_t)w.z | ((uint64_t)w.w << 32), 0});
-  }
 }
 
 __device__ __forceinline__ f162 shfl_xor_f162(f162 v, int m) {
@@ -214,8 +191,190 @@ __global__ void __launch_bounds__(256) k_switch_fold(Soa a, Soa p, uint64_t half
 }
 
 // ---------------------------------------------------------------------------------------------
+// Switch from the partials' blocks (rounds r < HB = LP - 12).
+//
+// After r folds with challenges r'_0..r'_{r-1}, a_r[j] = Phi_r(E_r(j)), E_r = eq over
+// r_hi[r..LP], and Phi_r(y) = sum_b bit_b(y) G_r[b] is GF(2)-linear with G_0 = batch and
+// G_{r+1}[b] = (1 + r'_r) Phi_r((1 + rho_r) X^b) + r'_r Phi_r(rho_r X^b), rho_r = r_hi[r]
+// (the LeanSwitch algebra of crossfield.rs:1478-1509, without any division). The folded
+// p_r[j] = sum_x w_x lift(pi0[x || j]) with w_x = eq over r'_0..r'_{r-1}.
+// With the blocks S_h[c] = sum_jl bit_c(pi0[h, jl]) E_lo[jl] folded from the bottom,
+// R_k[e][c] = sum_l eq(r_hi[HB-k..HB], l) S_{e 2^k + l}[c], the round message is
+//   e0   = sum_x w_x sum_c X^c Phi_r((1 + rho_r) R[2x][c]),
+//   einf = sum_x w_x sum_c X^c Phi_r(R[2x][c] + R[2x + 1][c]),   R = R_{HB - r - 1},
+// so these rounds read no table word; one pass then materialises p_HB (4096 entries).
+// ---------------------------------------------------------------------------------------------
+// R_{k+1}[i][c] = (1 + rho) R_k[2i][c] + rho R_k[2i + 1][c]
+__global__ void k_rblock_level(const b128* __restrict__ in, uint64_t nout, b128 rho, b128* __restrict__ out) {
+  uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (t >= nout * 128) return;
+  const uint64_t i = t >> 7, c = t & 127;
+  const b128 v0 = in[(2 * i) * 128 + c], v1 = in[(2 * i + 1) * 128 + c];
+  // (1 + rho) v0 + rho v1 = v0 + rho (v0 + v1)
+  out[t] = b128_add(v0, b128_mul(rho, b128_add(v0, v1)));
+}
+
+// x * X^c modulo x^162 + x^81 + 1, c < 128
+__device__ __forceinline__ f162 f162_shift(f162 f, int c) {
+  uint64_t w[6] = {f.w0, f.w1, f.w2, 0, 0, 0};
+  if (c >= 64) {
+    w[3] = w[2], w[2] = w[1], w[1] = w[0], w[0] = 0;
+    c -= 64;
+  }
+  if (c) {
+    w[4] = w[3] >> (64 - c);
+    w[3] = (w[3] << c) | (w[2] >> (64 - c));
+    w[2] = (w[2] << c) | (w[1] >> (64 - c));
+    w[1] = (w[1] << c) | (w[0] >> (64 - c));
+    w[0] = w[0] << c;
+  }
+  return f162_reduce(w[0], w[1], w[2], w[3], w[4], 0);
+}
+
+__device__ __forceinline__ f162 phi_apply(const f162* tab, b128 e) {
+  f162 v = {0, 0, 0};
+#pragma unroll
+  for (int c = 0; c < 16; ++c) {
+    uint32_t byte = (uint32_t)((c < 8 ? e.lo >> (8 * c) : e.hi >> (8 * (c - 8))) & 0xff);
+    v = f162_add(v, tab[c * 256 + byte]);
+  }
+  return v;
+}
+
+// One round's message from R (2X entries of 128 columns). Block of 128 threads: thread = column.
+__global__ void __launch_bounds__(128) k_switch_round_blocks(const b128* __restrict__ R, uint64_t X, b128 rho,
+                                                            const f162* __restrict__ phi, const f162* __restrict__ w,
+                                                            unsigned long long* __restrict__ msg) {
+  extern __shared__ __align__(16) uint64_t sm64[];
+  f162* tab = reinterpret_cast<f162*>(sm64);
+  for (int i = threadIdx.x; i < 16 * 256; i += blockDim.x) tab[i] = phi[i];
+  __syncthreads();
+  __shared__ f162 part[2][4];
+  const int c = threadIdx.x, lane = c & 31, warp = c >> 5;
+  const b128 one_rho = {rho.lo ^ 1, rho.hi};
+  f162 e0 = {0, 0, 0}, ei = {0, 0, 0};
+  for (uint64_t x = blockIdx.x; x < X; x += gridDim.x) {
+    const b128 v0 = R[(2 * x) * 128 + c], v1 = R[(2 * x + 1) * 128 + c];
+    f162 s0 = f162_shift(phi_apply(tab, b128_mul(one_rho, v0)), c);
+    f162 si = f162_shift(phi_apply(tab, b128_add(v0, v1)), c);
+    for (int m = 16; m; m >>= 1) {
+      s0.w0 ^= __shfl_xor_sync(0xffffffffu, s0.w0, m);
+      s0.w1 ^= __shfl_xor_sync(0xffffffffu, s0.w1, m);
+      s0.w2 ^= __shfl_xor_sync(0xffffffffu, s0.w2, m);
+      si.w0 ^= __shfl_xor_sync(0xffffffffu, si.w0, m);
+      si.w1 ^= __shfl_xor_sync(0xffffffffu, si.w1, m);
+      si.w2 ^= __shfl_xor_sync(0xffffffffu, si.w2, m);
+    }
+    if (lane == 0) part[0][warp] = s0, part[1][warp] = si;
+    __syncthreads();
+    if (c == 0) {
+      f162 a0 = f162_add(f162_add(part[0][0], part[0][1]), f162_add(part[0][2], part[0][3]));
+      f162 ai = f162_add(f162_add(part[1][0], part[1][1]), f162_add(part[1][2], part[1][3]));
+      const f162 wx = w[x];
+      e0 = f162_add(e0, f162_mul(wx, a0));
+      ei = f162_add(ei, f162_mul(wx, ai));
+    }
+    __syncthreads();
+  }
+  if (c == 0) {
+    atomicXor(&msg[0], (unsigned long long)e0.w0);
+    atomicXor(&msg[1], (unsigned long long)e0.w1);
+    atomicXor(&msg[2], (unsigned long long)e0.w2);
+    atomicXor(&msg[3], (unsigned long long)ei.w0);
+    atomicXor(&msg[4], (unsigned long long)ei.w1);
+    atomicXor(&msg[5], (unsigned long long)ei.w2);
+  }
+}
+
+// G_{r+1}[b] = Phi_r(y1) + r' (Phi_r(y1) + Phi_r(y2)), y1 = (1 + rho) X^b, y2 = rho X^b.
+__global__ void k_g_update(const f162* __restrict__ G, b128 rho, f162 rp, f162* __restrict__ Gn) {
+  __shared__ f162 g[128];
+  const int b = threadIdx.x;
+  g[b] = G[b];
+  __syncthreads();
+  b128 xb = {b < 64 ? 1ull << b : 0, b >= 64 ? 1ull << (b - 64) : 0};
+  b128 y2 = b128_mul(rho, xb);
+  b128 y1 = b128_add(xb, y2);
+  f162 p1 = {0, 0, 0}, p2 = {0, 0, 0};
+  for (int k = 0; k < 128; ++k) {
+    if (b128_bit(y1, k)) p1 = f162_add(p1, g[k]);
+    if (b128_bit(y2, k)) p2 = f162_add(p2, g[k]);
+  }
+  Gn[b] = f162_add(p1, f162_mul(rp, f162_add(p1, p2)));
+}
+
+// w_{r+1}[2x] = (1 + r') w_r[x], w_{r+1}[2x + 1] = r' w_r[x]
+__global__ void k_w_update(const f162* __restrict__ w, uint64_t X, f162 rp, f162* __restrict__ wn) {
+  uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (x >= X) return;
+  const f162 t = f162_mul(w[x], rp);
+  wn[2 * x] = f162_add(w[x], t);
+  wn[2 * x + 1] = t;
+}
+
+// a[j] = Phi(E_lo[j]) for the 4096 low entries.
+__global__ void __launch_bounds__(256) k_phi_apply(const b128* __restrict__ e, uint64_t n, const f162* __restrict__ phi,
+                                                   Soa a) {
+  extern __shared__ __align__(16) uint64_t sm64[];
+  f162* tab = reinterpret_cast<f162*>(sm64);
+  for (int i = threadIdx.x; i < 16 * 256; i += blockDim.x) tab[i] = phi[i];
+  __syncthreads();
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x)
+    a.put(j, phi_apply(tab, e[j]));
+}
+
+// p[j] = sum_x w[x] lift(pi0[x 2^12 + j]) for j < 4096: block (j tile of 256, x share).
+__global__ void __launch_bounds__(256) k_materialize(const uint4* __restrict__ table, const f162* __restrict__ w,
+                                                     uint64_t X, uint64_t x_share, Soa p) {
+  const uint64_t j = blockIdx.x * 256ull + threadIdx.x;
+  const uint64_t x0 = blockIdx.y * x_share, x1 = min(X, x0 + x_share);
+  f162 acc = {0, 0, 0};
+  for (uint64_t x = x0; x < x1; ++x) {
+    const uint4 v = table[(x << 12) + j];
+    const b128 b = {(uint64_t)v.x | ((uint64_t)v.y << 32), (uint64_t)v.z | ((uint64_t)v.w << 32)};
+    acc = f162_add(acc, f162_mul_lifted(w[x], b));
+  }
+  atomicXor(reinterpret_cast<unsigned long long*>(p.w0 + j), (unsigned long long)acc.w0);
+  atomicXor(reinterpret_cast<unsigned long long*>(p.w1 + j), (unsigned long long)acc.w1);
+  atomicXor(reinterpret_cast<unsigned long long*>(p.w2 + j), (unsigned long long)acc.w2);
+}
+
+// ---------------------------------------------------------------------------------------------
 // Launch wrappers
 // ---------------------------------------------------------------------------------------------
+void launch_rblock_level(const b128* in, uint64_t nout, b128 rho, b128* out, cudaStream_t s) {
+  uint64_t n = nout * 128;
+  k_rblock_level<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, nout, rho, out);
+}
+void launch_switch_round_blocks(const b128* R, uint64_t X, b128 rho, const f162* phi, const f162* w,
+                                unsigned long long* msg, int sms, cudaStream_t s) {
+  const int smem = 16 * 256 * 24;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_switch_round_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr = true;
+  }
+  unsigned g = (unsigned)(X < (uint64_t)sms ? X : (uint64_t)sms);
+  k_switch_round_blocks<<<g, 128, smem, s>>>(R, X, rho, phi, w, msg);
+}
+void launch_g_update(const f162* G, b128 rho, f162 rp, f162* Gn, cudaStream_t s) { k_g_update<<<1, 128, 0, s>>>(G, rho, rp, Gn); }
+void launch_w_update(const f162* w, uint64_t X, f162 rp, f162* wn, cudaStream_t s) {
+  k_w_update<<<(unsigned)((X + 127) / 128), 128, 0, s>>>(w, X, rp, wn);
+}
+void launch_phi_apply(const b128* e, uint64_t n, const f162* phi, Soa a, cudaStream_t s) {
+  const int smem = 16 * 256 * 24;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_phi_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr = true;
+  }
+  k_phi_apply<<<16, 256, smem, s>>>(e, n, phi, a);
+}
+void launch_materialize(const uint4* table, const f162* w, uint64_t X, Soa p, cudaStream_t s) {
+  uint64_t shares = X >= 64 ? 64 : X;
+  uint64_t x_share = (X + shares - 1) / shares;
+  k_materialize<<<dim3(16, (unsigned)shares), 256, 0, s>>>(table, w, X, x_share, p);
+}
 static unsigned grid_for(uint64_t n, int threads, unsigned cap) {
   uint64_t g = (n + threads - 1) / threads;
   if (g > cap) g = cap;
@@ -247,16 +406,6 @@ void launch_partials_combine(const b128* ehi, const uint8_t* sblk, int nblocks, 
   k_partials_combine<<<(nblocks + run - 1) / run, 128, 0, s>>>(ehi, sblk, nblocks, run, v);
 }
 void launch_psi_tables(const f162* batch, f162* tab, cudaStream_t s) { k_psi_tables<<<16, 256, 0, s>>>(batch, tab); }
-void launch_switch_init(const uint4* table, const b128* ehi, const b128* elo, int lb, const f162* psi, Soa a, Soa p,
-                        uint64_t n, int sms, cudaStream_t s) {
-  const int smem = 16 * 256 * 24;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_switch_init, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    attr = true;
-  }
-  k_switch_init<<<grid_for(n, 256, sms * 2), 256, smem, s>>>(table, ehi, elo, lb, psi, a, p, n);
-}
 void launch_switch_msg(Soa a, Soa p, uint64_t half, unsigned long long* msg, int sms, cudaStream_t s) {
   k_switch_msg<<<grid_for(half, 256, sms * 8), 256, 0, s>>>(a, p, half, msg);
 }
