@@ -176,7 +176,8 @@ struct KeyCache {
   u128 q = 0;
   uint64_t elements = 0;
   ModulusPlan mp;
-  DevBuf key;
+  DevBuf key;  // u32 [prime][element][leaf][k][l]: the 4x4 base-multiplication matrix per leaf
+  DevBuf t2;   // u32 [prime][T2_WORDS]: the fused lookup tables of the commitment kernel
 };
 
 }  // namespace
@@ -254,10 +255,12 @@ int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh) {
   DevBuf ared, leaf;
   CK(ared.ensure((size_t)mp.nprimes * E * RING_N * 4));
   CK(leaf.ensure((size_t)mp.nprimes * E * 4 * LEAVES * 4));
-  CK(ctx->key.key.ensure((size_t)mp.nprimes * E * LEAVES * 16 * 2));
+  CK(ctx->key.key.ensure((size_t)mp.nprimes * E * LEAVES * 16 * 4));
+  CK(ctx->key.t2.ensure(mp.t2.size() * 4));
+  CK(cudaMemcpyAsync(ctx->key.t2.p, mp.t2.data(), mp.t2.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
   upload_prime_consts(mp, ctx->stream);
   launch_matrix_expand(mp, E, ared.as<uint32_t>(), ctx->stream);
-  launch_key_transform(mp, E, ared.as<uint32_t>(), leaf.as<uint32_t>(), ctx->key.key.as<uint16_t>(), ctx->stream);
+  launch_key_transform(mp, E, ared.as<uint32_t>(), leaf.as<uint32_t>(), ctx->key.key.as<uint32_t>(), ctx->stream);
   CKL("key build");
   CK(cudaStreamSynchronize(ctx->stream));
   ared.release();
@@ -301,11 +304,12 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   cudaEventRecord(ctx->ev[2], st);
 
   // ---- commitment (K1 + K2), written after the 112 transcript prefix bytes of the stream ----
-  const int splits = commit_splits(sh.ring_elements);
+  const int splits = commit_splits(sh.ring_elements, ctx->key.mp.nprimes, ctx->sms);
   const ModulusPlan& mp = ctx->key.mp;
   CK(ctx->partial.ensure((size_t)splits * mp.nprimes * COLUMNS * LEAVES * 4 * 4));
   CK(ctx->stream_buf.ensure(STREAM_PREFIX + commit_bytes + 1024));
-  launch_commit(mp, sh, table, ctx->key.key.as<uint16_t>(), ctx->partial.as<uint32_t>(), splits, st);
+  launch_commit(mp, sh, table, ctx->key.key.as<uint32_t>(), ctx->key.t2.as<uint32_t>(), ctx->partial.as<uint32_t>(),
+                splits, st);
   cudaEventRecord(ctx->ev[11], st);
   launch_commit_finish(mp, sh, ctx->partial.as<uint32_t>(), splits, ctx->stream_buf.as<uint8_t>() + STREAM_PREFIX, st);
   CKL("commitment");
@@ -632,7 +636,7 @@ void lf_ctx_destroy(lf_ctx* ctx) {
   DevBuf* bufs[] = {&ctx->table, &ctx->stream_buf, &ctx->partial, &ctx->sblk, &ctx->ehi, &ctx->elo, &ctx->lo_planes,
                     &ctx->rhi, &ctx->vparts, &ctx->psi, &ctx->batch, &ctx->soa, &ctx->msg, &ctx->p0, &ctx->eqt,
                     &ctx->row, &ctx->hasher, &ctx->chal, &ctx->fold, &ctx->cvs, &ctx->cvs_scratch, &ctx->subtrees,
-                    &ctx->status, &ctx->phase, &ctx->scratch_small, &ctx->wbuf, &ctx->rbuf, &ctx->key.key};
+                    &ctx->status, &ctx->phase, &ctx->scratch_small, &ctx->wbuf, &ctx->rbuf, &ctx->key.key, &ctx->key.t2};
   for (DevBuf* b : bufs) b->release();
   for (auto& ev : ctx->ev) cudaEventDestroy(ev);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -124,6 +124,23 @@ static void fill_consts(const PrimePlan& pl, PrimeConst& c) {
   for (int s = 0; s < LEAVES; ++s) c.leaf_root[s] = (uint32_t)pw(pl.leaf_e[s]);
 }
 
+// The level-2 split fused into the lookups: output (child a, position q < 9) of level-2 node sb
+// is sum_t omega^(a t) tau^t T[sb][idx(q + 9 t)], tau = eta^(e/3) of node sb; entry
+// [sb][a][t][idx] holds omega^(a t) tau^t T[sb][idx].
+static void fill_t2(const PrimePlan& pl, const PrimeConst& c, uint32_t* t2) {
+  const uint64_t p = pl.p;
+  auto pw = [&](int64_t e) { return (uint64_t)pl.pw[((e % 486) + 486) % 486]; };
+  for (int sb = 0; sb < 6; ++sb) {
+    const uint64_t tau = pw(pl.node_e[2][sb] / 3);
+    for (int a = 0; a < 3; ++a)
+      for (int t = 0; t < 3; ++t) {
+        uint64_t f = pw(162 * ((a * t) % 3));
+        for (int i = 0; i < t; ++i) f = f * tau % p;
+        for (int idx = 0; idx < 32; ++idx) t2[((sb * 3 + a) * 3 + t) * 32 + idx] = (uint32_t)(f * c.T[sb][idx] % p);
+      }
+  }
+}
+
 static uint32_t bits_of(u128 x) {
   uint32_t n = 0;
   while (x) ++n, x >>= 1;
@@ -145,6 +162,7 @@ bool make_modulus_plan(u128 q, ModulusPlan& mp, std::string& err) {
     return false;
   }
   mp.consts.resize(mp.nprimes);
+  mp.t2.assign((size_t)mp.nprimes * T2_WORDS, 0);
   for (int i = 0; i < mp.nprimes; ++i) {
     PrimePlan pl;
     if (!make_plan(mp.primes[i], pl)) {
@@ -152,6 +170,7 @@ bool make_modulus_plan(u128 q, ModulusPlan& mp, std::string& err) {
       return false;
     }
     fill_consts(pl, mp.consts[i]);
+    fill_t2(pl, mp.consts[i], mp.t2.data() + (size_t)i * T2_WORDS);
     for (int j = 0; j < i; ++j) mp.garner_inv[i][j] = inv_mod(mp.primes[j], mp.primes[i]);
   }
   return true;
@@ -292,7 +311,7 @@ __global__ void k_key_forward(int nprimes, uint64_t elements, const uint32_t* ar
   for (int s = 0; s < LEAVES; ++s) o[s] = x[s];
 }
 
-__global__ void k_key_leafform(int nprimes, uint64_t elements, const uint32_t* leafvals, uint16_t* key) {
+__global__ void k_key_leafform(int nprimes, uint64_t elements, const uint32_t* leafvals, uint32_t* key) {
   uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   uint64_t total = (uint64_t)nprimes * elements * LEAVES;
   if (tid >= total) return;
@@ -304,13 +323,13 @@ __global__ void k_key_leafform(int nprimes, uint64_t elements, const uint32_t* l
   const uint32_t* lv = leafvals + ((size_t)pi * elements + m) * 4 * LEAVES;
   uint64_t A[4];
   for (int k = 0; k < 4; ++k) A[k] = lv[k * LEAVES + s];
-  uint16_t* o = key + (((size_t)pi * elements + m) * LEAVES + s) * 16;
+  uint32_t* o = key + (((size_t)pi * elements + m) * LEAVES + s) * 16;
   for (int k = 0; k < 4; ++k)
-    for (int l = 0; l < 4; ++l) o[4 * k + l] = (uint16_t)(l >= k ? A[l - k] : c * A[l - k + 4] % p);
+    for (int l = 0; l < 4; ++l) o[4 * k + l] = (uint32_t)(l >= k ? A[l - k] : c * A[l - k + 4] % p);
 }
 
 void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32_t* ared, uint32_t* leafvals,
-                          uint16_t* key, cudaStream_t s) {
+                          uint32_t* key, cudaStream_t s) {
   uint64_t t1 = (uint64_t)mp.nprimes * elements * 4;
   k_key_forward<<<(unsigned)((t1 + 127) / 128), 128, 0, s>>>(mp.nprimes, elements, ared, leafvals);
   uint64_t t2 = (uint64_t)mp.nprimes * elements * LEAVES;
@@ -319,14 +338,17 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
 
 // ------------------------------------------------------------------------------------------------
 // K1: the commitment in the transform domain.
-//   grid  (COLUMNS / 32 column tiles, primes, element splits); block 192 = 6 warps.
-//   warp w = level-2 node (sub-block) w of every word; lane = column of the tile.
-// Each thread keeps, for its column, the 27 leaves of its sub-block times the 4 coefficients
-// of X (108 u32 accumulators) over its split of the elements.
+//   grid  (COLUMNS / 32 column tiles, primes, element splits); block 576 = 18 warps.
+//   warp w = (level-2 node sb = w / 3, level-3 node a = w % 3) of every word; lane = column.
+// A thread produces, per table word, the 9 leaves of its level-3 node: the first three levels
+// (trinomial split, level-1 split, the level-2 split into node a) are three lookups in
+// twiddled 32-entry tables, then two radix-3 levels; at each leaf it multiplies with the key's
+// 4x4 base-multiplication matrix and accumulates 9 x 4 u32 over its split of the elements.
 // ------------------------------------------------------------------------------------------------
 constexpr int CT = 32;
-constexpr int MB = 4;
-constexpr int KTHREADS = 192;
+constexpr int MB = 8;
+constexpr int KWARPS = 18;
+constexpr int KTHREADS = 32 * KWARPS;
 
 // One radix-3 split of a node: inputs a (untwiddled), b, c; outputs in place.
 __device__ __forceinline__ void split3(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t t1, uint32_t t1s, uint32_t t2,
@@ -346,26 +368,35 @@ __device__ __forceinline__ uint32_t word_index_byte(uint32_t r0, uint32_t r1, ui
          (((r4 >> q) & 1) << 4);
 }
 
-__global__ void __launch_bounds__(KTHREADS, 2)
-    k_commit_ntt(const uint4* __restrict__ table, const uint16_t* __restrict__ key, uint32_t* __restrict__ partial,
-                 int rl, int elements, int per_split, int nprimes, int reduce_every) {
+size_t commit_smem_bytes() { return (size_t)(T2_WORDS + MB * LEAVES * 16) * 4 + (size_t)MB * CT * 27 * 4; }
+
+__global__ void __launch_bounds__(KTHREADS, 1)
+    k_commit_ntt(const uint4* __restrict__ table, const uint32_t* __restrict__ key, const uint32_t* __restrict__ t2g,
+                 uint32_t* __restrict__ partial, int rl, int elements, int per_split, int nprimes, int reduce_every) {
+  extern __shared__ __align__(16) uint32_t csm[];
+  uint32_t* sT2 = csm;                                  // [sb][a][t][32]
+  uint32_t* sKey = csm + T2_WORDS;                      // [MB][162][k][l]
+  uint8_t* sIdx = reinterpret_cast<uint8_t*>(sKey + MB * LEAVES * 16);  // [MB][CT][27][k]
   const int pi = blockIdx.y;
   const int col0 = blockIdx.x * CT;
   const int split = blockIdx.z;
   const int m_begin = split * per_split;
   const int m_end = min(elements, m_begin + per_split);
-  const int lane = threadIdx.x & 31, sb = threadIdx.x >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int sb = warp / 3, na = warp % 3;
   const PrimeConst& P = c_prime[pi];
   const uint32_t p = P.p;
+  for (int i = tid; i < T2_WORDS; i += KTHREADS) sT2[i] = t2g[pi * T2_WORDS + i];
+  const uint32_t* t20 = sT2 + ((sb * 3 + na) * 3 + 0) * 32;
+  const uint32_t* t21 = t20 + 32;
+  const uint32_t* t22 = t20 + 64;
+  // warp-uniform twiddles of the level-3 node (3 sb + na) and its three level-4 children
+  const uint32_t w3a = P.tw[sb][1 + na][0], w3as = P.tws[sb][1 + na][0];
+  const uint32_t w3b = P.tw[sb][1 + na][1], w3bs = P.tws[sb][1 + na][1];
 
-  __shared__ uint32_t sT[6][32];
-  __shared__ __align__(16) uint16_t sKey[MB][LEAVES][16];
-  __shared__ uint32_t sIdx[MB][CT][27];
-  sT[sb][lane] = P.T[sb][lane];
-
-  uint32_t acc[27][4];
+  uint32_t acc[9][4];
 #pragma unroll
-  for (int q = 0; q < 27; ++q)
+  for (int q = 0; q < 9; ++q)
 #pragma unroll
     for (int l = 0; l < 4; ++l) acc[q][l] = 0;
 
@@ -375,83 +406,68 @@ __global__ void __launch_bounds__(KTHREADS, 2)
     __syncthreads();
     {
       const uint4* src = reinterpret_cast<const uint4*>(key + ((size_t)pi * elements + mc) * LEAVES * 16);
-      uint4* dst = reinterpret_cast<uint4*>(&sKey[0][0][0]);
-      for (int i = threadIdx.x; i < nm * LEAVES * 2; i += KTHREADS) dst[i] = src[i];
+      uint4* dst = reinterpret_cast<uint4*>(sKey);
+      for (int i = tid; i < nm * LEAVES * 4; i += KTHREADS) dst[i] = src[i];
     }
-    for (int task = threadIdx.x; task < nm * CT; task += KTHREADS) {
-      const int ml = task / CT, c = task % CT;
-      const uint4* w = table + ((size_t)(col0 + c) << rl) + 4 * (size_t)(mc + ml);
-      uint32_t packed[27];
+    // 27 five-bit indices per table word, one word per task: bits q, q+27, q+54, q+81, q+108.
+    for (int task = tid; task < nm * CT * 4; task += KTHREADS) {
+      const int k = task & 3, c = (task >> 2) % CT, ml = (task >> 2) / CT;
+      const uint4 v = table[((size_t)(col0 + c) << rl) + 4 * (size_t)(mc + ml) + k];
+      const uint32_t M27 = (1u << 27) - 1;
+      const uint32_t r0 = v.x & M27;
+      const uint32_t r1 = ((v.x >> 27) | (v.y << 5)) & M27;
+      const uint32_t r2 = ((v.y >> 22) | (v.z << 10)) & M27;
+      const uint32_t r3 = ((v.z >> 17) | (v.w << 15)) & M27;
+      const uint32_t r4 = (v.w >> 12) & M27;
+      uint8_t* dst = sIdx + ((size_t)(ml * CT + c) * 27) * 4 + k;
 #pragma unroll
-      for (int q = 0; q < 27; ++q) packed[q] = 0;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        uint4 v = w[k];
-        const uint32_t M27 = (1u << 27) - 1;
-        uint32_t r0 = v.x & M27;
-        uint32_t r1 = ((v.x >> 27) | (v.y << 5)) & M27;
-        uint32_t r2 = ((v.y >> 22) | (v.z << 10)) & M27;
-        uint32_t r3 = ((v.z >> 17) | (v.w << 15)) & M27;
-        uint32_t r4 = (v.w >> 12) & M27;
-#pragma unroll
-        for (int q = 0; q < 27; ++q) packed[q] |= word_index_byte(r0, r1, r2, r3, r4, q) << (8 * k);
-      }
-#pragma unroll
-      for (int q = 0; q < 27; ++q) sIdx[ml][c][q] = packed[q];
+      for (int q = 0; q < 27; ++q) dst[4 * q] = (uint8_t)word_index_byte(r0, r1, r2, r3, r4, q);
     }
     __syncthreads();
 
     for (int ml = 0; ml < nm; ++ml) {
+      const uint8_t* ib = sIdx + ((size_t)(ml * CT + lane) * 27) * 4;
+      const uint32_t* kb = sKey + ((size_t)ml * LEAVES + 27 * sb + 9 * na) * 16;
 #pragma unroll 1
       for (int k = 0; k < 4; ++k) {
-        uint32_t x[27];
+        uint32_t x[9];
 #pragma unroll
-        for (int q = 0; q < 27; ++q) x[q] = sT[sb][(sIdx[ml][lane][q] >> (8 * k)) & 31];
-        // level-2 node (27 -> 3 x 9)
+        for (int q = 0; q < 9; ++q) x[q] = t20[ib[4 * q + k]] + t21[ib[4 * (q + 9) + k]] + t22[ib[4 * (q + 18) + k]];
+        // level-3 node (9 -> 3 x 3)
 #pragma unroll
-        for (int q = 0; q < 9; ++q)
-          split3(x[q], x[q + 9], x[q + 18], P.tw[sb][0][0], P.tws[sb][0][0], P.tw[sb][0][1], P.tws[sb][0][1], P.om,
-                 P.om_s, p);
-        // level-3 nodes (9 -> 3 x 3)
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int q = 0; q < 3; ++q)
-            split3(x[9 * a + q], x[9 * a + q + 3], x[9 * a + q + 6], P.tw[sb][1 + a][0], P.tws[sb][1 + a][0],
-                   P.tw[sb][1 + a][1], P.tws[sb][1 + a][1], P.om, P.om_s, p);
+        for (int q = 0; q < 3; ++q) split3(x[q], x[q + 3], x[q + 6], w3a, w3as, w3b, w3bs, P.om, P.om_s, p);
         // level-4 nodes (3 -> leaves)
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int b = 0; b < 3; ++b) {
-            const int t = 4 + 3 * a + b, o = 9 * a + 3 * b;
-            split3(x[o], x[o + 1], x[o + 2], P.tw[sb][t][0], P.tws[sb][t][0], P.tw[sb][t][1], P.tws[sb][t][1], P.om,
-                   P.om_s, p);
-          }
+        for (int b = 0; b < 3; ++b) {
+          const int t = 4 + 3 * na + b;
+          split3(x[3 * b], x[3 * b + 1], x[3 * b + 2], P.tw[sb][t][0], P.tws[sb][t][0], P.tw[sb][t][1],
+                 P.tws[sb][t][1], P.om, P.om_s, p);
+        }
         // Base multiplication with the key's leaves: acc[q][l] += M[k][l] x[q].
 #pragma unroll
-        for (int q = 0; q < 27; ++q) {
+        for (int q = 0; q < 9; ++q) {
           uint32_t v = x[q] - __umulhi(x[q], P.bar) * p;
           v = v >= p ? v - p : v;
-          const uint2 kv = *reinterpret_cast<const uint2*>(&sKey[ml][27 * sb + q][4 * k]);
-          acc[q][0] += (kv.x & 0xffff) * v;
-          acc[q][1] += (kv.x >> 16) * v;
-          acc[q][2] += (kv.y & 0xffff) * v;
-          acc[q][3] += (kv.y >> 16) * v;
+          const uint4 kv = *reinterpret_cast<const uint4*>(kb + q * 16 + 4 * k);
+          acc[q][0] += kv.x * v;
+          acc[q][1] += kv.y * v;
+          acc[q][2] += kv.z * v;
+          acc[q][3] += kv.w * v;
         }
       }
       if (++since == reduce_every) {
         since = 0;
 #pragma unroll
-        for (int q = 0; q < 27; ++q)
+        for (int q = 0; q < 9; ++q)
 #pragma unroll
           for (int l = 0; l < 4; ++l) acc[q][l] = reduce32(acc[q][l], P.bar, p);
       }
     }
   }
-  uint32_t* out = partial + ((((size_t)split * nprimes + pi) * COLUMNS + col0 + lane) * LEAVES + 27 * sb) * 4;
+  uint32_t* out =
+      partial + ((((size_t)split * nprimes + pi) * COLUMNS + col0 + lane) * LEAVES + 27 * sb + 9 * na) * 4;
 #pragma unroll
-  for (int q = 0; q < 27; ++q) {
+  for (int q = 0; q < 9; ++q) {
     uint4 v;
     v.x = reduce32(acc[q][0], P.bar, p);
     v.y = reduce32(acc[q][1], P.bar, p);
@@ -461,14 +477,28 @@ __global__ void __launch_bounds__(KTHREADS, 2)
   }
 }
 
-int commit_splits(uint64_t elements) {
-  int s = 16;
-  while (s > 1 && (uint64_t)s > elements) s >>= 1;
-  return s;
+// Element splits of K1: the grid (32 column tiles x primes x splits) at one block per SM should
+// fill whole waves; among 8..24 splits take the one with the least idle SM time, then the fewest.
+int commit_splits(uint64_t elements, int nprimes, int sms) {
+  if (sms < 1) sms = 1;
+  int best = 1;
+  double best_eff = -1;
+  for (int s = 8; s <= 24; ++s) {
+    if ((uint64_t)s * MB > elements) break;
+    const long blocks = (long)(COLUMNS / CT) * nprimes * s;
+    const long waves = (blocks + sms - 1) / sms;
+    const double eff = (double)blocks / (double)(waves * sms);
+    if (eff > best_eff + 1e-9) best_eff = eff, best = s;
+  }
+  if (best_eff < 0) {
+    best = 1;
+    while ((uint64_t)best * 2 * MB <= elements && best < 8) best *= 2;
+  }
+  return best;
 }
 
-void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint16_t* key, uint32_t* partial,
-                   int splits, cudaStream_t s) {
+void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint32_t* key, const uint32_t* t2,
+                   uint32_t* partial, int splits, cudaStream_t s) {
   int elements = (int)sh.ring_elements;
   int per = (elements + splits - 1) / splits;
   // Accumulators take 4 products below p^2 per element; reduce before 2^32 can be reached.
@@ -478,7 +508,13 @@ void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, c
   int reduce_every = (int)((0xffffffffull - pmax) / per_elem);
   if (reduce_every < 1) reduce_every = 1;
   dim3 grid(COLUMNS / CT, mp.nprimes, splits);
-  k_commit_ntt<<<grid, KTHREADS, 0, s>>>(table, key, partial, sh.rl, elements, per, mp.nprimes, reduce_every);
+  const size_t smem = commit_smem_bytes();
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_commit_ntt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  k_commit_ntt<<<grid, KTHREADS, smem, s>>>(table, key, t2, partial, sh.rl, elements, per, mp.nprimes, reduce_every);
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -18,6 +18,7 @@ constexpr int LEAVES = 162;      // slots of the transform over Y = X^4
 constexpr int COLUMN_LOG = 10;   // verifier/proof_verify/src/main.rs:37
 constexpr int COLUMNS = 1 << COLUMN_LOG;
 constexpr int MAX_PRIMES = 12;
+constexpr int T2_WORDS = 6 * 3 * 3 * 32;  // per prime: [sb][a][t][32]
 constexpr int STREAM_PREFIX = 112;  // transcript bytes before the commitment (see host code)
 
 // The shape of one instance, derived from LOG_VARS (main.rs:32-46).
@@ -69,6 +70,9 @@ struct ModulusPlan {
   uint32_t primes[MAX_PRIMES];
   bool exact_lift = false;         // true: CRT gives the integer product, reduced mod q after
   std::vector<PrimeConst> consts;
+  // Per prime, the level-2 split fused into the lookups: [sb][child a][term t][32] (lives in global
+  // memory; too large for the constant bank at 12 primes).
+  std::vector<uint32_t> t2;
   // Garner constants: inv[i][j] = p_j^-1 mod p_i for j < i
   uint32_t garner_inv[MAX_PRIMES][MAX_PRIMES];
 };
@@ -133,9 +137,10 @@ void upload_prime_consts(const ModulusPlan& mp, cudaStream_t s);
 void launch_matrix_expand(const ModulusPlan& mp, uint64_t elements, uint32_t* ared, cudaStream_t s);
 // Leaf-form key: key[prime][m][162][16] u16.
 void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32_t* ared, uint32_t* leafvals,
-                          uint16_t* key, cudaStream_t s);
-int commit_splits(uint64_t elements);
-void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint16_t* key,
+                          uint32_t* key, cudaStream_t s);
+int commit_splits(uint64_t elements, int nprimes, int sms);
+size_t commit_smem_bytes();
+void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint32_t* key, const uint32_t* t2,
                    uint32_t* partial, int splits, cudaStream_t s);
 void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t* partial, int splits,
                           uint8_t* out, cudaStream_t s);
