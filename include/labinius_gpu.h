@@ -28,6 +28,7 @@ extern "C" {
 #define LF_E_CUDA (-7)      /* a CUDA call failed; see lf_last_error() */
 #define LF_E_INTERNAL (-8)  /* a device-side check failed (challenge sampling bound, fold range) */
 #define LF_E_ADMISSION (-9) /* the request does not fit the context's HBM budget */
+#define LF_E_LIMIT (-10)    /* the request exceeds a fixed-size scratch (lf_sample_challenges_noalloc) */
 
 typedef struct lf_ctx lf_ctx;
 
@@ -98,6 +99,18 @@ int lf_sample_challenges(lf_ctx* ctx, const char* domain, const uint8_t* prefix,
  * and lane 0's squared norm. */
 int lf_sample_challenges_traced(lf_ctx* ctx, const char* domain, const uint8_t* prefix, size_t prefix_len, uint32_t n,
                                 uint8_t* out, uint32_t* trace64);
+/* lf_sample_challenges without a context and without allocating device memory. No counterpart
+ * in the reference (its sampler runs on the host, challenge.rs:707-737); it exists for callers
+ * that must not allocate on the device. Output as lf_sample_challenges. Limits: 1 <= n <=
+ * LF_NOALLOC_MAX_CHALLENGES, larger n returns LF_E_LIMIT before any device work; device < 64.
+ * Scratch is one fixed device array per device (about 390 KB), shared by all calls: calls are
+ * serialised by a process-wide lock and return after `stream` (a cudaStream_t; NULL = the
+ * legacy default stream) has drained. The first call on a device locates that array and
+ * uploads the phase tables with synchronous copies; make it before any stream of the device
+ * begins a capture. The caller's current device is restored on return. */
+#define LF_NOALLOC_MAX_CHALLENGES 4096
+int lf_sample_challenges_noalloc(int device, const char* domain, const uint8_t* prefix, size_t prefix_len, uint32_t n,
+                                 uint8_t* out, void* stream);
 const char* lf_strerror(int code);
 const char* lf_last_error(lf_ctx* ctx);
 

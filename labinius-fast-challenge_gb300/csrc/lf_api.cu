@@ -587,6 +587,78 @@ __global__ void k_table_prg(bk::Pending root, uint64_t blocks, uint4* out) {
   out[4 * b + 3] = make_uint4(w[12], w[13], w[14], w[15]);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Challenge sampling that allocates no device memory.
+//
+// Some callers cannot let a library allocate device memory: a serving process that hands all of
+// its HBM to its own pool before the first request (an allocation would fail, or take memory the
+// pool has already promised), and a caller running next to latency-critical streams, where
+// cudaMalloc / cudaFree can stall the whole device. For them the sampler's scratch lives in one
+// file-scope device array of fixed size, located once per device with cudaGetSymbolAddress:
+// the transcript state the kernel starts from, the status word (zeroed by every call before the
+// launch) and the challenges until they are copied out, plus the phase tables, written once.
+// All calls on a device share the array, so a process-wide lock serialises the calls and each
+// returns only after its stream has drained; work on other streams never touches the array.
+// ---------------------------------------------------------------------------------------------
+constexpr uint32_t NOALLOC_MAX_CHALLENGES = 4096;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+struct NoAllocScratch {
+  bk::Hasher hasher;                      // Transcript::new(domain) after absorb_bytes(prefix)
+  int status[4];                          // status[0] != 0: a challenge failed its norm bound
+  Challenge chal[NOALLOC_MAX_CHALLENGES];
+  double phase[2 * 162 * 88];             // phase tables (re, im)
+};
+
+static __device__ __align__(256) uint8_t g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+struct NoAllocDevice {
+  bool ready = false;
+  NoAllocScratch* scratch = nullptr;
+  uint32_t sign_key[8];
+};
+std::mutex g_noalloc_mu;
+NoAllocDevice g_noalloc_dev[NOALLOC_MAX_DEVICES];
+
+// Once per device, with that device current: locate the array and upload the phase tables.
+int noalloc_setup(NoAllocDevice& d) {
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return LF_E_CUDA;
+  NoAllocScratch* sc = static_cast<NoAllocScratch*>(p);
+  std::vector<double> re, im;
+  phase_tables(re, im);
+  if (cudaMemcpy(sc->phase, re.data(), 162 * 88 * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(sc->phase + 162 * 88, im.data(), 162 * 88 * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+    return LF_E_CUDA;
+  bk::Hasher h;
+  const char* c = "labinius 2026 challenge signs v1";
+  h.init_derive(c, (uint32_t)strlen(c));
+  memcpy(d.sign_key, h.key, 32);
+  d.scratch = sc;
+  d.ready = true;
+  return LF_OK;
+}
+
+int noalloc_sample(NoAllocDevice& d, const char* domain, const uint8_t* prefix, size_t prefix_len, uint32_t n,
+                   uint8_t* out, cudaStream_t st) {
+  Transcript t;
+  t.init(domain);
+  t.absorb_bytes(prefix, prefix_len);
+  NoAllocScratch* sc = d.scratch;
+  int status[4] = {0, 0, 0, 0};
+  if (cudaMemcpyAsync(&sc->hasher, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemsetAsync(sc->status, 0, sizeof(sc->status), st) != cudaSuccess)
+    return LF_E_CUDA;
+  launch_challenges(&sc->hasher, t.counter, d.sign_key, sc->phase, sc->phase + 162 * 88, sc->chal, (int)n, sc->status,
+                    st);
+  if (cudaGetLastError() != cudaSuccess) return LF_E_CUDA;
+  if (cudaMemcpyAsync(out, sc->chal, (size_t)n * sizeof(Challenge), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(status, sc->status, sizeof(status), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return LF_E_CUDA;
+  return status[0] ? LF_E_INTERNAL : LF_OK;
+}
+
 }  // namespace
 
 // =============================================================================================
@@ -782,6 +854,22 @@ int lf_sample_challenges_traced(lf_ctx* ctx, const char* domain, const uint8_t* 
   return LF_OK;
 }
 
+int lf_sample_challenges_noalloc(int device, const char* domain, const uint8_t* prefix, size_t prefix_len, uint32_t n,
+                                 uint8_t* out, void* stream) {
+  if (!domain || (!prefix && prefix_len) || !out || n == 0 || device < 0 || device >= NOALLOC_MAX_DEVICES)
+    return LF_E_ARGS;
+  if (n > NOALLOC_MAX_CHALLENGES) return LF_E_LIMIT;
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(device) != cudaSuccess) return LF_E_CUDA;
+  NoAllocDevice& d = g_noalloc_dev[device];
+  int rc = d.ready ? LF_OK : noalloc_setup(d);
+  if (rc == LF_OK)
+    rc = noalloc_sample(d, domain, prefix, prefix_len, n, out, static_cast<cudaStream_t>(stream));
+  cudaSetDevice(prev);
+  return rc;
+}
+
 int lf_last_profile(lf_ctx* ctx, lf_profile* out) {
   if (!ctx || !out) return LF_E_ARGS;
   *out = ctx->prof;
@@ -800,6 +888,7 @@ const char* lf_strerror(int code) {
     case LF_E_CUDA: return "CUDA error";
     case LF_E_INTERNAL: return "internal check failed";
     case LF_E_ADMISSION: return "request exceeds the HBM budget";
+    case LF_E_LIMIT: return "request exceeds the fixed scratch of lf_sample_challenges_noalloc (4096 challenges)";
     default: return "unknown error";
   }
 }

@@ -16,13 +16,14 @@ BASELINE_Q = 3889 * 9721 * 17497
 LF_OK = 0
 ERRORS = {
     -1: "LF_E_ARGS", -2: "LF_E_SHAPE", -3: "LF_E_MODULUS", -4: "LF_E_TABLE_LEN", -5: "LF_E_CAP",
-    -6: "LF_E_OOM", -7: "LF_E_CUDA", -8: "LF_E_INTERNAL", -9: "LF_E_ADMISSION",
+    -6: "LF_E_OOM", -7: "LF_E_CUDA", -8: "LF_E_INTERNAL", -9: "LF_E_ADMISSION", -10: "LF_E_LIMIT",
 }
+NOALLOC_MAX_CHALLENGES = 4096
 EXPORTS = [
     "lf_ctx_create", "lf_ctx_destroy", "lf_proof_size", "lf_accept_modulus", "lf_key_prepare", "lf_prove",
     "lf_prove_device", "lf_write_table_device", "lf_device_alloc", "lf_device_free", "lf_memcpy_h2d",
     "lf_last_profile", "lf_strerror", "lf_last_error", "lf_last_challenges",
-    "lf_sample_challenges",
+    "lf_sample_challenges", "lf_sample_challenges_noalloc",
 ]
 
 
@@ -79,6 +80,8 @@ def load(path=LIB_PATH):
     lib.lf_last_error.restype = ctypes.c_char_p
     lib.lf_last_challenges.argtypes = [p, u8p, sz]
     lib.lf_sample_challenges.argtypes = [p, ctypes.c_char_p, ctypes.c_char_p, sz, ctypes.c_uint32, u8p]
+    lib.lf_sample_challenges_noalloc.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p, sz, ctypes.c_uint32,
+                                                 u8p, p]
     _lib = lib
     return lib
 
@@ -90,6 +93,16 @@ def _parse_challenges(raw, n):
         w = int.from_bytes(c[36:40], "little")
         out.append((list(c[:w]), int.from_bytes(c[32:36], "little"), w))
     return out
+
+
+def sample_challenges_noalloc(domain, prefix, n, device=0, stream=None):
+    """n challenges from lf_sample_challenges_noalloc: no context and no device allocation.
+    `stream` is a cudaStream_t handle as an int (None = the legacy default stream)."""
+    buf = (ctypes.c_uint8 * (40 * max(n, 1)))()
+    rc = load().lf_sample_challenges_noalloc(device, domain.encode(), bytes(prefix), len(prefix), n, buf, stream)
+    if rc != LF_OK:
+        raise LfError(rc, load().lf_strerror(rc).decode())
+    return _parse_challenges(bytes(buf), n)
 
 
 def q_bytes(q):

@@ -51,3 +51,18 @@ def test_no_device_fails_loudly(gpu_lib):
         pass
     with pytest.raises(gpu_lib.LfError):
         gpu_lib.Prover(0)
+
+
+def test_noalloc_sampler_limits_checked_on_the_host(gpu_lib):
+    """Argument and size checks return before any device work, so they hold without a GPU."""
+    lib = gpu_lib.load()
+    import ctypes
+
+    buf = (ctypes.c_uint8 * 40)()
+    n_max = gpu_lib.NOALLOC_MAX_CHALLENGES
+    assert lib.lf_sample_challenges_noalloc(0, b"d", b"", 0, n_max + 1, buf, None) == -10
+    assert lib.lf_sample_challenges_noalloc(0, b"d", b"", 0, 0, buf, None) == -1
+    assert lib.lf_sample_challenges_noalloc(-1, b"d", b"", 0, 1, buf, None) == -1
+    assert lib.lf_sample_challenges_noalloc(64, b"d", b"", 0, 1, buf, None) == -1
+    assert lib.lf_sample_challenges_noalloc(0, None, b"", 0, 1, buf, None) == -1
+    assert b"4096" in lib.lf_strerror(-10)
