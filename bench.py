@@ -7,14 +7,15 @@ modulus Q = 3889 * 9721 * 17497: commitment, transcript, partials, the 24-round 
 evaluation, folding challenges and fold, proof bytes back in host memory.
 
 * value: milliseconds per proof with the table already resident in HBM (lf_prove_device), over
-  K timed steps; the tables (5 seeds, generated on the device by the table PRG outside the timed
-  region) are larger than L2, so no flush is needed.
+  K timed steps (CUDA events on the prover's stream); the tables (5 seeds, generated on the device
+  by the library's table PRG outside the timed region) are larger than L2, so no flush is needed.
 * e2e: the same metric through the public C ABI (lf_prove) from pinned host tables, with the
   256 MiB host->device copy and the proof's device->host copy inside the timed region.
 * process_e2e: the reference's own window (process start, table file load, proof written) for the
   labinius-fast command, median of 5 seeds.
 * cpu_baseline / --impl reference: the oracle's restatement of the reference prover
-  (oracle/liboracle.so, all host threads) on the same shape.
+  (oracle/liboracle.so, all host threads) on the same shape; the baseline leg also runs the
+  oracle's checker on the benchmarked GPU proof. Nothing else in this file touches the oracle.
 
 For N > 1 (torchrun) every rank proves its own seeds on its own GPU (replicas); the time is the
 maximum over ranks and value is milliseconds per proof of the whole job.
@@ -133,61 +134,78 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(log_vars, steps=1):
-    """The oracle's restatement of the reference prover on all host threads: one proof per step."""
+def cpu_baseline(log_vars, table, seed, proof):
+    """The CPU baseline leg: the oracle's restatement of the reference prover on all host threads,
+    one full proof timed, and the oracle's checker run on the GPU proof of the same table."""
     import pyoracle
 
     pyoracle.build()
-    seed = seeds(1)[0]
-    table = pyoracle.write_table(seed, log_vars)
-    times = []
-    for _ in range(steps):
-        t0 = time.perf_counter()
-        pyoracle.prove(seed, table, log_vars)
-        times.append((time.perf_counter() - t0) * 1e3)
-    return statistics.median(times), os.cpu_count()
+    t0 = time.perf_counter()
+    cpu_proof = pyoracle.prove(seed, table, log_vars)
+    ms = (time.perf_counter() - t0) * 1e3
+    ok, msg = pyoracle.verify(seed, proof, log_vars, table)
+    if not ok:
+        raise RuntimeError("the checker rejected the benchmarked proof: " + msg)
+    if cpu_proof != proof:
+        raise RuntimeError("GPU and CPU proofs of the same table differ")
+    return ms, os.cpu_count()
 
 
 def reference_arm(args, rank, world):
+    """The reference's algorithm on the host cores (the oracle port: the reference itself is Rust and
+    does not build here). A step is one full proof; the run is capped at 4 timed proofs (~25 s each
+    at 2^31 on 16 cores) so that it ends within a few minutes."""
     if rank != 0:
         return
-    for _ in range(args.warmup):
-        pass  # the oracle has no warm state worth priming beyond its first call below
     import pyoracle
 
     pyoracle.build()
     seed = seeds(1)[0]
     table = pyoracle.write_table(seed, args.log_vars)
-    pyoracle.prove(seed, table, args.log_vars)  # warm-up: page in, tables
+    warm = min(args.warmup, 1)
+    steps = max(1, min(args.steps, 4))
+    for _ in range(warm):
+        pyoracle.prove(seed, table, args.log_vars)
     times = []
-    for _ in range(args.steps):
+    for _ in range(steps):
         t0 = time.perf_counter()
         pyoracle.prove(seed, table, args.log_vars)
         times.append((time.perf_counter() - t0) * 1e3)
-    ms = sum(times) / len(times)
+    ms = statistics.median(times)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms/proof", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u32/GF(2^k)", "data": "synthetic (table PRG of seeded tables)",
-        "config": {"workload": f"plain opening, 2^{args.log_vars}-bit table, Q=661473542593", "log_vars": args.log_vars},
+        "steps": steps, "warmup": warm, "ms_per_step": round(ms, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32 mod p / GF(2^128), GF(2^162)",
+        "data": "synthetic: a table from the reference's table PRG of one seeded seed",
+        "config": {"workload": f"plain opening, 2^{args.log_vars}-bit table (2^{args.log_vars - 7} GHASH words), "
+                               "Q=661473542593, 1024 columns", "log_vars": args.log_vars,
+                   "requested_steps": args.steps, "requested_warmup": args.warmup},
         "cpu_baseline": {"value": round(ms, 3), "unit": "ms/proof", "cores": os.cpu_count(), "kind": "port",
                          "sample": f"one full proof per step at 2^{args.log_vars} bits (oracle restatement of "
-                                   "verifier/proof_verify/src/reference.rs with the 3-prime transform commit)"},
+                                   "verifier/proof_verify/src/reference.rs with the 3-prime transform commit), "
+                                   f"all {os.cpu_count()} host threads"},
         "e2e": {"value": round(ms, 3), "unit": "ms/proof", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def process_e2e(lfgpu, log_vars, n=5):
-    """labinius-fast as the harness runs it: process start -> proof file written (wall clock)."""
-    import pyoracle
+def device_table(prover, seed, log_vars):
+    """A table written on the device by the library's table PRG, in a torch-owned buffer."""
+    import torch
 
+    t = torch.empty((1 << log_vars) // 8, dtype=torch.uint8, device="cuda")
+    prover.write_table_device(seed, log_vars, t.data_ptr())
+    return t
+
+
+def process_e2e(lfgpu, prover, log_vars, n=5):
+    """labinius-fast as the harness runs it: process start -> proof file written (wall clock)."""
     times = []
     with tempfile.TemporaryDirectory() as d:
         for i, seed in enumerate(seeds(n, 99)):
             tpath = os.path.join(d, f"t{i}.bin")
             with open(tpath, "wb") as f:
-                f.write(pyoracle.write_table(seed, log_vars))
+                f.write(device_table(prover, seed, log_vars).cpu().numpy().tobytes())
             env = dict(os.environ, LABINIUS_SEED=seed.hex())
             t0 = time.perf_counter()
             p = subprocess.run([lfgpu.CLI_PATH, "--prove", os.path.join(d, f"p{i}.bin"), "--table", tpath,
@@ -197,6 +215,42 @@ def process_e2e(lfgpu, log_vars, n=5):
                 raise RuntimeError(p.stderr)
             os.unlink(tpath)
     return statistics.median(times), times
+
+
+def timed(stream, fn, steps):
+    """Device time of `steps` calls of fn on `stream` (CUDA events on the prover's own stream)."""
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(steps):
+        fn(i)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def commit_roofline(log_vars, commit_ms):
+    """Dominant kernel, the commitment (k_commit_tc). Its transform of the table words is a bf16
+    tensor-core product with the per-leaf Vandermonde limbs: per launch 2 x 972 x 128 x 2^(L-7)
+    FLOP (972 = 3 primes x 162 leaves x 2 limbs, K = 128 bits per word, one row per table word
+    and column). Peak: the sustained cuBLAS bf16 figure (the kernel runs inside back-to-back proofs)."""
+    words = 1 << (log_vars - 7)
+    flops = 2 * 972 * 128 * words
+    achieved = flops / (commit_ms * 1e-3) / 1e12
+    peak, kind = None, "fallback"
+    try:
+        with open(PEAKS) as f:
+            peak, kind = float(json.load(f)["bf16_tflops_sustained"]), "measured (sustained)"
+    except (OSError, KeyError, ValueError):
+        peak = 1700.0
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "k_commit_tc_traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get("bytes_per_launch")
+    return {"kernel": "k_commit_tc", "bound": "tensor", "achieved": round(achieved, 1), "peak": peak,
+            "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": kind,
+            "flops_per_launch": flops}
 
 
 def main():
@@ -224,104 +278,85 @@ def main():
     log_vars = args.log_vars
     tbytes = (1 << log_vars) // 8
     prover = lfgpu.Prover(local)
+    stream = torch.cuda.ExternalStream(prover.stream())
     ss = seeds(args.tables, rank)
-    tables = [prover.alloc(tbytes) for _ in ss]
-    for s, t in zip(ss, tables):
-        prover.write_table_device(s, log_vars, t)
+    tables = [device_table(prover, s, log_vars) for s in ss]
+    torch.cuda.synchronize()
     cap = lfgpu.proof_size(Q, log_vars)
     out = (ctypes.c_uint8 * cap)()
     prover.key_prepare(log_vars)
     nt = len(ss)
-    for i in range(max(3, args.warmup)):
-        prover.prove_device(ss[i % nt], tables[i % nt], log_vars, out=out)
+    warm = max(3, args.warmup)
+    for i in range(warm):
+        prover.prove_device(ss[i % nt], tables[i % nt].data_ptr(), log_vars, out=out)
 
-    # ---- value: device-resident tables ----
+    # ---- value: device-resident tables (one proof per step, 5 tables > L2 cycled) ----
     profs = []
+
+    def step_device(i):
+        prover.prove_device(ss[i % nt], tables[i % nt].data_ptr(), log_vars, out=out)
+        profs.append(prover.profile())
+
     barrier(world)
     torch.cuda.synchronize()
     with Clocks(local) as clk:
-        t0 = time.perf_counter()
-        for i in range(args.steps):
-            prover.prove_device(ss[i % nt], tables[i % nt], log_vars, out=out)
-            profs.append(prover.profile())
-        torch.cuda.synchronize()
-        elapsed = time.perf_counter() - t0
+        dev_ms = timed(stream, step_device, args.steps)
     barrier(world)
-    elapsed = max_over_ranks(elapsed, world)
-    ms_per_step = elapsed * 1e3 / args.steps
+    dev_ms = max_over_ranks(dev_ms, world)
+    ms_per_step = dev_ms / args.steps
     value = ms_per_step / world
-
-    # ---- e2e: pinned host tables through lf_prove ----
-    import pyoracle
-
+    med = {k: statistics.median(p[k] for p in profs) for k in profs[0]}
+    phases = {k: round(v, 4) for k, v in med.items() if k.endswith("_ms")}
     if args.no_e2e:
         if rank == 0:
-            print(json.dumps({"metric": METRIC, "value": round(value, 3), "unit": "ms/proof",
-                              "phases_ms": {k: round(statistics.median(p[k] for p in profs), 4) for k in profs[0]}}))
+            print(json.dumps({"metric": METRIC, "value": round(value, 3), "unit": "ms/proof", "phases_ms": phases,
+                              "gpu_launches": int(med["launches"]) * args.steps, "clocks": clk.summary()}))
         return
+
+    # ---- e2e: pinned host table through lf_prove (H2D of the table and D2H of the proof timed) ----
     host = torch.empty(tbytes, dtype=torch.uint8, pin_memory=True)
-    hp = host.data_ptr()
     e2e_seed = ss[0]
-    host.copy_(torch.frombuffer(bytearray(pyoracle.write_table(e2e_seed, log_vars)), dtype=torch.uint8))
-    tab = (ctypes.c_uint8 * tbytes).from_address(hp)
+    host.copy_(tables[0])
+    torch.cuda.synchronize()
+    tab = (ctypes.c_uint8 * tbytes).from_address(host.data_ptr())
+    proofs = []
     for _ in range(2):
         prover.prove(e2e_seed, tab, log_vars)
     barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        proof = prover.prove(e2e_seed, tab, log_vars)
-    e2e_elapsed = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_total = timed(stream, lambda i: proofs.append(prover.prove(e2e_seed, tab, log_vars)), args.steps)
+    e2e_total = max_over_ranks(e2e_total, world)
     barrier(world)
-    e2e_ms = e2e_elapsed * 1e3 / args.steps / world
-
+    e2e_ms = e2e_total / args.steps / world
     if rank != 0:
         return
-    # correctness of the last e2e proof against the oracle's checker
-    ok, msg = pyoracle.verify(e2e_seed, proof, log_vars, bytes(host.numpy()))
-    if not ok:
-        raise RuntimeError("the checker rejected the benchmarked proof: " + msg)
-
-    med = {k: statistics.median(p[k] for p in profs) for k in profs[0]}
-    hbm, peak_kind = peaks()
-    words = 1 << (log_vars - 7)
-    # Dominant kernel: the commitment (K1). Algorithmic bytes per launch: the table once (2^LP x 16 B)
-    # plus the transform-domain partial sums it writes (splits x 3 primes x 1024 x 648 x 4 B).
-    splits = 16
-    k1_bytes = words * 16 + splits * 3 * 1024 * 648 * 4
-    k1_ms = med["commit_ms"]
-    achieved = k1_bytes / (k1_ms * 1e-3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "k_commit_ntt_traffic.json")
-    if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get("bytes_per_launch")
+    proof = proofs[-1]
     proc_ms = None
     if not args.no_process:
         try:
-            proc_ms, _ = process_e2e(lfgpu, log_vars)
+            proc_ms, _ = process_e2e(lfgpu, prover, log_vars)
         except Exception as e:  # reported, not fatal
             proc_ms = f"failed: {e}"
     cpu = None
     if not args.no_cpu:
-        cms, cores = cpu_baseline(log_vars)
+        cms, cores = cpu_baseline(log_vars, bytes(host.numpy()), e2e_seed, proof)
         cpu = {"value": round(cms, 1), "unit": "ms/proof", "cores": cores, "kind": "port",
-               "sample": f"one full 2^{log_vars}-bit proof (oracle restatement of the reference prover, "
-                         "3-prime transform commit), all host threads"}
+               "sample": f"one full 2^{log_vars}-bit proof of the e2e table (oracle restatement of the reference "
+                         "prover, 3-prime transform commit), all host threads; its proof equals the GPU proof"}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "ms/proof", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32 mod p / GF(2^128), GF(2^162)",
-        "data": "synthetic: tables from the reference's table PRG (keyed BLAKE3 XOF) of 5 seeded seeds",
+        "data": f"synthetic: tables from the reference's table PRG (keyed BLAKE3 XOF) of {nt} seeded seeds",
         "config": {"workload": f"plain opening, 2^{log_vars}-bit table (2^{log_vars - 7} GHASH words), "
-                               "Q=661473542593, 1024 columns", "log_vars": log_vars, "seeds": 5,
-                   "l2": "inputs larger than L2 (256 MiB tables), no flush", "parallelism": f"replicas x{world}"},
+                               "Q=661473542593, 1024 columns", "log_vars": log_vars, "seeds": nt,
+                   "l2": f"inputs larger than L2 ({nt} tables of {tbytes >> 20} MiB cycled), no flush",
+                   "parallelism": f"replicas x{world}",
+                   "timing": "CUDA events on the prover's stream around the timed steps"},
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms/proof", "h2d_bytes_per_step": tbytes,
                 "d2h_bytes_per_step": cap},
         "process_e2e_ms": proc_ms,
-        "phases_ms": {k: round(v, 4) for k, v in med.items() if k.endswith("_ms")},
-        "roofline": {"kernel": "k_commit_ntt", "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
-                     "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": traffic,
-                     "peak_kind": peak_kind,
-                     "note": "integer-ALU bound transform; HBM fraction reported against the measured copy peak"},
+        "phases_ms": phases,
+        "roofline": commit_roofline(log_vars, med["commit_ms"]),
         "cpu_baseline": cpu,
         "gpu_launches": int(med["launches"]) * args.steps,
         "clocks": clk.summary(),

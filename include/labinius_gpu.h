@@ -49,6 +49,10 @@ typedef struct lf_profile {
  * (solution/labinius/crates/pcs/src/par.rs, solution/proof_generate/src/main.rs:1427-1569). */
 int lf_ctx_create(const lf_config* cfg, lf_ctx** out);
 void lf_ctx_destroy(lf_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), on which every kernel and copy of its calls runs, so
+ * that a caller can order its own work or timing events with them. No counterpart in the
+ * reference (its prover has no device). */
+void* lf_ctx_stream(lf_ctx* ctx);
 
 /* Size of the proof for modulus q (16 bytes little-endian) at 2^log_vars table bits; 0 if the
  * shape is unsupported. Replaces ProofLayout::instance (solution/proof_generate/src/main.rs:1252-1310). */

@@ -177,7 +177,7 @@ struct KeyCache {
   uint64_t elements = 0;
   ModulusPlan mp;
   DevBuf key;  // u32 [prime][element][leaf][k][l]: the 4x4 base-multiplication matrix per leaf
-  DevBuf t2;   // u32 [prime][T2_WORDS]: the fused lookup tables of the commitment kernel
+  DevBuf btiles;  // bf16 [prime][third][112 x 128]: Vandermonde limbs of the commitment kernel
 };
 
 }  // namespace
@@ -256,8 +256,9 @@ int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh) {
   CK(ared.ensure((size_t)mp.nprimes * E * RING_N * 4));
   CK(leaf.ensure((size_t)mp.nprimes * E * 4 * LEAVES * 4));
   CK(ctx->key.key.ensure((size_t)mp.nprimes * E * LEAVES * 16 * 4));
-  CK(ctx->key.t2.ensure(mp.t2.size() * 4));
-  CK(cudaMemcpyAsync(ctx->key.t2.p, mp.t2.data(), mp.t2.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx->key.btiles.ensure(mp.btiles.size() * 2));
+  CK(cudaMemcpyAsync(ctx->key.btiles.p, mp.btiles.data(), mp.btiles.size() * 2, cudaMemcpyHostToDevice,
+                     ctx->stream));
   upload_prime_consts(mp, ctx->stream);
   launch_matrix_expand(mp, E, ared.as<uint32_t>(), ctx->stream);
   launch_key_transform(mp, E, ared.as<uint32_t>(), leaf.as<uint32_t>(), ctx->key.key.as<uint32_t>(), ctx->stream);
@@ -308,8 +309,10 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   const ModulusPlan& mp = ctx->key.mp;
   CK(ctx->partial.ensure((size_t)splits * mp.nprimes * COLUMNS * LEAVES * 4 * 4));
   CK(ctx->stream_buf.ensure(STREAM_PREFIX + commit_bytes + 1024));
-  launch_commit(mp, sh, table, ctx->key.key.as<uint32_t>(), ctx->key.t2.as<uint32_t>(), ctx->partial.as<uint32_t>(),
-                splits, st);
+  CK(ctx->status.ensure(16));
+  CK(cudaMemsetAsync(ctx->status.p, 0, 16, st));
+  launch_commit(mp, sh, table, ctx->key.key.as<uint32_t>(), ctx->key.btiles.as<uint16_t>(),
+                ctx->partial.as<uint32_t>(), splits, ctx->status.as<int>(), st);
   cudaEventRecord(ctx->ev[11], st);
   launch_commit_finish(mp, sh, ctx->partial.as<uint32_t>(), splits, ctx->stream_buf.as<uint8_t>() + STREAM_PREFIX, st);
   CKL("commitment");
@@ -512,7 +515,8 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   CK(ctx->chal.ensure(COLUMNS * sizeof(Challenge)));
   CK(ctx->status.ensure(16));
   CK(cudaMemcpyAsync(ctx->hasher.p, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, st));
-  CK(cudaMemsetAsync(ctx->status.p, 0, 16, st));
+  // status[0] was zeroed before the commitment: 3 = commitment pipeline timeout, 1 = sampling
+  // bound, 2 = fold range.
   launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.as<double>(), ctx->phase.as<double>() + 162 * 88,
                     ctx->chal.as<Challenge>(), COLUMNS, ctx->status.as<int>(), st);
   t.counter += COLUMNS;
@@ -532,6 +536,8 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   CK(cudaStreamSynchronize(st));
   if (status[0] == 1) return fail(ctx, LF_E_INTERNAL, "challenge sampling exceeded its attempt bound");
   if (status[0] == 2) return fail(ctx, LF_E_INTERNAL, "a fold coefficient does not fit the wire codec");
+  if (status[0] == 3) return fail(ctx, LF_E_INTERNAL, "the commitment kernel's pipeline timed out");
+  if (status[0] != 0) return fail(ctx, LF_E_INTERNAL, "a device-side check failed");
 
   // ---- encode (main.rs:98-124) ----
   uint8_t* o = proof;
@@ -701,6 +707,8 @@ int lf_ctx_create(const lf_config* cfg, lf_ctx** out) {
   return LF_OK;
 }
 
+void* lf_ctx_stream(lf_ctx* ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
+
 void lf_ctx_destroy(lf_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
@@ -708,7 +716,7 @@ void lf_ctx_destroy(lf_ctx* ctx) {
   DevBuf* bufs[] = {&ctx->table, &ctx->stream_buf, &ctx->partial, &ctx->sblk, &ctx->ehi, &ctx->elo, &ctx->lo_planes,
                     &ctx->rhi, &ctx->vparts, &ctx->psi, &ctx->batch, &ctx->soa, &ctx->msg, &ctx->p0, &ctx->eqt,
                     &ctx->row, &ctx->hasher, &ctx->chal, &ctx->fold, &ctx->cvs, &ctx->cvs_scratch, &ctx->subtrees,
-                    &ctx->status, &ctx->phase, &ctx->scratch_small, &ctx->wbuf, &ctx->rbuf, &ctx->key.key, &ctx->key.t2};
+                    &ctx->status, &ctx->phase, &ctx->scratch_small, &ctx->wbuf, &ctx->rbuf, &ctx->key.key, &ctx->key.btiles};
   for (DevBuf* b : bufs) b->release();
   for (auto& ev : ctx->ev) cudaEventDestroy(ev);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -18,10 +18,27 @@
 
 #include "lf_blake3.cuh"
 #include "lf_internal.h"
+#include "lf_tc.cuh"
 
 namespace lf {
 
 __constant__ PrimeConst c_prime[MAX_PRIMES];
+
+// Shape of K1 on the tensor cores (the kernel is described where it is defined).
+constexpr int TC_COLS = 128;                         // table columns per block (MMA M)
+constexpr int TC_LEAVES = 54;                        // leaves per block (a third of a prime)
+constexpr int TC_N = 112;                            // MMA N: 54 leaves x 2 limbs, padded to 16
+constexpr int TC_EPI_WARPS = 24;
+constexpr int TC_THREADS = 32 * (TC_EPI_WARPS + 3);  // + 2 producer warps + 1 MMA warp
+constexpr int TC_A_BYTES = TC_COLS * 128 * 2;        // 32 KB per A slot
+constexpr int TC_B_BYTES = TC_N * 128 * 2;           // 28 KB
+constexpr int TC_KEY_INTS = TC_LEAVES * 16;          // one element's key rows for the block's leaves
+constexpr int TC_SMEM = 4 * TC_A_BYTES + TC_B_BYTES + 4 * TC_KEY_INTS * 4 + 24 * 8 + 16;
+constexpr int TC_REDUCE_EVERY = 6;                   // elements between accumulator reductions
+constexpr long long TC_WAIT_CYCLES = 2000000000LL;   // ~1 s at 2 GHz
+
+
+static void fill_btiles(const PrimePlan& pl, const PrimeConst& c, uint16_t* out);
 
 // ------------------------------------------------------------------------------------------------
 // Host: plans
@@ -74,38 +91,9 @@ static void fill_consts(const PrimePlan& pl, PrimeConst& c) {
   memset(&c, 0, sizeof c);
   const uint64_t p = pl.p;
   auto pw = [&](int64_t e) { return (uint64_t)pl.pw[((e % 486) + 486) % 486]; };
-  auto shoup = [&](uint64_t w) { return (uint32_t)((w << 32) / p); };
   c.p = pl.p;
   c.bar = (uint32_t)((1ull << 32) / p);
   c.om = (uint32_t)pw(162);
-  c.om_s = shoup(c.om);
-  for (int sb = 0; sb < 6; ++sb) {
-    auto put = [&](int slot, uint32_t e) {
-      uint64_t t1 = pw(e / 3), t2 = pw(2 * (e / 3));
-      c.tw[sb][slot][0] = (uint32_t)t1, c.tw[sb][slot][1] = (uint32_t)t2;
-      c.tws[sb][slot][0] = shoup(t1), c.tws[sb][slot][1] = shoup(t2);
-    };
-    put(0, pl.node_e[2][sb]);
-    for (int a = 0; a < 3; ++a) put(1 + a, pl.node_e[3][3 * sb + a]);
-    for (int a = 0; a < 3; ++a)
-      for (int b = 0; b < 3; ++b) put(4 + 3 * a + b, pl.node_e[4][9 * sb + 3 * a + b]);
-    // Fused trinomial split + level-1 split for sub-block sb = (node n, child i).
-    int n = sb / 3, i = sb % 3;
-    uint64_t e = pl.node_e[1][n];
-    uint64_t tau = pw(e / 3), om_i = pw(162 * i), c_n = pw(e);
-    uint64_t coef[5];
-    coef[0] = 1;
-    coef[1] = tau * om_i % p;
-    coef[2] = tau * tau % p * om_i % p * om_i % p;
-    coef[3] = c_n;
-    coef[4] = coef[1] * c_n % p;
-    for (int idx = 0; idx < 32; ++idx) {
-      uint64_t v = 0;
-      for (int t = 0; t < 5; ++t)
-        if ((idx >> t) & 1) v += coef[t];
-      c.T[sb][idx] = (uint32_t)(v % p);
-    }
-  }
   for (int l = 1; l <= 4; ++l)
     for (size_t n = 0; n < pl.node_e[l].size(); ++n) {
       uint32_t e = pl.node_e[l][n];
@@ -122,23 +110,6 @@ static void fill_consts(const PrimePlan& pl, PrimeConst& c) {
   c.w5 = (uint32_t)pw(405);
   c.inv_split = inv_mod((c.w + p - c.w5) % p, p);
   for (int s = 0; s < LEAVES; ++s) c.leaf_root[s] = (uint32_t)pw(pl.leaf_e[s]);
-}
-
-// The level-2 split fused into the lookups: output (child a, position q < 9) of level-2 node sb
-// is sum_t omega^(a t) tau^t T[sb][idx(q + 9 t)], tau = eta^(e/3) of node sb; entry
-// [sb][a][t][idx] holds omega^(a t) tau^t T[sb][idx].
-static void fill_t2(const PrimePlan& pl, const PrimeConst& c, uint32_t* t2) {
-  const uint64_t p = pl.p;
-  auto pw = [&](int64_t e) { return (uint64_t)pl.pw[((e % 486) + 486) % 486]; };
-  for (int sb = 0; sb < 6; ++sb) {
-    const uint64_t tau = pw(pl.node_e[2][sb] / 3);
-    for (int a = 0; a < 3; ++a)
-      for (int t = 0; t < 3; ++t) {
-        uint64_t f = pw(162 * ((a * t) % 3));
-        for (int i = 0; i < t; ++i) f = f * tau % p;
-        for (int idx = 0; idx < 32; ++idx) t2[((sb * 3 + a) * 3 + t) * 32 + idx] = (uint32_t)(f * c.T[sb][idx] % p);
-      }
-  }
 }
 
 static uint32_t bits_of(u128 x) {
@@ -162,7 +133,7 @@ bool make_modulus_plan(u128 q, ModulusPlan& mp, std::string& err) {
     return false;
   }
   mp.consts.resize(mp.nprimes);
-  mp.t2.assign((size_t)mp.nprimes * T2_WORDS, 0);
+  mp.btiles.assign((size_t)mp.nprimes * 3 * (TC_B_BYTES / 2), 0);
   for (int i = 0; i < mp.nprimes; ++i) {
     PrimePlan pl;
     if (!make_plan(mp.primes[i], pl)) {
@@ -170,7 +141,7 @@ bool make_modulus_plan(u128 q, ModulusPlan& mp, std::string& err) {
       return false;
     }
     fill_consts(pl, mp.consts[i]);
-    fill_t2(pl, mp.consts[i], mp.t2.data() + (size_t)i * T2_WORDS);
+    fill_btiles(pl, mp.consts[i], mp.btiles.data() + (size_t)i * 3 * (TC_B_BYTES / 2));
     for (int j = 0; j < i; ++j) mp.garner_inv[i][j] = inv_mod(mp.primes[j], mp.primes[i]);
   }
   return true;
@@ -337,184 +308,340 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
 }
 
 // ------------------------------------------------------------------------------------------------
-// K1: the commitment in the transform domain.
-//   grid  (COLUMNS / 32 column tiles, primes, element splits); block 576 = 18 warps.
-//   warp w = (level-2 node sb = w / 3, level-3 node a = w % 3) of every word; lane = column.
-// A thread produces, per table word, the 9 leaves of its level-3 node: the first three levels
-// (trinomial split, level-1 split, the level-2 split into node a) are three lookups in
-// twiddled 32-entry tables, then two radix-3 levels; at each leaf it multiplies with the key's
-// 4x4 base-multiplication matrix and accumulates 9 x 4 u32 over its split of the elements.
+// K1 on the tensor cores.
+//
+// The transform of a table word (128 bits = the Y-coefficients 0..127 of one residue class of X
+// mod 4) at leaf s is the evaluation sum_j bit_j zeta_s^j (mod p), zeta_s the leaf's root: a
+// product with the Vandermonde matrix V[s][j] = zeta_s^j. On the tensor core it is exact:
+//   A (M = 128 table columns x K = 128 bits) holds each bit as bf16 2.0 or 0,
+//   B (N = 112 x K) holds, per leaf, the two limbs (V mod 256) / 2 and (V >> 8) * 128 (both exact
+//   in bf16), and the f32 accumulators give D_lo + D_hi = sum_j bit_j V[s][j] < 2^22 exactly.
+// The epilogue reduces that sum mod p in f32 (exact: every intermediate is an integer below
+// 2^24), then does the 4x4 base multiplication with the key on the integer pipe.
+//
+// Block = one prime x one third of its 162 leaves (54) x 128 table columns x an element range.
+//   warps 0-23  epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (= its 32 columns) and owns
+//               leaves 9 (w / 4) .. +8 of the third, 9 x 4 accumulators per thread;
+//   warps 24-25 producers: table words -> bf16 A tiles (4 slots, one per word k of an element)
+//               and the element's key rows -> shared memory (4-element ring);
+//   warp 26     lane 0 issues the MMAs: word k of an element into TMEM columns 112 k .. +111.
+// Every wait is bounded (about a second); a timeout sets *status = 3 and the block drains.
 // ------------------------------------------------------------------------------------------------
-constexpr int CT = 32;
-constexpr int MB = 8;
-constexpr int KWARPS = 18;
-constexpr int KTHREADS = 32 * KWARPS;
-
-// One radix-3 split of a node: inputs a (untwiddled), b, c; outputs in place.
-__device__ __forceinline__ void split3(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t t1, uint32_t t1s, uint32_t t2,
-                                       uint32_t t2s, uint32_t om, uint32_t oms, uint32_t p) {
-  uint32_t b1 = shoup(b, t1, t1s, p);
-  uint32_t c1 = shoup(c, t2, t2s, p);
-  uint32_t m = shoup(b1 + 2 * p - c1, om, oms, p);
-  uint32_t y0 = a + b1 + c1;
-  uint32_t y1 = a + m + 2 * p - c1;
-  uint32_t y2 = a + 4 * p - b1 - m;
-  a = y0, b = y1, c = y2;
+// Word -> one row of an A slot. u32 o = 16 w + t of the row holds bits 32 w + t (low bf16) and
+// 32 w + t + 16 (high bf16) of the word as 2.0 (0x4000) or 0; the B tiles use the same K order.
+__device__ __forceinline__ void tc_write_row(uint8_t* slot, int c, uint4 v) {
+  const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const uint32_t x = xs[q >> 2];
+    uint32_t u[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int t = (q & 3) * 4 + i;
+      u[i] = t < 15 ? (x << (14 - t)) & 0x40004000u : (x >> 1) & 0x40004000u;
+    }
+    *reinterpret_cast<uint4*>(slot + (c >> 3) * 2048 + q * 128 + (c & 7) * 16) = make_uint4(u[0], u[1], u[2], u[3]);
+  }
 }
 
-__device__ __forceinline__ uint32_t word_index_byte(uint32_t r0, uint32_t r1, uint32_t r2, uint32_t r3, uint32_t r4,
-                                                    int q) {
-  return ((r0 >> q) & 1) | (((r1 >> q) & 1) << 1) | (((r2 >> q) & 1) << 2) | (((r3 >> q) & 1) << 3) |
-         (((r4 >> q) & 1) << 4);
-}
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_commit_tc(const uint4* __restrict__ table, const uint32_t* __restrict__ key, const uint4* __restrict__ btiles,
+                uint32_t* __restrict__ partial, int rl, int elements, int per_split, int nprimes, int* status) {
+  extern __shared__ __align__(1024) uint8_t tsm[];
+  uint8_t* sA = tsm;
+  uint8_t* sB = tsm + 4 * TC_A_BYTES;
+  int* sKey = reinterpret_cast<int*>(sB + TC_B_BYTES);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sKey + 4 * TC_KEY_INTS);
+  uint64_t* a_full = bars;
+  uint64_t* a_empty = bars + 4;
+  uint64_t* t_full = bars + 8;
+  uint64_t* t_empty = bars + 12;
+  uint64_t* k_full = bars + 16;
+  uint64_t* k_empty = bars + 20;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 24);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
 
-size_t commit_smem_bytes() { return (size_t)(T2_WORDS + MB * LEAVES * 16) * 4 + (size_t)MB * CT * 27 * 4; }
-
-__global__ void __launch_bounds__(KTHREADS, 1)
-    k_commit_ntt(const uint4* __restrict__ table, const uint32_t* __restrict__ key, const uint32_t* __restrict__ t2g,
-                 uint32_t* __restrict__ partial, int rl, int elements, int per_split, int nprimes, int reduce_every) {
-  extern __shared__ __align__(16) uint32_t csm[];
-  uint32_t* sT2 = csm;                                  // [sb][a][t][32]
-  uint32_t* sKey = csm + T2_WORDS;                      // [MB][162][k][l]
-  uint8_t* sIdx = reinterpret_cast<uint8_t*>(sKey + MB * LEAVES * 16);  // [MB][CT][27][k]
-  const int pi = blockIdx.y;
-  const int col0 = blockIdx.x * CT;
+  const int pi = blockIdx.x / 3, third = blockIdx.x % 3;
+  const int col0 = blockIdx.y * TC_COLS;
   const int split = blockIdx.z;
   const int m_begin = split * per_split;
-  const int m_end = min(elements, m_begin + per_split);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int sb = warp / 3, na = warp % 3;
+  const int nelem = max(0, min(elements, m_begin + per_split) - m_begin);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const PrimeConst& P = c_prime[pi];
   const uint32_t p = P.p;
-  for (int i = tid; i < T2_WORDS; i += KTHREADS) sT2[i] = t2g[pi * T2_WORDS + i];
-  const uint32_t* t20 = sT2 + ((sb * 3 + na) * 3 + 0) * 32;
-  const uint32_t* t21 = t20 + 32;
-  const uint32_t* t22 = t20 + 64;
-  // warp-uniform twiddles of the level-3 node (3 sb + na) and its three level-4 children
-  const uint32_t w3a = P.tw[sb][1 + na][0], w3as = P.tws[sb][1 + na][0];
-  const uint32_t w3b = P.tw[sb][1 + na][1], w3bs = P.tws[sb][1 + na][1];
 
-  uint32_t acc[9][4];
-#pragma unroll
-  for (int q = 0; q < 9; ++q)
-#pragma unroll
-    for (int l = 0; l < 4; ++l) acc[q][l] = 0;
-
-  int since = 0;
-  for (int mc = m_begin; mc < m_end; mc += MB) {
-    const int nm = min(MB, m_end - mc);
-    __syncthreads();
-    {
-      const uint4* src = reinterpret_cast<const uint4*>(key + ((size_t)pi * elements + mc) * LEAVES * 16);
-      uint4* dst = reinterpret_cast<uint4*>(sKey);
-      for (int i = tid; i < nm * LEAVES * 4; i += KTHREADS) dst[i] = src[i];
+  if (tid == 0) {
+    *abort_flag = 0;
+    for (int i = 0; i < 4; ++i) {
+      tc::mbar_init(&a_full[i], 2);
+      tc::mbar_init(&a_empty[i], 1);
+      tc::mbar_init(&t_full[i], 1);
+      tc::mbar_init(&t_empty[i], TC_EPI_WARPS);
+      tc::mbar_init(&k_full[i], 2);
+      tc::mbar_init(&k_empty[i], TC_EPI_WARPS);
     }
-    // 27 five-bit indices per table word, one word per task: bits q, q+27, q+54, q+81, q+108.
-    for (int task = tid; task < nm * CT * 4; task += KTHREADS) {
-      const int k = task & 3, c = (task >> 2) % CT, ml = (task >> 2) / CT;
-      const uint4 v = table[((size_t)(col0 + c) << rl) + 4 * (size_t)(mc + ml) + k];
-      const uint32_t M27 = (1u << 27) - 1;
-      const uint32_t r0 = v.x & M27;
-      const uint32_t r1 = ((v.x >> 27) | (v.y << 5)) & M27;
-      const uint32_t r2 = ((v.y >> 22) | (v.z << 10)) & M27;
-      const uint32_t r3 = ((v.z >> 17) | (v.w << 15)) & M27;
-      const uint32_t r4 = (v.w >> 12) & M27;
-      uint8_t* dst = sIdx + ((size_t)(ml * CT + c) * 27) * 4 + k;
-#pragma unroll
-      for (int q = 0; q < 27; ++q) dst[4 * q] = (uint8_t)word_index_byte(r0, r1, r2, r3, r4, q);
-    }
-    __syncthreads();
+    tc::mbar_init_fence();
+  }
+  if (warp == 0) tc::tmem_alloc(tslot, 512);
+  {
+    const uint4* src = btiles + (size_t)blockIdx.x * (TC_B_BYTES / 16);
+    for (int i = tid; i < TC_B_BYTES / 16; i += TC_THREADS) reinterpret_cast<uint4*>(sB)[i] = src[i];
+  }
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = *tslot;
 
-    for (int ml = 0; ml < nm; ++ml) {
-      const uint8_t* ib = sIdx + ((size_t)(ml * CT + lane) * 27) * 4;
-      const uint32_t* kb = sKey + ((size_t)ml * LEAVES + 27 * sb + 9 * na) * 16;
-#pragma unroll 1
-      for (int k = 0; k < 4; ++k) {
-        uint32_t x[9];
+  auto give_up = [&]() {
+    *abort_flag = 1;
+    atomicExch(status, 3);
+  };
+  // Warp-uniform forms of the bounded wait and of the abort check: every lane takes the same
+  // branch before the warp-collective steps (__syncwarp, tcgen05.ld).
+  auto wait_all = [&](uint64_t* bar, uint32_t parity) {
+    const bool r = tc::mbar_wait(bar, parity, abort_flag, TC_WAIT_CYCLES);
+    return __all_sync(0xffffffffu, r);
+  };
+  auto aborted = [&]() { return __any_sync(0xffffffffu, *abort_flag != 0); };
+
+  if (warp >= TC_EPI_WARPS && warp < TC_EPI_WARPS + 2) {
+    // ---------------- producers ----------------
+    const int pid = tid - 32 * TC_EPI_WARPS;  // 0..63: rows pid and pid + 64
+    const uint4* row0 = table + ((size_t)(col0 + pid) << rl);
+    const uint4* row1 = table + ((size_t)(col0 + pid + 64) << rl);
+    const int half = (int)(p - 1) / 2;
+    for (int e = 0; e < nelem; ++e) {
+      if (aborted()) break;
+      const int m = m_begin + e;
+      uint4 w0[4], w1[4];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) x[q] = t20[ib[4 * q + k]] + t21[ib[4 * (q + 9) + k]] + t22[ib[4 * (q + 18) + k]];
-        // level-3 node (9 -> 3 x 3)
-#pragma unroll
-        for (int q = 0; q < 3; ++q) split3(x[q], x[q + 3], x[q + 6], w3a, w3as, w3b, w3bs, P.om, P.om_s, p);
-        // level-4 nodes (3 -> leaves)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-          const int t = 4 + 3 * na + b;
-          split3(x[3 * b], x[3 * b + 1], x[3 * b + 2], P.tw[sb][t][0], P.tws[sb][t][0], P.tw[sb][t][1],
-                 P.tws[sb][t][1], P.om, P.om_s, p);
+      for (int k = 0; k < 4; ++k) w0[k] = row0[4 * (size_t)m + k], w1[k] = row1[4 * (size_t)m + k];
+      // key rows of element m for the block's 54 leaves, centred into (-p/2, p/2]
+      const int ks = e & 3;
+      if (e >= 4 && !wait_all(&k_empty[ks], ((e >> 2) - 1) & 1)) {
+        give_up();
+        break;
+      }
+      {
+        const uint4* ksrc =
+            reinterpret_cast<const uint4*>(key + (((size_t)pi * elements + m) * LEAVES + TC_LEAVES * third) * 16);
+        int4* kdst = reinterpret_cast<int4*>(sKey + ks * TC_KEY_INTS);
+        for (int i = pid; i < TC_KEY_INTS / 4; i += 64) {
+          const uint4 u = ksrc[i];
+          int4 v;
+          v.x = (int)u.x > half ? (int)u.x - (int)p : (int)u.x;
+          v.y = (int)u.y > half ? (int)u.y - (int)p : (int)u.y;
+          v.z = (int)u.z > half ? (int)u.z - (int)p : (int)u.z;
+          v.w = (int)u.w > half ? (int)u.w - (int)p : (int)u.w;
+          kdst[i] = v;
         }
-        // Base multiplication with the key's leaves: acc[q][l] += M[k][l] x[q].
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&k_full[ks]);
+      }
+      bool ok = true;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-          uint32_t v = x[q] - __umulhi(x[q], P.bar) * p;
-          v = v >= p ? v - p : v;
-          const uint4 kv = *reinterpret_cast<const uint4*>(kb + q * 16 + 4 * k);
-          acc[q][0] += kv.x * v;
-          acc[q][1] += kv.y * v;
-          acc[q][2] += kv.z * v;
-          acc[q][3] += kv.w * v;
+      for (int k = 0; k < 4; ++k) {
+        if (ok && e >= 1 && !wait_all(&a_empty[k], (e - 1) & 1)) ok = false;
+        if (ok) {
+          uint8_t* slot = sA + k * TC_A_BYTES;
+          tc_write_row(slot, pid, w0[k]);
+          tc_write_row(slot, pid + 64, w1[k]);
+          tc::fence_proxy_async();
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(&a_full[k]);
         }
       }
-      if (++since == reduce_every) {
+      if (!ok) {
+        give_up();
+        break;
+      }
+    }
+  } else if (warp == TC_EPI_WARPS + 2) {
+    // ---------------- MMA issue ----------------
+    if (lane == 0) {
+      const uint32_t idesc = tc::idesc_bf16_f32(TC_COLS, TC_N);
+      const uint32_t b0 = tc::smem_u32(sB);
+      int issued = 0;
+      for (int e = 0; e < nelem && !*abort_flag; ++e) {
+        bool ok = true;
+        for (int k = 0; k < 4; ++k) {
+          if (!tc::mbar_wait(&a_full[k], e & 1, abort_flag, TC_WAIT_CYCLES) ||
+              (e >= 1 && !tc::mbar_wait(&t_empty[k], (e - 1) & 1, abort_flag, TC_WAIT_CYCLES))) {
+            ok = false;
+            break;
+          }
+          tc::fence_after_sync();
+          const uint32_t a0 = tc::smem_u32(sA + k * TC_A_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < 8; ++kk)
+            tc::mma_bf16(tbase + k * TC_N, tc::sdesc(a0 + kk * 256, 128, 2048), tc::sdesc(b0 + kk * 256, 128, 2048),
+                         idesc, kk > 0 ? 1u : 0u);
+          tc::mma_commit(&a_empty[k]);
+          tc::mma_commit(&t_full[k]);
+          ++issued;
+        }
+        if (!ok) {
+          give_up();
+          break;
+        }
+      }
+      // Drain: the last issued MMA must complete before the tensor memory is released.
+      if (issued > 0) {
+        const int last = issued - 1, e = last >> 2, k = last & 3;
+        const long long t0 = clock64();
+        while (!tc::mbar_try_wait(&t_full[k], e & 1) && clock64() - t0 < TC_WAIT_CYCLES) {
+        }
+      }
+    }
+  } else {
+    // ---------------- epilogue ----------------
+    const int g = warp >> 2, qd = warp & 3;
+    const int c = 32 * qd + lane;
+    const float pf = (float)p, invp = 1.0f / (float)p;
+    const float MAGIC = 12582912.0f;  // 1.5 * 2^23: adding it rounds to an integer
+    const uint32_t bias = (0x80000000u / p) * p;
+    int acc[9][4];
+#pragma unroll
+    for (int i = 0; i < 9; ++i)
+#pragma unroll
+      for (int l = 0; l < 4; ++l) acc[i][l] = 0;
+    int since = 0;
+    bool ok = true;
+    for (int e = 0; e < nelem && ok; ++e) {
+      const int ks = e & 3;
+      if (!wait_all(&k_full[ks], (e >> 2) & 1)) {
+        ok = false;
+        break;
+      }
+      const int4* kp = reinterpret_cast<const int4*>(sKey + ks * TC_KEY_INTS) + 9 * g * 4;
+      for (int k = 0; k < 4; ++k) {
+        if (!wait_all(&t_full[k], e & 1)) {
+          ok = false;
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t ta = tbase + ((uint32_t)(32 * qd) << 16) + k * TC_N + 18 * g;
+        // three leaves at a time keeps the live registers low (72 per thread at 864 threads)
+#pragma unroll
+        for (int ig = 0; ig < 3; ++ig) {
+          uint32_t v[6];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) tc::tmem_ld_x2(ta + 6 * ig + 2 * i, v[2 * i], v[2 * i + 1]);
+          tc::tmem_wait_ld(v);
+          if (ig == 2) {
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&t_empty[k]);
+          }
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            const int li = 3 * ig + i;
+            const float L = __uint_as_float(v[2 * i]) + __uint_as_float(v[2 * i + 1]);
+            const float q = fmaf(L, invp, MAGIC) - MAGIC;
+            const float r = fmaf(-q, pf, L);
+            const int ri = __float_as_int(r + MAGIC) - 0x4B400000;
+            const int4 kv = kp[li * 4 + k];
+            acc[li][0] += kv.x * ri;
+            acc[li][1] += kv.y * ri;
+            acc[li][2] += kv.z * ri;
+            acc[li][3] += kv.w * ri;
+          }
+        }
+      }
+      if (!ok) break;
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&k_empty[ks]);
+      if (++since == TC_REDUCE_EVERY) {
         since = 0;
 #pragma unroll
-        for (int q = 0; q < 9; ++q)
+        for (int i = 0; i < 9; ++i)
 #pragma unroll
-          for (int l = 0; l < 4; ++l) acc[q][l] = reduce32(acc[q][l], P.bar, p);
+          for (int l = 0; l < 4; ++l) acc[i][l] = (int)reduce32((uint32_t)acc[i][l] + bias, P.bar, p);
+      }
+    }
+    if (!ok) {
+      give_up();
+    } else {
+      uint32_t* out = partial + ((((size_t)split * nprimes + pi) * COLUMNS + col0 + c) * LEAVES + TC_LEAVES * third +
+                                 9 * g) * 4;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        uint4 o;
+        o.x = reduce32((uint32_t)acc[i][0] + bias, P.bar, p);
+        o.y = reduce32((uint32_t)acc[i][1] + bias, P.bar, p);
+        o.z = reduce32((uint32_t)acc[i][2] + bias, P.bar, p);
+        o.w = reduce32((uint32_t)acc[i][3] + bias, P.bar, p);
+        reinterpret_cast<uint4*>(out)[i] = o;
       }
     }
   }
-  uint32_t* out =
-      partial + ((((size_t)split * nprimes + pi) * COLUMNS + col0 + lane) * LEAVES + 27 * sb + 9 * na) * 4;
-#pragma unroll
-  for (int q = 0; q < 9; ++q) {
-    uint4 v;
-    v.x = reduce32(acc[q][0], P.bar, p);
-    v.y = reduce32(acc[q][1], P.bar, p);
-    v.z = reduce32(acc[q][2], P.bar, p);
-    v.w = reduce32(acc[q][3], P.bar, p);
-    reinterpret_cast<uint4*>(out)[q] = v;
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tbase, 512);
+}
+
+// B tiles of K1 on the tensor cores, per (prime, third): row n = 2 x (leaf within the third) +
+// limb, K order as tc_write_row, bf16 in the no-swizzle K-major core-matrix layout.
+static void fill_btiles(const PrimePlan& pl, const PrimeConst& c, uint16_t* out /* 3 x TC_B_BYTES/2 */) {
+  const uint64_t p = pl.p;
+  for (int third = 0; third < 3; ++third) {
+    uint16_t* tile = out + (size_t)third * (TC_B_BYTES / 2);
+    memset(tile, 0, TC_B_BYTES);
+    for (int n = 0; n < 2 * TC_LEAVES; ++n) {
+      const int s = TC_LEAVES * third + n / 2, limb = n & 1;
+      // V[s][j] = zeta_s^j for the 128 bit positions j
+      uint64_t pw[128];
+      pw[0] = 1;
+      for (int j = 1; j < 128; ++j) pw[j] = pw[j - 1] * c.leaf_root[s] % p;
+      for (int kappa = 0; kappa < 128; ++kappa) {
+        const int o = kappa >> 1, h = kappa & 1, w = o >> 4, t = o & 15;
+        const int j = 32 * w + t + 16 * h;
+        const uint64_t V = pw[j];
+        const float f = limb == 0 ? (float)(V & 255) * 0.5f : (float)(V >> 8) * 128.0f;
+        uint32_t u;
+        memcpy(&u, &f, 4);
+        const size_t off = (size_t)(n >> 3) * 2048 + (kappa >> 3) * 128 + (n & 7) * 16 + (kappa & 7) * 2;
+        tile[off / 2] = (uint16_t)(u >> 16);
+      }
+    }
   }
 }
 
-// Element splits of K1: the grid (32 column tiles x primes x splits) at one block per SM should
-// fill whole waves; among 8..24 splits take the one with the least idle SM time, then the fewest.
+// Element splits of K1: the grid (8 column tiles x primes x 3 leaf thirds x splits), one block
+// per SM, should fill whole waves; among 8..40 splits take the one with the least idle SM time,
+// then the fewest.
 int commit_splits(uint64_t elements, int nprimes, int sms) {
   if (sms < 1) sms = 1;
   int best = 1;
   double best_eff = -1;
-  for (int s = 8; s <= 24; ++s) {
-    if ((uint64_t)s * MB > elements) break;
-    const long blocks = (long)(COLUMNS / CT) * nprimes * s;
+  for (int s = 8; s <= 40; ++s) {
+    if ((uint64_t)s * 8 > elements) break;
+    const long blocks = (long)(COLUMNS / TC_COLS) * nprimes * 3 * s;
     const long waves = (blocks + sms - 1) / sms;
     const double eff = (double)blocks / (double)(waves * sms);
     if (eff > best_eff + 1e-9) best_eff = eff, best = s;
   }
   if (best_eff < 0) {
     best = 1;
-    while ((uint64_t)best * 2 * MB <= elements && best < 8) best *= 2;
+    while ((uint64_t)best * 2 <= elements && best < 8) best *= 2;
   }
   return best;
 }
 
-void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint32_t* key, const uint32_t* t2,
-                   uint32_t* partial, int splits, cudaStream_t s) {
-  int elements = (int)sh.ring_elements;
-  int per = (elements + splits - 1) / splits;
-  // Accumulators take 4 products below p^2 per element; reduce before 2^32 can be reached.
-  uint64_t pmax = 0;
-  for (int i = 0; i < mp.nprimes; ++i) pmax = mp.primes[i] > pmax ? mp.primes[i] : pmax;
-  uint64_t per_elem = 4 * (pmax - 1) * (pmax - 1);
-  int reduce_every = (int)((0xffffffffull - pmax) / per_elem);
-  if (reduce_every < 1) reduce_every = 1;
-  dim3 grid(COLUMNS / CT, mp.nprimes, splits);
-  const size_t smem = commit_smem_bytes();
+void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint32_t* key,
+                   const uint16_t* btiles, uint32_t* partial, int splits, int* status, cudaStream_t s) {
+  const int elements = (int)sh.ring_elements;
+  const int per = (elements + splits - 1) / splits;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_commit_ntt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_commit_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     attr = true;
   }
-  k_commit_ntt<<<grid, KTHREADS, smem, s>>>(table, key, t2, partial, sh.rl, elements, per, mp.nprimes, reduce_every);
+  dim3 grid(mp.nprimes * 3, COLUMNS / TC_COLS, splits);
+  k_commit_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(table, key, reinterpret_cast<const uint4*>(btiles), partial, sh.rl,
+                                                 elements, per, mp.nprimes, status);
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -18,7 +18,6 @@ constexpr int LEAVES = 162;      // slots of the transform over Y = X^4
 constexpr int COLUMN_LOG = 10;   // verifier/proof_verify/src/main.rs:37
 constexpr int COLUMNS = 1 << COLUMN_LOG;
 constexpr int MAX_PRIMES = 12;
-constexpr int T2_WORDS = 6 * 3 * 3 * 32;  // per prime: [sb][a][t][32]
 constexpr int STREAM_PREFIX = 112;  // transcript bytes before the commitment (see host code)
 
 // The shape of one instance, derived from LOG_VARS (main.rs:32-46).
@@ -52,10 +51,7 @@ bool make_plan(uint32_t p, PrimePlan& out);
 // Device-side constants of one prime, uploaded once per modulus.
 struct PrimeConst {
   uint32_t p, bar;                 // bar = floor(2^32 / p)
-  uint32_t om, om_s;               // cube root of unity eta^162 and its Shoup companion
-  uint32_t tw[6][13][2];           // forward twiddles of the 13 nodes inside a sub-block
-  uint32_t tws[6][13][2];          // Shoup companions
-  uint32_t T[6][32];               // fused first two levels on 5 input bits
+  uint32_t om;                     // cube root of unity eta^162
   uint32_t itw[80][2];             // inverse twiddles eta^-(e/3), eta^-(2e/3) per internal node
   uint32_t inv3, iom, iom2;        // 1/3, omega^-1, omega^-2
   uint32_t w, w5, inv_split;       // eta^81, eta^405, 1/(eta^81 - eta^405)
@@ -70,9 +66,9 @@ struct ModulusPlan {
   uint32_t primes[MAX_PRIMES];
   bool exact_lift = false;         // true: CRT gives the integer product, reduced mod q after
   std::vector<PrimeConst> consts;
-  // Per prime, the level-2 split fused into the lookups: [sb][child a][term t][32] (lives in global
-  // memory; too large for the constant bank at 12 primes).
-  std::vector<uint32_t> t2;
+  // Per prime and third of its leaves, the Vandermonde limbs of the tensor-core commitment
+  // (bf16 bits in the MMA's shared-memory layout).
+  std::vector<uint16_t> btiles;
   // Garner constants: inv[i][j] = p_j^-1 mod p_i for j < i
   uint32_t garner_inv[MAX_PRIMES][MAX_PRIMES];
 };
@@ -139,9 +135,8 @@ void launch_matrix_expand(const ModulusPlan& mp, uint64_t elements, uint32_t* ar
 void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32_t* ared, uint32_t* leafvals,
                           uint32_t* key, cudaStream_t s);
 int commit_splits(uint64_t elements, int nprimes, int sms);
-size_t commit_smem_bytes();
-void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint32_t* key, const uint32_t* t2,
-                   uint32_t* partial, int splits, cudaStream_t s);
+void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint32_t* key,
+                   const uint16_t* btiles, uint32_t* partial, int splits, int* status, cudaStream_t s);
 void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t* partial, int splits,
                           uint8_t* out, cudaStream_t s);
 

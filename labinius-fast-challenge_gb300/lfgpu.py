@@ -20,7 +20,7 @@ ERRORS = {
 }
 NOALLOC_MAX_CHALLENGES = 4096
 EXPORTS = [
-    "lf_ctx_create", "lf_ctx_destroy", "lf_proof_size", "lf_accept_modulus", "lf_key_prepare", "lf_prove",
+    "lf_ctx_create", "lf_ctx_destroy", "lf_ctx_stream", "lf_proof_size", "lf_accept_modulus", "lf_key_prepare", "lf_prove",
     "lf_prove_device", "lf_write_table_device", "lf_device_alloc", "lf_device_free", "lf_memcpy_h2d",
     "lf_last_profile", "lf_strerror", "lf_last_error", "lf_last_challenges",
     "lf_sample_challenges", "lf_sample_challenges_noalloc",
@@ -61,6 +61,8 @@ def load(path=LIB_PATH):
     lib.lf_ctx_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(p)]
     lib.lf_ctx_destroy.argtypes = [p]
     lib.lf_ctx_destroy.restype = None
+    lib.lf_ctx_stream.argtypes = [p]
+    lib.lf_ctx_stream.restype = p
     lib.lf_proof_size.argtypes = [ctypes.c_char_p, ctypes.c_uint32]
     lib.lf_proof_size.restype = sz
     lib.lf_accept_modulus.argtypes = [ctypes.c_char_p, ctypes.c_uint32]
@@ -166,6 +168,10 @@ class Prover:
 
     def key_prepare(self, log_vars, q=BASELINE_Q):
         self._check(self.lib.lf_key_prepare(self.ctx, q_bytes(q), log_vars))
+
+    def stream(self):
+        """The context's cudaStream_t as an int (every call of this prover runs on it)."""
+        return self.lib.lf_ctx_stream(self.ctx) or 0
 
     def alloc(self, nbytes):
         p = ctypes.c_void_p()
