@@ -27,16 +27,15 @@ __constant__ PrimeConst c_prime[MAX_PRIMES];
 // Shape of K1 on the tensor cores (the kernel is described where it is defined).
 constexpr int TC_COLS = 128;                         // table columns per block (MMA M)
 constexpr int TC_LEAVES = 54;                        // leaves per block (a third of a prime)
-constexpr int TC_N = 112;                            // MMA N: 54 leaves x 2 limbs, padded to 16
-constexpr int TC_EPI_WARPS = 24;
-constexpr int TC_THREADS = 32 * (TC_EPI_WARPS + 3);  // + 2 producer warps + 1 MMA warp
-constexpr int TC_A_BYTES = TC_COLS * 128 * 2;        // 32 KB per A slot
-constexpr int TC_B_BYTES = TC_N * 128 * 2;           // 28 KB
+constexpr int TC_N = 64;                             // MMA N: 6 groups of 10 rows (9 leaves + 1 zero), padded
+constexpr int TC_K = 256;                            // MMA K: 128 bits x 2 limbs (A read twice)
+constexpr int TC_THREADS = 32 * 24;                  // 24 warps; lane 0 of the last also issues the MMAs
+constexpr int TC_A_BYTES = TC_COLS * 128 * 2;        // 32 KB per A slot (one table word per column)
+constexpr int TC_B_BYTES = TC_N * TC_K * 2;          // 32 KB
 constexpr int TC_KEY_INTS = TC_LEAVES * 16;          // one element's key rows for the block's leaves
-constexpr int TC_SMEM = 4 * TC_A_BYTES + TC_B_BYTES + 4 * TC_KEY_INTS * 4 + 24 * 8 + 16;
+constexpr int TC_SMEM = 4 * TC_A_BYTES + TC_B_BYTES + 4 * TC_KEY_INTS * 4 + 2 * 8 + 16;
 constexpr int TC_REDUCE_EVERY = 6;                   // elements between accumulator reductions
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;   // ~1 s at 2 GHz
-
 
 static void fill_btiles(const PrimePlan& pl, const PrimeConst& c, uint16_t* out);
 
@@ -313,19 +312,25 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
 // The transform of a table word (128 bits = the Y-coefficients 0..127 of one residue class of X
 // mod 4) at leaf s is the evaluation sum_j bit_j zeta_s^j (mod p), zeta_s the leaf's root: a
 // product with the Vandermonde matrix V[s][j] = zeta_s^j. On the tensor core it is exact:
-//   A (M = 128 table columns x K = 128 bits) holds each bit as bf16 2.0 or 0,
-//   B (N = 112 x K) holds, per leaf, the two limbs (V mod 256) / 2 and (V >> 8) * 128 (both exact
-//   in bf16), and the f32 accumulators give D_lo + D_hi = sum_j bit_j V[s][j] < 2^22 exactly.
-// The epilogue reduces that sum mod p in f32 (exact: every intermediate is an integer below
-// 2^24), then does the 4x4 base multiplication with the key on the integer pipe.
+//   A (M = 128 table columns x 128 bits) holds each bit as bf16 2.0 or 0 and is read twice;
+//   B (N = 64 x K = 256) holds per leaf (V mod 256) / 2 against the first reading and
+//   (V >> 8) * 128 against the second (both exact in bf16), so the f32 accumulator is
+//   sum_j bit_j V[s][j] < 2^22, an exact integer.
+// The epilogue reduces that sum mod p in f32 (every intermediate is an integer below 2^24), then
+// does the 4x4 base multiplication with the key on the integer pipe.
 //
 // Block = one prime x one third of its 162 leaves (54) x 128 table columns x an element range.
-//   warps 0-23  epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (= its 32 columns) and owns
-//               leaves 9 (w / 4) .. +8 of the third, 9 x 4 accumulators per thread;
-//   warps 24-25 producers: table words -> bf16 A tiles (4 slots, one per word k of an element)
-//               and the element's key rows -> shared memory (4-element ring);
-//   warp 26     lane 0 issues the MMAs: word k of an element into TMEM columns 112 k .. +111.
-// Every wait is bounded (about a second); a timeout sets *status = 3 and the block drains.
+// Warps 0-23 do everything but the MMAs, in one loop over elements e:
+//   wait until the MMAs of e are done (their A slots are then free and TMEM buffer e % 2 full);
+//   expand element e + 1 into the four A slots (threads 0-511: column t % 128, word t / 128;
+//   its words were loaded one element earlier) and copy its key rows (threads 512-727) into a
+//   4-element ring; block barrier;
+//   epilogue of e: warp w reads TMEM lanes 32 (w % 4) .. +31 (its 32 columns), columns
+//   256 (e % 2) + 64 k + 10 (w / 4) + i, for leaves 9 (w / 4) + i, and accumulates 9 x 4 values.
+// After the barrier, lane 0 of warp 23 issues the MMAs of e + 1 (64 instructions), so the tensor
+// core works on e + 1 while the CUDA cores finish e. The waits on the tensor core are bounded
+// (about a second); a timeout sets *status = 3 and the block skips its remaining work but keeps
+// the barrier count, so every thread drains.
 // ------------------------------------------------------------------------------------------------
 // Word -> one row of an A slot. u32 o = 16 w + t of the row holds bits 32 w + t (low bf16) and
 // 32 w + t + 16 (high bf16) of the word as 2.0 (0x4000) or 0; the B tiles use the same K order.
@@ -351,14 +356,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint8_t* sA = tsm;
   uint8_t* sB = tsm + 4 * TC_A_BYTES;
   int* sKey = reinterpret_cast<int*>(sB + TC_B_BYTES);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sKey + 4 * TC_KEY_INTS);
-  uint64_t* a_full = bars;
-  uint64_t* a_empty = bars + 4;
-  uint64_t* t_full = bars + 8;
-  uint64_t* t_empty = bars + 12;
-  uint64_t* k_full = bars + 16;
-  uint64_t* k_empty = bars + 20;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 24);
+  uint64_t* t_full = reinterpret_cast<uint64_t*>(sKey + 4 * TC_KEY_INTS);  // [2] MMAs of an element done
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(t_full + 2);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
 
   const int pi = blockIdx.x / 3, third = blockIdx.x % 3;
@@ -372,14 +371,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
   if (tid == 0) {
     *abort_flag = 0;
-    for (int i = 0; i < 4; ++i) {
-      tc::mbar_init(&a_full[i], 2);
-      tc::mbar_init(&a_empty[i], 1);
-      tc::mbar_init(&t_full[i], 1);
-      tc::mbar_init(&t_empty[i], TC_EPI_WARPS);
-      tc::mbar_init(&k_full[i], 2);
-      tc::mbar_init(&k_empty[i], TC_EPI_WARPS);
-    }
+    tc::mbar_init(&t_full[0], 1);
+    tc::mbar_init(&t_full[1], 1);
     tc::mbar_init_fence();
   }
   if (warp == 0) tc::tmem_alloc(tslot, 512);
@@ -393,109 +386,51 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
 
-  auto give_up = [&]() {
-    *abort_flag = 1;
-    atomicExch(status, 3);
+  // MMA issue (lane 0 of warp 23): element e into TMEM buffer e % 2, one commit per element.
+  const bool issuer = tid == TC_THREADS - 32;
+  int last = -1;
+  auto issue = [&](int e) {
+    if (!issuer || *abort_flag) return;
+    const uint32_t idesc = tc::idesc_bf16_f32(TC_COLS, TC_N);
+    const uint64_t adesc0 = tc::sdesc(tc::smem_u32(sA), 128, 2048);
+    const uint64_t bdesc0 = tc::sdesc(tc::smem_u32(sB), 128, 4096);
+    const uint32_t d0 = tbase + 256 * (e & 1);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int kk = 0; kk < TC_K / 16; ++kk)
+        tc::mma_bf16(d0 + TC_N * k, adesc0 + (uint64_t)(k * (TC_A_BYTES >> 4) + (kk & 7) * 16),
+                     bdesc0 + (uint64_t)(kk * 16), idesc, kk > 0 ? 1u : 0u);
+    tc::mma_commit(&t_full[e & 1]);
+    last = e;
   };
-  // Warp-uniform forms of the bounded wait and of the abort check: every lane takes the same
-  // branch before the warp-collective steps (__syncwarp, tcgen05.ld).
-  auto wait_all = [&](uint64_t* bar, uint32_t parity) {
-    const bool r = tc::mbar_wait(bar, parity, abort_flag, TC_WAIT_CYCLES);
-    return __all_sync(0xffffffffu, r);
-  };
-  auto aborted = [&]() { return __any_sync(0xffffffffu, *abort_flag != 0); };
-
-  if (warp >= TC_EPI_WARPS && warp < TC_EPI_WARPS + 2) {
-    // ---------------- producers ----------------
-    const int pid = tid - 32 * TC_EPI_WARPS;  // 0..63: rows pid and pid + 64
-    const uint4* row0 = table + ((size_t)(col0 + pid) << rl);
-    const uint4* row1 = table + ((size_t)(col0 + pid + 64) << rl);
+  {
+    // ---------------- expansion + epilogue ----------------
+    const bool expander = tid < 4 * TC_COLS;                      // column tid % 128, word tid / 128
+    const bool keyer = tid >= 4 * TC_COLS && tid < 4 * TC_COLS + TC_KEY_INTS / 4;
+    const uint4* wsrc = table + ((size_t)(col0 + (tid & (TC_COLS - 1))) << rl) + (tid >> 7);
+    const uint4* ksrc = reinterpret_cast<const uint4*>(key) +
+                        ((size_t)pi * elements * LEAVES + TC_LEAVES * third) * 4 + (tid - 4 * TC_COLS);
     const int half = (int)(p - 1) / 2;
-    for (int e = 0; e < nelem; ++e) {
-      if (aborted()) break;
-      const int m = m_begin + e;
-      uint4 w0[4], w1[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) w0[k] = row0[4 * (size_t)m + k], w1[k] = row1[4 * (size_t)m + k];
-      // key rows of element m for the block's 54 leaves, centred into (-p/2, p/2]
-      const int ks = e & 3;
-      if (e >= 4 && !wait_all(&k_empty[ks], ((e >> 2) - 1) & 1)) {
-        give_up();
-        break;
+    auto load_pre = [&](int e) -> uint4 {  // this thread's input for element e
+      const size_t m = (size_t)(m_begin + e);
+      if (expander) return wsrc[4 * m];
+      if (keyer) return ksrc[m * LEAVES * 4];
+      return make_uint4(0, 0, 0, 0);
+    };
+    auto store_pre = [&](int e, uint4 u) {  // ... into the A slots / the key ring
+      if (expander) {
+        tc_write_row(sA + (tid >> 7) * TC_A_BYTES, tid & (TC_COLS - 1), u);
+      } else if (keyer) {
+        int4 v;  // centred into (-p/2, p/2]
+        v.x = (int)u.x > half ? (int)u.x - (int)p : (int)u.x;
+        v.y = (int)u.y > half ? (int)u.y - (int)p : (int)u.y;
+        v.z = (int)u.z > half ? (int)u.z - (int)p : (int)u.z;
+        v.w = (int)u.w > half ? (int)u.w - (int)p : (int)u.w;
+        reinterpret_cast<int4*>(sKey + (e & 3) * TC_KEY_INTS)[tid - 4 * TC_COLS] = v;
       }
-      {
-        const uint4* ksrc =
-            reinterpret_cast<const uint4*>(key + (((size_t)pi * elements + m) * LEAVES + TC_LEAVES * third) * 16);
-        int4* kdst = reinterpret_cast<int4*>(sKey + ks * TC_KEY_INTS);
-        for (int i = pid; i < TC_KEY_INTS / 4; i += 64) {
-          const uint4 u = ksrc[i];
-          int4 v;
-          v.x = (int)u.x > half ? (int)u.x - (int)p : (int)u.x;
-          v.y = (int)u.y > half ? (int)u.y - (int)p : (int)u.y;
-          v.z = (int)u.z > half ? (int)u.z - (int)p : (int)u.z;
-          v.w = (int)u.w > half ? (int)u.w - (int)p : (int)u.w;
-          kdst[i] = v;
-        }
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&k_full[ks]);
-      }
-      bool ok = true;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        if (ok && e >= 1 && !wait_all(&a_empty[k], (e - 1) & 1)) ok = false;
-        if (ok) {
-          uint8_t* slot = sA + k * TC_A_BYTES;
-          tc_write_row(slot, pid, w0[k]);
-          tc_write_row(slot, pid + 64, w1[k]);
-          tc::fence_proxy_async();
-          __syncwarp();
-          if (lane == 0) tc::mbar_arrive(&a_full[k]);
-        }
-      }
-      if (!ok) {
-        give_up();
-        break;
-      }
-    }
-  } else if (warp == TC_EPI_WARPS + 2) {
-    // ---------------- MMA issue ----------------
-    if (lane == 0) {
-      const uint32_t idesc = tc::idesc_bf16_f32(TC_COLS, TC_N);
-      const uint32_t b0 = tc::smem_u32(sB);
-      int issued = 0;
-      for (int e = 0; e < nelem && !*abort_flag; ++e) {
-        bool ok = true;
-        for (int k = 0; k < 4; ++k) {
-          if (!tc::mbar_wait(&a_full[k], e & 1, abort_flag, TC_WAIT_CYCLES) ||
-              (e >= 1 && !tc::mbar_wait(&t_empty[k], (e - 1) & 1, abort_flag, TC_WAIT_CYCLES))) {
-            ok = false;
-            break;
-          }
-          tc::fence_after_sync();
-          const uint32_t a0 = tc::smem_u32(sA + k * TC_A_BYTES);
-#pragma unroll
-          for (int kk = 0; kk < 8; ++kk)
-            tc::mma_bf16(tbase + k * TC_N, tc::sdesc(a0 + kk * 256, 128, 2048), tc::sdesc(b0 + kk * 256, 128, 2048),
-                         idesc, kk > 0 ? 1u : 0u);
-          tc::mma_commit(&a_empty[k]);
-          tc::mma_commit(&t_full[k]);
-          ++issued;
-        }
-        if (!ok) {
-          give_up();
-          break;
-        }
-      }
-      // Drain: the last issued MMA must complete before the tensor memory is released.
-      if (issued > 0) {
-        const int last = issued - 1, e = last >> 2, k = last & 3;
-        const long long t0 = clock64();
-        while (!tc::mbar_try_wait(&t_full[k], e & 1) && clock64() - t0 < TC_WAIT_CYCLES) {
-        }
-      }
-    }
-  } else {
-    // ---------------- epilogue ----------------
+    };
+
     const int g = warp >> 2, qd = warp & 3;
     const int c = 32 * qd + lane;
     const float pf = (float)p, invp = 1.0f / (float)p;
@@ -506,63 +441,74 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     for (int i = 0; i < 9; ++i)
 #pragma unroll
       for (int l = 0; l < 4; ++l) acc[i][l] = 0;
+
+    uint4 pre = make_uint4(0, 0, 0, 0);
+    if (nelem > 0) {
+      store_pre(0, load_pre(0));
+      if (nelem > 1) pre = load_pre(1);
+      tc::fence_proxy_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      tc::fence_after_sync();
+      issue(0);
+    }
     int since = 0;
-    bool ok = true;
-    for (int e = 0; e < nelem && ok; ++e) {
-      const int ks = e & 3;
-      if (!wait_all(&k_full[ks], (e >> 2) & 1)) {
-        ok = false;
-        break;
-      }
-      const int4* kp = reinterpret_cast<const int4*>(sKey + ks * TC_KEY_INTS) + 9 * g * 4;
-      for (int k = 0; k < 4; ++k) {
-        if (!wait_all(&t_full[k], e & 1)) {
-          ok = false;
-          break;
+    for (int e = 0; e < nelem; ++e) {
+      bool ok = !*abort_flag;
+      if (ok) {
+        ok = __all_sync(0xffffffffu, tc::mbar_wait(&t_full[e & 1], (e >> 1) & 1, abort_flag, TC_WAIT_CYCLES));
+        if (!ok) {
+          *abort_flag = 1;
+          atomicExch(status, 3);
         }
+      }
+      ok = __all_sync(0xffffffffu, ok);
+      tc::fence_after_sync();
+      if (e + 1 < nelem) {
+        if (ok) store_pre(e + 1, pre);
+        if (e + 2 < nelem) pre = load_pre(e + 2);
+        tc::fence_proxy_async();
+        tc::fence_before_sync();
+        __syncthreads();
         tc::fence_after_sync();
-        const uint32_t ta = tbase + ((uint32_t)(32 * qd) << 16) + k * TC_N + 18 * g;
-        // three leaves at a time keeps the live registers low (72 per thread at 864 threads)
-#pragma unroll
-        for (int ig = 0; ig < 3; ++ig) {
-          uint32_t v[6];
-#pragma unroll
-          for (int i = 0; i < 3; ++i) tc::tmem_ld_x2(ta + 6 * ig + 2 * i, v[2 * i], v[2 * i + 1]);
+        issue(e + 1);
+      }
+      if (ok) {
+        const int4* kp = reinterpret_cast<const int4*>(sKey + (e & 3) * TC_KEY_INTS) + 9 * g * 4;
+        const uint32_t tb = tbase + ((uint32_t)(32 * qd) << 16) + 256 * (e & 1) + 10 * g;
+        for (int k = 0; k < 4; ++k) {
+          const uint32_t ta = tb + TC_N * k;
+          uint32_t v[9];
+          tc::tmem_ld_x2(ta + 0, v[0], v[1]);
+          tc::tmem_ld_x2(ta + 2, v[2], v[3]);
+          tc::tmem_ld_x2(ta + 4, v[4], v[5]);
+          tc::tmem_ld_x2(ta + 6, v[6], v[7]);
+          tc::tmem_ld_x1(ta + 8, v[8]);
           tc::tmem_wait_ld(v);
-          if (ig == 2) {
-            tc::fence_before_sync();
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(&t_empty[k]);
-          }
 #pragma unroll
-          for (int i = 0; i < 3; ++i) {
-            const int li = 3 * ig + i;
-            const float L = __uint_as_float(v[2 * i]) + __uint_as_float(v[2 * i + 1]);
+          for (int i = 0; i < 9; ++i) {
+            const float L = __uint_as_float(v[i]);
             const float q = fmaf(L, invp, MAGIC) - MAGIC;
             const float r = fmaf(-q, pf, L);
             const int ri = __float_as_int(r + MAGIC) - 0x4B400000;
-            const int4 kv = kp[li * 4 + k];
-            acc[li][0] += kv.x * ri;
-            acc[li][1] += kv.y * ri;
-            acc[li][2] += kv.z * ri;
-            acc[li][3] += kv.w * ri;
+            const int4 kv = kp[i * 4 + k];
+            acc[i][0] += kv.x * ri;
+            acc[i][1] += kv.y * ri;
+            acc[i][2] += kv.z * ri;
+            acc[i][3] += kv.w * ri;
           }
         }
-      }
-      if (!ok) break;
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&k_empty[ks]);
-      if (++since == TC_REDUCE_EVERY) {
-        since = 0;
+        if (++since == TC_REDUCE_EVERY) {
+          since = 0;
 #pragma unroll
-        for (int i = 0; i < 9; ++i)
+          for (int i = 0; i < 9; ++i)
 #pragma unroll
-          for (int l = 0; l < 4; ++l) acc[i][l] = (int)reduce32((uint32_t)acc[i][l] + bias, P.bar, p);
+            for (int l = 0; l < 4; ++l) acc[i][l] = (int)reduce32((uint32_t)acc[i][l] + bias, P.bar, p);
+        }
       }
     }
-    if (!ok) {
-      give_up();
-    } else {
+    tc::fence_before_sync();
+    if (!*abort_flag) {
       uint32_t* out = partial + ((((size_t)split * nprimes + pi) * COLUMNS + col0 + c) * LEAVES + TC_LEAVES * third +
                                  9 * g) * 4;
 #pragma unroll
@@ -576,36 +522,45 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
     }
   }
+  // Drain: the last commit covers every MMA issued; TMEM is released only after it.
+  if (issuer && last >= 0) {
+    const long long t0 = clock64();
+    while (!tc::mbar_try_wait(&t_full[last & 1], (last >> 1) & 1) && clock64() - t0 < TC_WAIT_CYCLES) {
+    }
+  }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   if (warp == 0) tc::tmem_dealloc(tbase, 512);
 }
 
-// B tiles of K1 on the tensor cores, per (prime, third): row n = 2 x (leaf within the third) +
-// limb, K order as tc_write_row, bf16 in the no-swizzle K-major core-matrix layout.
+// B tiles of K1 on the tensor cores, per (prime, third): row 10 g + i = leaf 9 g + i of the third
+// (rows 10 g + 9 and 60..63 zero); K position kappa < 128 carries the low limb of bit j(kappa),
+// kappa >= 128 the high limb of bit j(kappa - 128), j in the K order of tc_write_row; bf16 in
+// the no-swizzle K-major core-matrix layout (8 x 16 B cores, K-adjacent 128 B apart, 8-row
+// groups 4096 B apart).
 static void fill_btiles(const PrimePlan& pl, const PrimeConst& c, uint16_t* out /* 3 x TC_B_BYTES/2 */) {
   const uint64_t p = pl.p;
   for (int third = 0; third < 3; ++third) {
     uint16_t* tile = out + (size_t)third * (TC_B_BYTES / 2);
     memset(tile, 0, TC_B_BYTES);
-    for (int n = 0; n < 2 * TC_LEAVES; ++n) {
-      const int s = TC_LEAVES * third + n / 2, limb = n & 1;
-      // V[s][j] = zeta_s^j for the 128 bit positions j
-      uint64_t pw[128];
-      pw[0] = 1;
-      for (int j = 1; j < 128; ++j) pw[j] = pw[j - 1] * c.leaf_root[s] % p;
-      for (int kappa = 0; kappa < 128; ++kappa) {
-        const int o = kappa >> 1, h = kappa & 1, w = o >> 4, t = o & 15;
-        const int j = 32 * w + t + 16 * h;
-        const uint64_t V = pw[j];
-        const float f = limb == 0 ? (float)(V & 255) * 0.5f : (float)(V >> 8) * 128.0f;
-        uint32_t u;
-        memcpy(&u, &f, 4);
-        const size_t off = (size_t)(n >> 3) * 2048 + (kappa >> 3) * 128 + (n & 7) * 16 + (kappa & 7) * 2;
-        tile[off / 2] = (uint16_t)(u >> 16);
+    for (int g = 0; g < 6; ++g)
+      for (int i = 0; i < 9; ++i) {
+        const int n = 10 * g + i, s = TC_LEAVES * third + 9 * g + i;
+        uint64_t pw[128];  // V[s][j] = zeta_s^j
+        pw[0] = 1;
+        for (int j = 1; j < 128; ++j) pw[j] = pw[j - 1] * c.leaf_root[s] % p;
+        for (int kappa = 0; kappa < TC_K; ++kappa) {
+          const int limb = kappa >> 7, kk = kappa & 127;
+          const int o = kk >> 1, h = kk & 1, w = o >> 4, t = o & 15;
+          const uint64_t V = pw[32 * w + t + 16 * h];
+          const float f = limb == 0 ? (float)(V & 255) * 0.5f : (float)(V >> 8) * 128.0f;
+          uint32_t u;
+          memcpy(&u, &f, 4);
+          const size_t off = (size_t)(n >> 3) * 4096 + (kappa >> 3) * 128 + (n & 7) * 16 + (kappa & 7) * 2;
+          tile[off / 2] = (uint16_t)(u >> 16);
+        }
       }
-    }
   }
 }
 
