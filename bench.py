@@ -42,7 +42,8 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 def seeds(n, rank=0):
     import hashlib
 
-    return [hashlib.sha256(b"lf-bench/seed" + bytes([rank, i])).digest() for i in range(n)]
+    return [hashlib.sha256(b"lf-bench/seed" + rank.to_bytes(4, "little") + i.to_bytes(4, "little")).digest()
+            for i in range(n)]
 
 
 def dist_init(n_gpus):
@@ -253,6 +254,83 @@ def commit_roofline(log_vars, commit_ms):
             "flops_per_launch": flops}
 
 
+def batched_leg(lfgpu, prover, n=32, seed=20260):
+    """32 proofs through lf_prove_batch from page-locked host tables, L_i = 20 + floor(9 U_i)
+    (tables 2^13..2^21 words, log-uniform over integer exponents); keys for every shape are built
+    by a first, untimed batch."""
+    import random
+
+    import torch
+
+    rng = random.Random(seed)
+    shapes = [20 + int(9 * rng.random()) for _ in range(n)]
+    hosts, jobs = {}, []
+    for i, lv in enumerate(shapes):
+        s = seeds(1, 200 + i)[0]
+        dev = device_table(prover, s, lv)
+        h = torch.empty(dev.numel(), dtype=torch.uint8, pin_memory=True)
+        h.copy_(dev)
+        hosts[i] = h
+        jobs.append(prover.make_job(s, h.data_ptr(), lv, nbytes=h.numel()))
+    torch.cuda.synchronize()
+    prover.prove_batch(jobs)  # keys for every shape, pages touched
+    t0 = time.perf_counter()
+    res = prover.prove_batch(jobs)
+    dt = time.perf_counter() - t0
+    bad = [r.status for r in res if r.status != 0]
+    if bad:
+        raise RuntimeError(f"batched proofs failed: {bad}")
+    return {"proofs_per_s": round(n / dt, 1), "jobs": n, "total_ms": round(dt * 1e3, 2),
+            "log_vars": shapes, "tables": "page-locked host memory, H2D inside the timed batch"}
+
+
+def serving_leg(lfgpu, prover, requests=100, rate=8.0, seed=20261):
+    """Poisson arrivals at `rate`/s, L uniform over the integers 22..31 (log-uniform table sizes),
+    a fresh seed per request, one page-locked table per shape; latency = queueing + proving as
+    the server reports it. p50/p99 over the requests."""
+    import random
+
+    import torch
+
+    rng = random.Random(seed)
+    pool = {}
+    for lv in range(22, 32):
+        dev = device_table(prover, seeds(1, 300 + lv)[0], lv)
+        h = torch.empty(dev.numel(), dtype=torch.uint8, pin_memory=True)
+        h.copy_(dev)
+        pool[lv] = h
+    torch.cuda.synchronize()
+    warm = [prover.make_job(seeds(1, 400 + lv)[0], pool[lv].data_ptr(), lv, nbytes=pool[lv].numel())
+            for lv in range(22, 32)]
+    prover.prove_batch(warm)  # keys for every shape
+    arrivals, t = [], 0.0
+    for _ in range(requests):
+        t += rng.expovariate(rate)
+        arrivals.append(t)
+    shapes = [rng.randint(22, 31) for _ in range(requests)]
+    jobs, tickets = [], []
+    t0 = time.perf_counter()
+    for i, (at, lv) in enumerate(zip(arrivals, shapes)):
+        delay = at - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        j = prover.make_job(seeds(1, 1000 + i)[0], pool[lv].data_ptr(), lv, nbytes=pool[lv].numel())
+        jobs.append(j)
+        tickets.append(prover.submit(j))
+    lat = []
+    for t_ in tickets:
+        rc, r = prover.poll(t_, 120000)
+        if rc != 0 or r.status != 0:
+            raise RuntimeError(f"served request failed: {rc} {r.status}")
+        lat.append(r.queue_ms + r.run_ms)
+    wall = time.perf_counter() - t0
+    lat.sort()
+    pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))]
+    return {"p50_ms": round(pct(0.50), 3), "p99_ms": round(pct(0.99), 3), "requests": requests,
+            "rate_per_s": rate, "log_vars": "uniform 22..31", "wall_s": round(wall, 2),
+            "latency": "queue + prove, host tables (H2D included)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -264,6 +342,9 @@ def main():
     ap.add_argument("--no-process", action="store_true", help="skip the process-level end-to-end leg")
     ap.add_argument("--tables", type=int, default=5, help="distinct seeded tables the timed steps cycle over")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-table (lf_prove) leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched (lf_prove_batch) leg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving (lf_submit/lf_poll) leg")
+    ap.add_argument("--serve-requests", type=int, default=100, help="requests of the serving leg (Poisson, 8/s)")
     args = ap.parse_args()
     rank, world, local = dist_init(args.gpus)
     if args.impl == "reference":
@@ -336,6 +417,18 @@ def main():
             proc_ms, _ = process_e2e(lfgpu, prover, log_vars)
         except Exception as e:  # reported, not fatal
             proc_ms = f"failed: {e}"
+    batched = None
+    if not args.no_batch:
+        try:
+            batched = batched_leg(lfgpu, prover)
+        except Exception as e:  # reported, not fatal
+            batched = f"failed: {e}"
+    serving = None
+    if not args.no_serve:
+        try:
+            serving = serving_leg(lfgpu, prover, requests=args.serve_requests)
+        except Exception as e:  # reported, not fatal
+            serving = f"failed: {e}"
     cpu = None
     if not args.no_cpu:
         cms, cores = cpu_baseline(log_vars, bytes(host.numpy()), e2e_seed, proof)
@@ -355,6 +448,8 @@ def main():
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms/proof", "h2d_bytes_per_step": tbytes,
                 "d2h_bytes_per_step": cap},
         "process_e2e_ms": proc_ms,
+        "batched": batched,
+        "serving": serving,
         "phases_ms": phases,
         "roofline": commit_roofline(log_vars, med["commit_ms"]),
         "cpu_baseline": cpu,

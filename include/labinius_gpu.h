@@ -29,6 +29,8 @@ extern "C" {
 #define LF_E_INTERNAL (-8)  /* a device-side check failed (challenge sampling bound, fold range) */
 #define LF_E_ADMISSION (-9) /* the request does not fit the context's HBM budget */
 #define LF_E_LIMIT (-10)    /* the request exceeds a fixed-size scratch (lf_sample_challenges_noalloc) */
+#define LF_E_TIMEOUT (-11)  /* lf_poll: the job has not finished within the wait */
+#define LF_E_TICKET (-12)   /* lf_poll: no such ticket (never issued, or its result was already taken) */
 
 typedef struct lf_ctx lf_ctx;
 
@@ -93,6 +95,44 @@ int lf_last_profile(lf_ctx* ctx, lf_profile* out);
  * (solution-arm/labinius/crates/pcs/src/challenge.rs:707-737). The proof itself carries only
  * their effect, the fold. */
 int lf_last_challenges(lf_ctx* ctx, uint8_t* out, size_t cap);
+
+/* One proof request. The table is 2^log_vars / 8 bytes, in host memory (copied by the library)
+ * or, with table_on_device = 1, a device pointer on the context's GPU. All buffers stay owned by
+ * the caller and must stay valid until the job's result is reported. */
+typedef struct lf_job {
+  const uint8_t* seed; /* 32 bytes */
+  const uint8_t* q_le; /* 16 bytes, little-endian */
+  uint32_t log_vars;
+  int table_on_device;
+  const void* table;
+  size_t table_bytes;
+  uint8_t* proof; /* at least lf_proof_size(q_le, log_vars) bytes */
+  size_t proof_cap;
+} lf_job;
+
+typedef struct lf_result {
+  int status;       /* LF_OK or the job's LF_E_* code */
+  size_t proof_len; /* bytes written to the job's proof buffer */
+  double queue_ms;  /* submission (or batch start) to the start of the proof */
+  double run_ms;    /* start of the proof to its bytes in the proof buffer */
+} lf_result;
+
+/* Proves n independent jobs (any mix of shapes; each shape's key is built once and cached on
+ * the context) in order on the context's GPU. The next job's host table is copied to the device
+ * on a second stream while the current job is proven. results[i] receives job i's outcome;
+ * the return value is LF_OK if every job succeeded, else the first failing job's code.
+ * The reference proves one table per process (solution/proof_generate/src/main.rs:2050-2090);
+ * this is the batched form of that call. */
+int lf_prove_batch(lf_ctx* ctx, size_t n, const lf_job* jobs, lf_result* results);
+
+/* Serving: lf_submit queues a job (FIFO, one at a time on the context's GPU, on a worker thread
+ * of the context) and returns a ticket; a job whose device footprint exceeds the context's HBM
+ * budget is refused here with LF_E_ADMISSION. lf_poll waits up to wait_ms (0 = just look) for the
+ * ticket: LF_OK with *out filled (the ticket is then retired), LF_E_TIMEOUT while the job is
+ * queued or running, LF_E_TICKET for an unknown ticket. lf_ctx_destroy completes the job in
+ * progress and reports LF_E_INTERNAL for jobs still queued. No counterpart in the reference. */
+int lf_submit(lf_ctx* ctx, const lf_job* job, uint64_t* ticket);
+int lf_poll(lf_ctx* ctx, uint64_t ticket, uint32_t wait_ms, lf_result* out);
 
 /* Diagnostics: n folding challenges sampled on the device from Transcript::new(domain) after
  * absorb_bytes(prefix) (challenge.rs:240-259, 707-737), 40 bytes each as above. */

@@ -8,7 +8,12 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -151,6 +156,10 @@ void pack_f162(const std::vector<f162>& v, uint8_t* out) {
 struct DevBuf {
   void* p = nullptr;
   size_t cap = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
   cudaError_t ensure(size_t n) {
     if (n <= cap) return cudaSuccess;
     if (p) cudaFree(p);
@@ -171,14 +180,17 @@ struct DevBuf {
   }
 };
 
+// The commitment key of one (Q, ring elements per column): built once on the device, kept.
 struct KeyCache {
-  bool valid = false;
   u128 q = 0;
   uint64_t elements = 0;
+  uint64_t last_use = 0;
   ModulusPlan mp;
-  DevBuf key;  // u32 [prime][element][leaf][k][l]: the 4x4 base-multiplication matrix per leaf
-  DevBuf btiles;  // bf16 [prime][third][112 x 128]: Vandermonde limbs of the commitment kernel
+  DevBuf key;     // u32 [prime][element][leaf][k][l]: the 4x4 base-multiplication matrix per leaf
+  DevBuf btiles;  // bf16 [prime][third][64 x 256]: Vandermonde limbs of the commitment kernel
+  size_t bytes() const { return key.cap + btiles.cap; }
 };
+constexpr size_t MAX_KEYS = 12;  // shapes cached per context (log_vars 19..30 fit)
 
 }  // namespace
 
@@ -190,13 +202,36 @@ struct lf_ctx {
   std::mutex mu;
   std::string err;
   lf_profile prof{};
-  KeyCache key;
-  bool consts_for_key = false;
+  std::vector<std::unique_ptr<KeyCache>> keys;  // per shape, least recently used evicted first
+  KeyCache* key = nullptr;                      // the key of the proof in progress
+  u128 consts_q = 0;                            // modulus whose prime constants are on the device
+  uint64_t key_clock = 0;
   DevBuf table, stream_buf, partial, sblk, ehi, elo, lo_planes, rhi, vparts, psi, batch, soa, msg, p0, eqt, row,
       hasher, chal, fold, cvs, cvs_scratch, subtrees, status, phase, scratch_small, wbuf, rbuf;
   uint32_t sign_key[8];
   std::vector<uint8_t> host_fold;
   cudaEvent_t ev[16];
+  // batches: a second table buffer and a copy stream, so the next table uploads during a proof
+  DevBuf table2;
+  cudaStream_t upload_stream = nullptr;
+  cudaEvent_t uploaded[2] = {nullptr, nullptr};
+  // serving: FIFO of submitted jobs, drained by one worker thread
+  struct Queued {
+    uint64_t ticket;
+    lf_job job;
+    std::chrono::steady_clock::time_point submitted;
+  };
+  struct Outcome {
+    bool done = false;
+    lf_result result{};
+  };
+  std::thread worker;
+  std::mutex qmu;
+  std::condition_variable qcv;
+  std::deque<Queued> queue;
+  std::map<uint64_t, Outcome> outcomes;
+  uint64_t next_ticket = 1;
+  bool stopping = false;
 };
 
 namespace {
@@ -239,38 +274,81 @@ void phase_tables(std::vector<double>& re, std::vector<double>& im) {
     }
 }
 
+// Device bytes one proof at this shape may hold beyond the cached keys: the table (when it is
+// copied from the host), the commitment's split partial sums, the partial-sum blocks, the
+// transcript stream, the fold output and the smaller work buffers, plus the transient buffers of
+// a key build. Used for admission against the context's HBM budget.
+size_t proof_footprint(const Shape& sh, bool host_table, int sms) {
+  const size_t key = (size_t)3 * sh.ring_elements * LEAVES * 64;
+  const size_t build = (size_t)3 * sh.ring_elements * (RING_N + 4 * LEAVES) * 4;
+  const size_t partial = (size_t)commit_splits(sh.ring_elements, 3, sms) * 3 * COLUMNS * LEAVES * 16;
+  const size_t blocks = (sh.words / 4096) * (128 * 16 + 16);
+  const size_t stream = STREAM_PREFIX + (size_t)12 * COLUMNS * RING_N + 1024;
+  const size_t fold = (size_t)4 * RING_N * sh.ring_elements;
+  const size_t small = (size_t)16 << 20;
+  return (host_table ? sh.words * 16 : 0) + key + build + partial + blocks + stream + fold + small;
+}
+
+int admit(lf_ctx* ctx, const Shape& sh, bool host_table) {
+  if (ctx->budget == 0) return LF_OK;
+  const size_t need = proof_footprint(sh, host_table, ctx->sms);
+  if (need > ctx->budget)
+    return fail(ctx, LF_E_ADMISSION, "request needs " + std::to_string(need >> 20) + " MiB of device memory, budget " +
+                                         std::to_string(ctx->budget >> 20) + " MiB");
+  return LF_OK;
+}
+
 int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh) {
-  if (ctx->key.valid && ctx->key.q == q && ctx->key.elements == sh.ring_elements) {
-    if (!ctx->consts_for_key) {
-      upload_prime_consts(ctx->key.mp, ctx->stream);
-      ctx->consts_for_key = true;
+  ctx->key = nullptr;
+  for (auto& k : ctx->keys)
+    if (k->q == q && k->elements == sh.ring_elements) ctx->key = k.get();
+  if (!ctx->key) {
+    std::string e;
+    ModulusPlan mp;
+    if (!make_modulus_plan(q, mp, e)) return fail(ctx, LF_E_MODULUS, e);
+    // Evict least recently used shapes: beyond the count limit, or while the cached keys and
+    // this proof would exceed the budget.
+    auto cached = [&]() {
+      size_t b = 0;
+      for (auto& k : ctx->keys) b += k->bytes();
+      return b;
+    };
+    const size_t need = proof_footprint(sh, true, ctx->sms);
+    while (!ctx->keys.empty() &&
+           (ctx->keys.size() >= MAX_KEYS || (ctx->budget && cached() + need > ctx->budget))) {
+      auto oldest = std::min_element(ctx->keys.begin(), ctx->keys.end(),
+                                     [](const std::unique_ptr<KeyCache>& a, const std::unique_ptr<KeyCache>& b) {
+                                       return a->last_use < b->last_use;
+                                     });
+      ctx->keys.erase(oldest);
     }
-    return LF_OK;
+    std::unique_ptr<KeyCache> kc(new KeyCache());
+    const uint64_t E = sh.ring_elements;
+    DevBuf ared, leaf;
+    CK(ared.ensure((size_t)mp.nprimes * E * RING_N * 4));
+    CK(leaf.ensure((size_t)mp.nprimes * E * 4 * LEAVES * 4));
+    CK(kc->key.ensure((size_t)mp.nprimes * E * LEAVES * 16 * 4));
+    CK(kc->btiles.ensure(mp.btiles.size() * 2));
+    CK(cudaMemcpyAsync(kc->btiles.p, mp.btiles.data(), mp.btiles.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
+    upload_prime_consts(mp, ctx->stream);
+    ctx->consts_q = q;
+    launch_matrix_expand(mp, E, ared.as<uint32_t>(), ctx->stream);
+    launch_key_transform(mp, E, ared.as<uint32_t>(), leaf.as<uint32_t>(), kc->key.as<uint32_t>(), ctx->stream);
+    CKL("key build");
+    CK(cudaStreamSynchronize(ctx->stream));
+    ared.release();
+    leaf.release();
+    kc->mp = mp;
+    kc->q = q;
+    kc->elements = E;
+    ctx->keys.push_back(std::move(kc));
+    ctx->key = ctx->keys.back().get();
   }
-  std::string e;
-  ModulusPlan mp;
-  if (!make_modulus_plan(q, mp, e)) return fail(ctx, LF_E_MODULUS, e);
-  ctx->key.valid = false;
-  uint64_t E = sh.ring_elements;
-  DevBuf ared, leaf;
-  CK(ared.ensure((size_t)mp.nprimes * E * RING_N * 4));
-  CK(leaf.ensure((size_t)mp.nprimes * E * 4 * LEAVES * 4));
-  CK(ctx->key.key.ensure((size_t)mp.nprimes * E * LEAVES * 16 * 4));
-  CK(ctx->key.btiles.ensure(mp.btiles.size() * 2));
-  CK(cudaMemcpyAsync(ctx->key.btiles.p, mp.btiles.data(), mp.btiles.size() * 2, cudaMemcpyHostToDevice,
-                     ctx->stream));
-  upload_prime_consts(mp, ctx->stream);
-  launch_matrix_expand(mp, E, ared.as<uint32_t>(), ctx->stream);
-  launch_key_transform(mp, E, ared.as<uint32_t>(), leaf.as<uint32_t>(), ctx->key.key.as<uint32_t>(), ctx->stream);
-  CKL("key build");
-  CK(cudaStreamSynchronize(ctx->stream));
-  ared.release();
-  leaf.release();
-  ctx->key.mp = mp;
-  ctx->key.q = q;
-  ctx->key.elements = E;
-  ctx->key.valid = true;
-  ctx->consts_for_key = true;
+  ctx->key->last_use = ++ctx->key_clock;
+  if (ctx->consts_q != q) {
+    upload_prime_consts(ctx->key->mp, ctx->stream);
+    ctx->consts_q = q;
+  }
   return LF_OK;
 }
 
@@ -305,13 +383,13 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   cudaEventRecord(ctx->ev[2], st);
 
   // ---- commitment (K1 + K2), written after the 112 transcript prefix bytes of the stream ----
-  const int splits = commit_splits(sh.ring_elements, ctx->key.mp.nprimes, ctx->sms);
-  const ModulusPlan& mp = ctx->key.mp;
+  const int splits = commit_splits(sh.ring_elements, ctx->key->mp.nprimes, ctx->sms);
+  const ModulusPlan& mp = ctx->key->mp;
   CK(ctx->partial.ensure((size_t)splits * mp.nprimes * COLUMNS * LEAVES * 4 * 4));
   CK(ctx->stream_buf.ensure(STREAM_PREFIX + commit_bytes + 1024));
   CK(ctx->status.ensure(16));
   CK(cudaMemsetAsync(ctx->status.p, 0, 16, st));
-  launch_commit(mp, sh, table, ctx->key.key.as<uint32_t>(), ctx->key.btiles.as<uint16_t>(),
+  launch_commit(mp, sh, table, ctx->key->key.as<uint32_t>(), ctx->key->btiles.as<uint16_t>(),
                 ctx->partial.as<uint32_t>(), splits, ctx->status.as<int>(), st);
   cudaEventRecord(ctx->ev[11], st);
   launch_commit_finish(mp, sh, ctx->partial.as<uint32_t>(), splits, ctx->stream_buf.as<uint8_t>() + STREAM_PREFIX, st);
@@ -581,6 +659,72 @@ int check_request(lf_ctx* ctx, const uint8_t* q_le, uint32_t log_vars, uint8_t* 
   return LF_OK;
 }
 
+// Shape, modulus, buffer and budget checks of one job, before any device work.
+int check_job(lf_ctx* ctx, const lf_job& j, u128& q, Shape& sh) {
+  if (!j.seed || !j.table || !j.q_le) return fail(ctx, LF_E_ARGS, "null argument");
+  size_t len = 0;
+  int rc = check_request(ctx, j.q_le, j.log_vars, j.proof, j.proof_cap, &len, q, sh);
+  if (rc) return rc;
+  if (!j.table_on_device && j.table_bytes != sh.words * 16)
+    return fail(ctx, LF_E_TABLE_LEN, "witness table has the wrong length");
+  return admit(ctx, sh, !j.table_on_device);
+}
+
+using clk = std::chrono::steady_clock;
+double ms_between(clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); }
+
+// One job with the context lock held; table_dev is the job's table already on the device.
+int run_job(lf_ctx* ctx, const lf_job& j, const uint4* table_dev, size_t* proof_len) {
+  u128 q;
+  Shape sh;
+  int rc = check_job(ctx, j, q, sh);
+  if (rc) return rc;
+  cudaSetDevice(ctx->device);
+  ctx->prof = lf_profile{};
+  cudaEventRecord(ctx->ev[0], ctx->stream);
+  return prove_device(ctx, j.seed, q, sh, table_dev, j.proof, proof_len);
+}
+
+void serve_loop(lf_ctx* ctx) {
+  for (;;) {
+    lf_ctx::Queued item;
+    {
+      std::unique_lock<std::mutex> lk(ctx->qmu);
+      ctx->qcv.wait(lk, [&] { return ctx->stopping || !ctx->queue.empty(); });
+      if (ctx->queue.empty()) return;
+      item = ctx->queue.front();
+      ctx->queue.pop_front();
+    }
+    lf_result r{};
+    const auto start = clk::now();
+    r.queue_ms = ms_between(item.submitted, start);
+    {
+      std::lock_guard<std::mutex> g(ctx->mu);
+      const lf_job& j = item.job;
+      const uint4* table = reinterpret_cast<const uint4*>(j.table);
+      r.status = LF_OK;
+      if (!j.table_on_device) {
+        Shape sh;
+        if (sh.set(j.log_vars) && j.table_bytes == sh.words * 16) {
+          cudaSetDevice(ctx->device);
+          if (ctx->table.ensure(j.table_bytes) != cudaSuccess ||
+              cudaMemcpyAsync(ctx->table.p, j.table, j.table_bytes, cudaMemcpyHostToDevice, ctx->stream) !=
+                  cudaSuccess)
+            r.status = fail(ctx, LF_E_CUDA, "table upload failed");
+          table = ctx->table.as<uint4>();
+        }
+      }
+      if (r.status == LF_OK) r.status = run_job(ctx, j, table, &r.proof_len);
+    }
+    r.run_ms = ms_between(start, clk::now());
+    {
+      std::lock_guard<std::mutex> lk(ctx->qmu);
+      ctx->outcomes[item.ticket] = lf_ctx::Outcome{true, r};
+    }
+    ctx->qcv.notify_all();
+  }
+}
+
 // Table PRG (verifier/table_writer/src/main.rs:14-22): keyed BLAKE3 XOF of the context string.
 __global__ void k_table_prg(bk::Pending root, uint64_t blocks, uint4* out) {
   uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -711,14 +855,31 @@ void* lf_ctx_stream(lf_ctx* ctx) { return ctx ? static_cast<void*>(ctx->stream) 
 
 void lf_ctx_destroy(lf_ctx* ctx) {
   if (!ctx) return;
+  {
+    std::lock_guard<std::mutex> lk(ctx->qmu);
+    for (auto& item : ctx->queue) {
+      lf_result r{};
+      r.status = LF_E_INTERNAL;
+      ctx->outcomes[item.ticket] = lf_ctx::Outcome{true, r};
+    }
+    ctx->queue.clear();
+    ctx->stopping = true;
+  }
+  ctx->qcv.notify_all();
+  if (ctx->worker.joinable()) ctx->worker.join();
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   DevBuf* bufs[] = {&ctx->table, &ctx->stream_buf, &ctx->partial, &ctx->sblk, &ctx->ehi, &ctx->elo, &ctx->lo_planes,
                     &ctx->rhi, &ctx->vparts, &ctx->psi, &ctx->batch, &ctx->soa, &ctx->msg, &ctx->p0, &ctx->eqt,
                     &ctx->row, &ctx->hasher, &ctx->chal, &ctx->fold, &ctx->cvs, &ctx->cvs_scratch, &ctx->subtrees,
-                    &ctx->status, &ctx->phase, &ctx->scratch_small, &ctx->wbuf, &ctx->rbuf, &ctx->key.key, &ctx->key.btiles};
+                    &ctx->status, &ctx->phase, &ctx->scratch_small, &ctx->wbuf, &ctx->rbuf};
+  ctx->keys.clear();
   for (DevBuf* b : bufs) b->release();
+  ctx->table2.release();
   for (auto& ev : ctx->ev) cudaEventDestroy(ev);
+  for (auto& ev : ctx->uploaded)
+    if (ev) cudaEventDestroy(ev);
+  if (ctx->upload_stream) cudaStreamDestroy(ctx->upload_stream);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -757,6 +918,7 @@ int lf_prove_device(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16],
   Shape sh;
   int rc = check_request(ctx, q_le, log_vars, proof, proof_cap, proof_len, q, sh);
   if (rc) return rc;
+  if ((rc = admit(ctx, sh, false))) return rc;
   cudaSetDevice(ctx->device);
   auto t0 = std::chrono::steady_clock::now();
   ctx->prof = lf_profile{};
@@ -775,6 +937,7 @@ int lf_prove(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32
   int rc = check_request(ctx, q_le, log_vars, proof, proof_cap, proof_len, q, sh);
   if (rc) return rc;
   if (table_bytes != sh.words * 16) return fail(ctx, LF_E_TABLE_LEN, "witness table has the wrong length");
+  if ((rc = admit(ctx, sh, true))) return rc;
   cudaSetDevice(ctx->device);
   auto t0 = std::chrono::steady_clock::now();
   ctx->prof = lf_profile{};
@@ -862,6 +1025,95 @@ int lf_sample_challenges_traced(lf_ctx* ctx, const char* domain, const uint8_t* 
   return LF_OK;
 }
 
+int lf_prove_batch(lf_ctx* ctx, size_t n, const lf_job* jobs, lf_result* results) {
+  if (!ctx || (n && (!jobs || !results))) return LF_E_ARGS;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaSetDevice(ctx->device);
+  if (!ctx->upload_stream) {
+    CK(cudaStreamCreateWithFlags(&ctx->upload_stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ctx->uploaded[0], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->uploaded[1], cudaEventDisableTiming));
+  }
+  const auto t_batch = clk::now();
+  DevBuf* tb[2] = {&ctx->table, &ctx->table2};
+  std::vector<int> pre(n, LF_OK);  // per-job check before any device work
+  for (size_t i = 0; i < n; ++i) {
+    u128 q;
+    Shape sh;
+    pre[i] = check_job(ctx, jobs[i], q, sh);
+  }
+  // Copy a host table into buffer b on the copy stream (job i), marking its completion.
+  auto upload = [&](size_t i, int b) -> int {
+    const lf_job& j = jobs[i];
+    if (pre[i] != LF_OK || j.table_on_device) return LF_OK;
+    CK(tb[b]->ensure(j.table_bytes));
+    CK(cudaMemcpyAsync(tb[b]->p, j.table, j.table_bytes, cudaMemcpyHostToDevice, ctx->upload_stream));
+    CK(cudaEventRecord(ctx->uploaded[b], ctx->upload_stream));
+    return LF_OK;
+  };
+  int first = LF_OK;
+  int up = n ? upload(0, 0) : LF_OK;
+  for (size_t i = 0; i < n; ++i) {
+    lf_result& r = results[i];
+    r = lf_result{};
+    const auto start = clk::now();
+    r.queue_ms = ms_between(t_batch, start);
+    const lf_job& j = jobs[i];
+    const int b = (int)(i & 1);
+    r.status = pre[i] != LF_OK ? pre[i] : up;
+    const uint4* table = reinterpret_cast<const uint4*>(j.table);
+    if (r.status == LF_OK && !j.table_on_device) {
+      table = tb[b]->as<uint4>();
+      if (cudaStreamWaitEvent(ctx->stream, ctx->uploaded[b], 0) != cudaSuccess)
+        r.status = fail(ctx, LF_E_CUDA, "stream wait failed");
+    }
+    // The other buffer's job finished (prove_device ends in a stream synchronisation): fill it.
+    up = i + 1 < n ? upload(i + 1, b ^ 1) : LF_OK;
+    if (r.status == LF_OK) r.status = run_job(ctx, j, table, &r.proof_len);
+    r.run_ms = ms_between(start, clk::now());
+    if (r.status != LF_OK && first == LF_OK) first = r.status;
+  }
+  cudaStreamSynchronize(ctx->upload_stream);
+  return first;
+}
+
+int lf_submit(lf_ctx* ctx, const lf_job* job, uint64_t* ticket) {
+  if (!ctx || !job || !ticket) return LF_E_ARGS;
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    u128 q;
+    Shape sh;
+    int rc = check_job(ctx, *job, q, sh);
+    if (rc) return rc;
+  }
+  std::lock_guard<std::mutex> lk(ctx->qmu);
+  if (ctx->stopping) return LF_E_ARGS;
+  *ticket = ctx->next_ticket++;
+  ctx->outcomes[*ticket] = lf_ctx::Outcome{};
+  ctx->queue.push_back(lf_ctx::Queued{*ticket, *job, clk::now()});
+  if (!ctx->worker.joinable()) ctx->worker = std::thread(serve_loop, ctx);
+  ctx->qcv.notify_all();
+  return LF_OK;
+}
+
+int lf_poll(lf_ctx* ctx, uint64_t ticket, uint32_t wait_ms, lf_result* out) {
+  if (!ctx || !out) return LF_E_ARGS;
+  std::unique_lock<std::mutex> lk(ctx->qmu);
+  auto it = ctx->outcomes.find(ticket);
+  if (it == ctx->outcomes.end()) return LF_E_TICKET;
+  if (!it->second.done && wait_ms)
+    ctx->qcv.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] {
+      auto f = ctx->outcomes.find(ticket);
+      return f == ctx->outcomes.end() || f->second.done;
+    });
+  it = ctx->outcomes.find(ticket);
+  if (it == ctx->outcomes.end()) return LF_E_TICKET;
+  if (!it->second.done) return LF_E_TIMEOUT;
+  *out = it->second.result;
+  ctx->outcomes.erase(it);
+  return LF_OK;
+}
+
 int lf_sample_challenges_noalloc(int device, const char* domain, const uint8_t* prefix, size_t prefix_len, uint32_t n,
                                  uint8_t* out, void* stream) {
   if (!domain || (!prefix && prefix_len) || !out || n == 0 || device < 0 || device >= NOALLOC_MAX_DEVICES)
@@ -896,6 +1148,8 @@ const char* lf_strerror(int code) {
     case LF_E_CUDA: return "CUDA error";
     case LF_E_INTERNAL: return "internal check failed";
     case LF_E_ADMISSION: return "request exceeds the HBM budget";
+    case LF_E_TIMEOUT: return "the job has not finished yet";
+    case LF_E_TICKET: return "no such ticket";
     case LF_E_LIMIT: return "request exceeds the fixed scratch of lf_sample_challenges_noalloc (4096 challenges)";
     default: return "unknown error";
   }

@@ -17,13 +17,15 @@ LF_OK = 0
 ERRORS = {
     -1: "LF_E_ARGS", -2: "LF_E_SHAPE", -3: "LF_E_MODULUS", -4: "LF_E_TABLE_LEN", -5: "LF_E_CAP",
     -6: "LF_E_OOM", -7: "LF_E_CUDA", -8: "LF_E_INTERNAL", -9: "LF_E_ADMISSION", -10: "LF_E_LIMIT",
+    -11: "LF_E_TIMEOUT", -12: "LF_E_TICKET",
 }
+LF_E_TIMEOUT = -11
 NOALLOC_MAX_CHALLENGES = 4096
 EXPORTS = [
     "lf_ctx_create", "lf_ctx_destroy", "lf_ctx_stream", "lf_proof_size", "lf_accept_modulus", "lf_key_prepare", "lf_prove",
     "lf_prove_device", "lf_write_table_device", "lf_device_alloc", "lf_device_free", "lf_memcpy_h2d",
     "lf_last_profile", "lf_strerror", "lf_last_error", "lf_last_challenges",
-    "lf_sample_challenges", "lf_sample_challenges_noalloc",
+    "lf_sample_challenges", "lf_sample_challenges_noalloc", "lf_prove_batch", "lf_submit", "lf_poll",
 ]
 
 
@@ -35,6 +37,17 @@ class LfError(RuntimeError):
 
 class Config(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("hbm_budget", ctypes.c_size_t)]
+
+
+class Job(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_char_p), ("q_le", ctypes.c_char_p), ("log_vars", ctypes.c_uint32),
+                ("table_on_device", ctypes.c_int), ("table", ctypes.c_void_p), ("table_bytes", ctypes.c_size_t),
+                ("proof", ctypes.POINTER(ctypes.c_uint8)), ("proof_cap", ctypes.c_size_t)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("proof_len", ctypes.c_size_t), ("queue_ms", ctypes.c_double),
+                ("run_ms", ctypes.c_double)]
 
 
 class Profile(ctypes.Structure):
@@ -82,6 +95,9 @@ def load(path=LIB_PATH):
     lib.lf_last_error.restype = ctypes.c_char_p
     lib.lf_last_challenges.argtypes = [p, u8p, sz]
     lib.lf_sample_challenges.argtypes = [p, ctypes.c_char_p, ctypes.c_char_p, sz, ctypes.c_uint32, u8p]
+    lib.lf_prove_batch.argtypes = [p, sz, ctypes.POINTER(Job), ctypes.POINTER(Result)]
+    lib.lf_submit.argtypes = [p, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_uint64)]
+    lib.lf_poll.argtypes = [p, ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(Result)]
     lib.lf_sample_challenges_noalloc.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p, sz, ctypes.c_uint32,
                                                  u8p, p]
     _lib = lib
@@ -168,6 +184,46 @@ class Prover:
 
     def key_prepare(self, log_vars, q=BASELINE_Q):
         self._check(self.lib.lf_key_prepare(self.ctx, q_bytes(q), log_vars))
+
+    def make_job(self, seed, table, log_vars, q=BASELINE_Q, on_device=False, nbytes=None):
+        """A job and the buffers it points to (kept alive on the returned object). `table` is bytes /
+        a ctypes buffer / an int host address (host tables), or an int device pointer with
+        on_device=True."""
+        cap = proof_size(q, log_vars)
+        keep = {"seed": bytes(seed), "q": q_bytes(q), "proof": (ctypes.c_uint8 * cap)()}
+        if on_device:
+            addr, n = int(table), 0
+        elif isinstance(table, int):
+            addr, n = table, nbytes
+        else:
+            buf = table if isinstance(table, ctypes.Array) else (ctypes.c_uint8 * len(table)).from_buffer_copy(table)
+            keep["table"] = buf
+            addr, n = ctypes.addressof(buf), ctypes.sizeof(buf)
+        job = Job(keep["seed"], keep["q"], log_vars, 1 if on_device else 0, addr, n, keep["proof"], cap)
+        job._keep = keep
+        return job
+
+    @staticmethod
+    def job_proof(job, result):
+        return ctypes.string_at(job._keep["proof"], result.proof_len)
+
+    def prove_batch(self, jobs):
+        """Results of lf_prove_batch, one per job (status checked by the caller)."""
+        arr = (Job * len(jobs))(*jobs)
+        res = (Result * len(jobs))()
+        self.lib.lf_prove_batch(self.ctx, len(jobs), arr, res)
+        return list(res)
+
+    def submit(self, job):
+        t = ctypes.c_uint64()
+        self._check(self.lib.lf_submit(self.ctx, ctypes.byref(job), ctypes.byref(t)))
+        return t.value
+
+    def poll(self, ticket, wait_ms=0):
+        """(code, Result): LF_OK with the result, LF_E_TIMEOUT while pending."""
+        r = Result()
+        rc = self.lib.lf_poll(self.ctx, ticket, wait_ms, ctypes.byref(r))
+        return rc, r
 
     def stream(self):
         """The context's cudaStream_t as an int (every call of this prover runs on it)."""
