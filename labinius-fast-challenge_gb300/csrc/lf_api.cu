@@ -458,14 +458,14 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   CK(ctx->rhi.ensure(64 * 16));
   CK(ctx->elo.ensure(4096 * 16));
   CK(ctx->ehi.ensure(nblocks * 16));
-  CK(ctx->lo_planes.ensure(4096 / 32 * 128 * 4));
+  CK(ctx->lo_planes.ensure(4096 * 256));  // E_lo expanded to bf16 rows (32 tiles of 128)
   CK(ctx->sblk.ensure(nblocks * 128 * 16));
   CK(ctx->vparts.ensure(256 * 8));
   CK(cudaMemcpyAsync(ctx->rhi.p, hi.data(), 16 * hi.size(), cudaMemcpyHostToDevice, st));
   launch_eq_b128(ctx->rhi.as<b128>() + HB, LB, ctx->elo.as<b128>(), st);
   launch_eq_b128(ctx->rhi.as<b128>(), HB, ctx->ehi.as<b128>(), st);
-  launch_planes_b128(ctx->elo.as<b128>(), 4096, ctx->lo_planes.as<uint32_t>(), st);
-  launch_sblock(table, nblocks, ctx->lo_planes.as<uint32_t>(), ctx->sblk.as<uint8_t>(), st);
+  launch_expand_rows(ctx->elo.as<b128>(), 4096, ctx->lo_planes.as<uint8_t>(), st);
+  launch_sblock(table, nblocks, ctx->lo_planes.as<uint8_t>(), ctx->sblk.as<uint8_t>(), ctx->status.as<int>(), st);
   CK(cudaMemsetAsync(ctx->vparts.p, 0, 256 * 8, st));
   launch_partials_combine(ctx->ehi.as<b128>(), ctx->sblk.as<uint8_t>(), (int)nblocks,
                           ctx->vparts.as<unsigned long long>(), st);
@@ -615,6 +615,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   if (status[0] == 1) return fail(ctx, LF_E_INTERNAL, "challenge sampling exceeded its attempt bound");
   if (status[0] == 2) return fail(ctx, LF_E_INTERNAL, "a fold coefficient does not fit the wire codec");
   if (status[0] == 3) return fail(ctx, LF_E_INTERNAL, "the commitment kernel's pipeline timed out");
+  if (status[0] == 4) return fail(ctx, LF_E_INTERNAL, "the partial-sum kernel's pipeline timed out");
   if (status[0] != 0) return fail(ctx, LF_E_INTERNAL, "a device-side check failed");
 
   // ---- encode (main.rs:98-124) ----

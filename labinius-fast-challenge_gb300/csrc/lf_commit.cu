@@ -332,23 +332,6 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
 // (about a second); a timeout sets *status = 3 and the block skips its remaining work but keeps
 // the barrier count, so every thread drains.
 // ------------------------------------------------------------------------------------------------
-// Word -> one row of an A slot. u32 o = 16 w + t of the row holds bits 32 w + t (low bf16) and
-// 32 w + t + 16 (high bf16) of the word as 2.0 (0x4000) or 0; the B tiles use the same K order.
-__device__ __forceinline__ void tc_write_row(uint8_t* slot, int c, uint4 v) {
-  const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    const uint32_t x = xs[q >> 2];
-    uint32_t u[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int t = (q & 3) * 4 + i;
-      u[i] = t < 15 ? (x << (14 - t)) & 0x40004000u : (x >> 1) & 0x40004000u;
-    }
-    *reinterpret_cast<uint4*>(slot + (c >> 3) * 2048 + q * 128 + (c & 7) * 16) = make_uint4(u[0], u[1], u[2], u[3]);
-  }
-}
-
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_commit_tc(const uint4* __restrict__ table, const uint32_t* __restrict__ key, const uint4* __restrict__ btiles,
                 uint32_t* __restrict__ partial, int rl, int elements, int per_split, int nprimes, int* status) {
@@ -420,7 +403,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     };
     auto store_pre = [&](int e, uint4 u) {  // ... into the A slots / the key ring
       if (expander) {
-        tc_write_row(sA + (tid >> 7) * TC_A_BYTES, tid & (TC_COLS - 1), u);
+        tc::write_row(sA + (tid >> 7) * TC_A_BYTES, tid & (TC_COLS - 1), u);
       } else if (keyer) {
         int4 v;  // centred into (-p/2, p/2]
         v.x = (int)u.x > half ? (int)u.x - (int)p : (int)u.x;
@@ -536,7 +519,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
 // B tiles of K1 on the tensor cores, per (prime, third): row 10 g + i = leaf 9 g + i of the third
 // (rows 10 g + 9 and 60..63 zero); K position kappa < 128 carries the low limb of bit j(kappa),
-// kappa >= 128 the high limb of bit j(kappa - 128), j in the K order of tc_write_row; bf16 in
+// kappa >= 128 the high limb of bit j(kappa - 128), j in the K order of tc::write_row; bf16 in
 // the no-swizzle K-major core-matrix layout (8 x 16 B cores, K-adjacent 128 B apart, 8-row
 // groups 4096 B apart).
 static void fill_btiles(const PrimePlan& pl, const PrimeConst& c, uint16_t* out /* 3 x TC_B_BYTES/2 */) {
@@ -551,9 +534,8 @@ static void fill_btiles(const PrimePlan& pl, const PrimeConst& c, uint16_t* out 
         pw[0] = 1;
         for (int j = 1; j < 128; ++j) pw[j] = pw[j - 1] * c.leaf_root[s] % p;
         for (int kappa = 0; kappa < TC_K; ++kappa) {
-          const int limb = kappa >> 7, kk = kappa & 127;
-          const int o = kk >> 1, h = kk & 1, w = o >> 4, t = o & 15;
-          const uint64_t V = pw[32 * w + t + 16 * h];
+          const int limb = kappa >> 7;
+          const uint64_t V = pw[tc::row_bit(kappa & 127)];
           const float f = limb == 0 ? (float)(V & 255) * 0.5f : (float)(V >> 8) * 128.0f;
           uint32_t u;
           memcpy(&u, &f, 4);

@@ -98,8 +98,9 @@ struct Challenge {
 // ---- launch wrappers (lf_switch.cu) ----
 void launch_eq_b128(const b128* r, int n, b128* out, cudaStream_t s);
 void launch_eq_table_f162(const f162* ps, int n, f162* out, cudaStream_t s);
-void launch_planes_b128(const b128* x, uint64_t n, uint32_t* planes, cudaStream_t s);
-void launch_sblock(const uint4* table, uint64_t nblocks, const uint32_t* lo_planes, uint8_t* sblk, cudaStream_t s);
+void launch_expand_rows(const b128* x, int n, uint8_t* rows, cudaStream_t s);
+void launch_sblock(const uint4* table, uint64_t nblocks, const uint8_t* elo_rows, uint8_t* sblk, int* status,
+                   cudaStream_t s);
 void launch_partials_combine(const b128* ehi, const uint8_t* sblk, int nblocks, unsigned long long* v, cudaStream_t s);
 void launch_psi_tables(const f162* batch, f162* tab, cudaStream_t s);
 void launch_rblock_level(const b128* in, uint64_t nout, b128 rho, b128* out, cudaStream_t s);

@@ -13,6 +13,7 @@
 #include <cstdio>
 
 #include "lf_internal.h"
+#include "lf_tc.cuh"
 
 namespace lf {
 
@@ -45,81 +46,130 @@ __global__ void k_eq_table_f162(const f162* __restrict__ ps, int n, f162* __rest
   out[j] = v;
 }
 
-// Bit planes of B128 values, word-major: planes[w * 128 + b] holds bit b of entries 32w..32w+31.
-__global__ void k_planes_b128(const b128* __restrict__ x, uint64_t n, uint32_t* __restrict__ planes) {
-  uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (w * 32 >= n) return;
-  b128 v = x[w * 32 + lane];
-  uint32_t keep[4] = {0, 0, 0, 0};
-#pragma unroll
-  for (int b = 0; b < 128; ++b) {
-    uint32_t bit = b < 64 ? (uint32_t)(v.lo >> b) & 1 : (uint32_t)(v.hi >> (b - 64)) & 1;
-    uint32_t m = __ballot_sync(0xffffffffu, bit);
-    if (lane == (b & 31)) keep[b >> 5] = m;
-  }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) planes[w * 128 + 32 * i + lane] = keep[i];
+// ---------------------------------------------------------------------------------------------
+// S blocks on the tensor cores: sblk[h][c] (16 bytes, bit b) = parity of
+//   count_h[c][b] = sum_{j < 4096} bit_c(pi0[4096 h + j]) bit_b(E_lo[j]),
+// an exact integer in f32. Both operands are the words expanded to bf16 rows
+// (tc::write_row), read MN-major: row = entry j (K), 128 bit positions along M (table word) or
+// N (E_lo). A block takes two h; the 4096 entries run in 32 k-tiles of 128 through two shared
+// memory stages, so the expansion of tile t + 1 overlaps the MMAs of tile t. E_lo's rows are
+// expanded once per proof (k_expand_rows) and streamed with cp.async. D for both h sits in TMEM
+// (2 x 128 columns). Set bits are bf16 2.0 in both operands, so D = 4 x count (<= 16384, exact);
+// the count's parity is bit 2 of the f32 mantissa after adding 2^23. Waits are bounded; a
+// timeout sets *status = 4.
+// ---------------------------------------------------------------------------------------------
+constexpr int SBT_THREADS = 256;
+constexpr int SBT_TILE = 128 * 128 * 2;                       // 128 entries x 128 bits, bf16
+constexpr int SBT_SMEM = 2 * SBT_TILE + 2 * 2 * SBT_TILE + 64;  // [B0][B1][A0: 2 h][A1: 2 h][barriers]
+constexpr long long SBT_WAIT_CYCLES = 2000000000LL;
+
+__global__ void k_expand_rows(const uint4* __restrict__ x, int n, uint8_t* __restrict__ rows) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) tc::write_row(rows + (size_t)(j >> 7) * SBT_TILE, j & 127, x[j]);
 }
 
-// ---------------------------------------------------------------------------------------------
-// S blocks: sblk[h][c] (16 bytes, bit b) = parity sum_jl bit_c(pi0[h, jl]) bit_b(E_lo[jl]).
-// One block of 256 threads per h; 4096 words = 128 plane words of 32 entries.
-// ---------------------------------------------------------------------------------------------
-constexpr int SB_W = 128;  // plane words per block (4096 entries)
-
-__global__ void __launch_bounds__(256, 1) k_sblock(const uint4* __restrict__ table, const uint32_t* __restrict__ lo_planes,
-                                                    uint8_t* __restrict__ sblk) {
-  extern __shared__ __align__(16) uint32_t smem[];
-  uint32_t* sP = smem;                 // [SB_W][128]
-  uint32_t* sL = smem + SB_W * 128;    // [SB_W][128]
-  const int h = blockIdx.x;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  {
-    const uint4* src = reinterpret_cast<const uint4*>(lo_planes);
-    uint4* dst = reinterpret_cast<uint4*>(sL);
-    for (int i = threadIdx.x; i < SB_W * 32; i += 256) dst[i] = src[i];
+__global__ void __launch_bounds__(SBT_THREADS, 1)
+    k_sblock_tc(const uint4* __restrict__ table, uint64_t nblocks, const uint4* __restrict__ elo_rows,
+                uint8_t* __restrict__ sblk, int* status) {
+  extern __shared__ __align__(1024) uint8_t sbs[];
+  uint8_t* sB = sbs;                  // stage s at sB + s * SBT_TILE (E_lo rows of the k-tile)
+  uint8_t* sA = sbs + 2 * SBT_TILE;   // stage s, block hb at sA + (2 s + hb) * SBT_TILE
+  uint64_t* done = reinterpret_cast<uint64_t*>(sbs + 6 * SBT_TILE);  // [2] MMAs of a stage done
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 2);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint64_t h0 = 2 * (uint64_t)blockIdx.x;
+  const int hb = tid >> 7, j = tid & 127;
+  const bool live = h0 + hb < nblocks;
+  const uint4* src = table + (h0 + hb) * 4096 + j;  // entry 128 t + j of block h0 + hb
+  if (tid == 0) {
+    *abort_flag = 0;
+    tc::mbar_init(&done[0], 1);
+    tc::mbar_init(&done[1], 1);
+    tc::mbar_init_fence();
   }
-  const uint4* blk = table + (size_t)h * SB_W * 32;
-  for (int w = warp; w < SB_W; w += 8) {
-    uint4 v = blk[w * 32 + lane];
-    uint32_t keep[4] = {0, 0, 0, 0};
-#pragma unroll
-    for (int b = 0; b < 128; ++b) {
-      uint32_t word = b < 32 ? v.x : b < 64 ? v.y : b < 96 ? v.z : v.w;
-      uint32_t m = __ballot_sync(0xffffffffu, (word >> (b & 31)) & 1);
-      if (lane == (b & 31)) keep[b >> 5] = m;
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) sP[w * 128 + 32 * i + lane] = keep[i];
-  }
+  if (warp == 0) tc::tmem_alloc(tslot, 256);
+  tc::fence_before_sync();
   __syncthreads();
-  const int cb = threadIdx.x >> 4, bb = threadIdx.x & 15;
-  uint32_t acc[8][8];
+  tc::fence_after_sync();
+  const uint32_t tbase = *tslot;
+  const uint32_t idesc = tc::idesc_bf16_f32(128, 128) | (1u << 15) | (1u << 16);  // A and B MN-major
+  auto wait_all = [&](uint64_t* bar, uint32_t parity) {
+    const bool r = tc::mbar_wait(bar, parity, abort_flag, SBT_WAIT_CYCLES);
+    return __all_sync(0xffffffffu, r);
+  };
+
+  uint4 w = live ? src[0] : make_uint4(0, 0, 0, 0);
+  int last = -1;  // k-tile of the issuer's last commit
+  for (int t = 0; t < 32; ++t) {
+    const int s = t & 1;
+    if (t >= 2 && !wait_all(&done[s], ((t >> 1) - 1) & 1)) {
+      *abort_flag = 1;
+      atomicExch(status, 4);
+    }
+    const bool go = !*abort_flag;
+    if (go) {
+      const uint4* bsrc = elo_rows + (size_t)t * (SBT_TILE / 16);
+      for (int i = tid; i < SBT_TILE / 16; i += SBT_THREADS) tc::cp_async16(sB + s * SBT_TILE + 16 * i, bsrc + i);
+      tc::write_row(sA + (2 * s + hb) * SBT_TILE, j, w);
+    }
+    if (t + 1 < 32) w = live ? src[(t + 1) * 128] : make_uint4(0, 0, 0, 0);
+    tc::cp_async_wait_all();
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0 && go && !*abort_flag) {
+      const uint32_t b0 = tc::smem_u32(sB + s * SBT_TILE);
 #pragma unroll
-  for (int i = 0; i < 8; ++i)
+      for (int h2 = 0; h2 < 2; ++h2) {
+        const uint32_t a0 = tc::smem_u32(sA + (2 * s + h2) * SBT_TILE);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = 0;
-#pragma unroll 2
-  for (int w = 0; w < SB_W; ++w) {
-    const uint4* pp = reinterpret_cast<const uint4*>(sP + w * 128 + 8 * cb);
-    const uint4* lp = reinterpret_cast<const uint4*>(sL + w * 128 + 8 * bb);
-    uint4 p0 = pp[0], p1 = pp[1], l0 = lp[0], l1 = lp[1];
-    uint32_t pv[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
-    uint32_t lv[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-      for (int j = 0; j < 8; ++j) acc[i][j] ^= pv[i] & lv[j];
+        for (int kk = 0; kk < 8; ++kk)
+          tc::mma_bf16(tbase + 128 * h2, tc::sdesc(a0 + kk * 4096, 2048, 128), tc::sdesc(b0 + kk * 4096, 2048, 128),
+                       idesc, (t | kk) ? 1u : 0u);
+      }
+      tc::mma_commit(&done[s]);
+      last = t;
+    }
   }
-  uint8_t* out = sblk + (size_t)h * 128 * 16;
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    uint32_t byte = 0;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) byte |= (__popc(acc[i][j]) & 1u) << j;
-    out[(8 * cb + i) * 16 + bb] = (uint8_t)byte;
+  // Drain: the issuer's last commit covers every MMA it issued (also after an abort).
+  if (tid == 0 && last >= 0) {
+    const long long t0 = clock64();
+    while (!tc::mbar_try_wait(&done[last & 1], (last >> 1) & 1) && clock64() - t0 < SBT_WAIT_CYCLES) {
+    }
   }
+  // The last commit (k-tile 31, stage 1, its 16th) covers every MMA of the block.
+  bool ok = !*abort_flag && wait_all(&done[1], 1);
+  ok = __syncthreads_and(ok);
+  tc::fence_after_sync();
+  if (ok) {
+    const int h2 = warp >> 2, qd = warp & 3;
+    if (h0 + h2 < nblocks) {
+      const int m = 32 * qd + lane, c = tc::row_bit(m);
+      uint32_t out[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int n0 = 0; n0 < 128; n0 += 16) {
+        uint32_t v[16];
+        tc::tmem_ld_x16(tbase + ((uint32_t)(32 * qd) << 16) + 128 * h2 + n0, v);
+        tc::tmem_wait_ld(v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int b = tc::row_bit(n0 + i);
+          // both operands hold set bits as 2.0: D = 4 x count, so the count's parity is bit 2
+          const uint32_t par = (__float_as_uint(__uint_as_float(v[i]) + 8388608.0f) >> 2) & 1u;
+          out[b >> 5] |= par << (b & 31);
+        }
+      }
+      *reinterpret_cast<uint4*>(sblk + ((h0 + h2) * 128 + c) * 16) = make_uint4(out[0], out[1], out[2], out[3]);
+    }
+  } else if (tid == 0) {
+    atomicExch(status, 4);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tbase, 256);
 }
 
 // v[c] = sum_h E_hi[h] * S_h[c]: block of 128 threads (one per c) over a run of h.
@@ -389,17 +439,18 @@ void launch_eq_table_f162(const f162* ps, int n, f162* out, cudaStream_t s) {
   uint64_t N = 1ull << n;
   k_eq_table_f162<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(ps, n, out);
 }
-void launch_planes_b128(const b128* x, uint64_t n, uint32_t* planes, cudaStream_t s) {
-  k_planes_b128<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, n, planes);
+void launch_expand_rows(const b128* x, int n, uint8_t* rows, cudaStream_t s) {
+  k_expand_rows<<<(n + 127) / 128, 128, 0, s>>>(reinterpret_cast<const uint4*>(x), n, rows);
 }
-void launch_sblock(const uint4* table, uint64_t nblocks, const uint32_t* lo_planes, uint8_t* sblk, cudaStream_t s) {
-  const int smem = 2 * SB_W * 128 * 4;
+void launch_sblock(const uint4* table, uint64_t nblocks, const uint8_t* elo_rows, uint8_t* sblk, int* status,
+                   cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_sblock, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_sblock_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SBT_SMEM);
     attr = true;
   }
-  k_sblock<<<(unsigned)nblocks, 256, smem, s>>>(table, lo_planes, sblk);
+  k_sblock_tc<<<(unsigned)((nblocks + 1) / 2), SBT_THREADS, SBT_SMEM, s>>>(
+      table, nblocks, reinterpret_cast<const uint4*>(elo_rows), sblk, status);
 }
 void launch_partials_combine(const b128* ehi, const uint8_t* sblk, int nblocks, unsigned long long* v, cudaStream_t s) {
   int run = 16;
