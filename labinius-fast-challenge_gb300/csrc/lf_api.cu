@@ -212,7 +212,7 @@ struct lf_ctx {
   std::vector<uint8_t> host_fold;
   cudaEvent_t ev[16];
   // batches: a second table buffer and a copy stream, so the next table uploads during a proof
-  DevBuf table2;
+  DevBuf table2, fold_strips, fold_part;
   cudaStream_t upload_stream = nullptr;
   cudaEvent_t uploaded[2] = {nullptr, nullptr};
   // serving: FIFO of submitted jobs, drained by one worker thread
@@ -603,8 +603,11 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
 
   // ---- fold (reference.rs:72-133), straight into the proof's i32 region ----
   CK(ctx->fold.ensure(fold_bytes));
-  launch_fold(table, sh.rl, sh.ring_elements, ctx->chal.as<Challenge>(), ctx->fold.as<int32_t>(),
-              ctx->status.as<int>(), st);
+  const int fsplits = fold_splits(sh.ring_elements, ctx->sms);
+  CK(ctx->fold_strips.ensure(COLUMNS * FOLD_STRIP_BYTES));
+  CK(ctx->fold_part.ensure((size_t)fsplits * fold_bytes));
+  launch_fold(table, sh.rl, sh.ring_elements, ctx->chal.as<Challenge>(), ctx->fold_strips.as<uint8_t>(),
+              ctx->fold_part.as<int32_t>(), fsplits, ctx->fold.as<int32_t>(), ctx->status.as<int>(), st);
   CKL("fold");
   cudaEventRecord(ctx->ev[9], st);
   CK(cudaMemcpyAsync(proof + at_fold, ctx->fold.p, fold_bytes, cudaMemcpyDeviceToHost, st));
@@ -616,6 +619,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   if (status[0] == 2) return fail(ctx, LF_E_INTERNAL, "a fold coefficient does not fit the wire codec");
   if (status[0] == 3) return fail(ctx, LF_E_INTERNAL, "the commitment kernel's pipeline timed out");
   if (status[0] == 4) return fail(ctx, LF_E_INTERNAL, "the partial-sum kernel's pipeline timed out");
+  if (status[0] == 5) return fail(ctx, LF_E_INTERNAL, "the fold kernel's pipeline timed out");
   if (status[0] != 0) return fail(ctx, LF_E_INTERNAL, "a device-side check failed");
 
   // ---- encode (main.rs:98-124) ----
@@ -877,6 +881,8 @@ void lf_ctx_destroy(lf_ctx* ctx) {
   ctx->keys.clear();
   for (DevBuf* b : bufs) b->release();
   ctx->table2.release();
+  ctx->fold_strips.release();
+  ctx->fold_part.release();
   for (auto& ev : ctx->ev) cudaEventDestroy(ev);
   for (auto& ev : ctx->uploaded)
     if (ev) cudaEventDestroy(ev);

@@ -119,8 +119,10 @@ struct HasherImage;  // a bk::Hasher copied to the device
 void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint32_t sign_key[8], const double* phase_re,
                        const double* phase_im, Challenge* out, int n, int* status, cudaStream_t s,
                        uint32_t* dbg = nullptr);
-void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Challenge* ch, int32_t* out, int* status,
-                 cudaStream_t s);
+int fold_splits(uint64_t ring_elements, int sms);
+constexpr size_t FOLD_STRIP_BYTES = 53 * 128;  // per column
+void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Challenge* ch, uint8_t* strips,
+                 int32_t* part, int splits, int32_t* out, int* status, cudaStream_t s);
 void launch_chunk_cvs(const uint8_t* stream, uint64_t nchunks, const uint32_t key[8], uint32_t mode, uint32_t* cvs,
                       cudaStream_t s);
 // Reduce nchunks chunk values to the chaining values of the complete subtrees of the stream

@@ -4,6 +4,7 @@
 
 #include "lf_blake3.cuh"
 #include "lf_internal.h"
+#include "lf_tc.cuh"
 
 namespace lf {
 
@@ -215,277 +216,230 @@ void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint
 // ---------------------------------------------------------------------------------------------
 // Fold (reference.rs:72-133): v_m = sum_j c_j W_{j,m} over the integers. A challenge sits in R_648
 // as c(-X^4), so with Y = X^4 each table word k of element m is folded on its own:
-// V_{m,k}(Y) = sum_j sum_t s_{j,t} Y^{pos_{j,t}} W_{j,m,k}(Y), s = sign bit XOR (pos odd), then
-// Y^162 = Y^81 - 1. Bit-sliced: a block handles 8 elements (32 words, one per bit of a u32),
-// thread y owns raw position y (0..288) as a 16-plane two's-complement counter.
+//   V_{m,k}(Y) = sum_j sum_t s_{j,t} Y^{pos_{j,t}} W_{j,m,k}(Y),  s = sign bit XOR (pos odd),
+// raw positions y = x + pos in [0, 289), then Y^162 = Y^81 - 1 (so Y^y = Y^(y-81) - Y^(y-162)
+// for 162 <= y < 243 and Y^y = -Y^(y-243) above).
+//
+// On the tensor cores this is one product per block of 128 table words (rows) and run of columns:
+//   D[row][n] = sum_j sum_x bit_x(word_j of the row) * C_j[303 - n - x],   n = 303 - y,
+// C_j the signed challenge (+-1 at its 28 positions). A = the words expanded to bf16 (2.0 per set
+// bit, bits in natural order, K-major); B[x][n] = C_j[303 - n - x] / 2 depends on x + n only, so
+// its 8 x 8 core matrices depend only on (k group + n group): one strip of 53 cores per column
+// (k_fold_cores) read through an MN-major descriptor whose k-group and n-group strides are both
+// one core. D (128 x 304, two MMAs of N = 160 and 144) is exact in f32 (|.| <= 28 x 1024).
 // ---------------------------------------------------------------------------------------------
-constexpr int FOLD_ELEMS = 8;
-constexpr int FOLD_THREADS = 320;
-constexpr int FOLD_BATCH = FOLD_THREADS / 32;  // columns transposed per step, one per warp
-constexpr int RAW_Y = 128 + 161;               // 289 raw positions
+constexpr int RAW_Y = 128 + 161;                // 289 raw positions
+constexpr int FT_CORES = 53;                    // cores per column strip
+constexpr int FT_STRIP = FT_CORES * 128;        // 6784 bytes
+constexpr int FT_TILE = 128 * 128 * 2;          // A tile: 128 words x 128 bits, bf16
+constexpr int FT_STAGES = 4;
+constexpr int FT_THREADS = 128;
+constexpr int FT_SMEM = FT_STAGES * (FT_TILE + FT_STRIP) + 64;
+constexpr long long FT_WAIT_CYCLES = 2000000000LL;
 
-__global__ void __launch_bounds__(FOLD_THREADS) k_fold(const uint4* __restrict__ table, int rl,
-                                                      uint64_t ring_elements, const Challenge* __restrict__ ch,
-                                                      int32_t* __restrict__ out, int* status) {
-  __shared__ uint32_t vec[FOLD_BATCH][128];
-  __shared__ uint8_t cpos[FOLD_BATCH][32];
-  __shared__ uint32_t csign[FOLD_BATCH];
-  __shared__ int32_t raw[32][RAW_Y + 1];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint64_t m0 = (uint64_t)blockIdx.x * FOLD_ELEMS;
-  // Columns with fewer than 8 ring elements: lanes past the last element fold zero words.
-  const int live_words = (int)min((uint64_t)FOLD_ELEMS, ring_elements - m0) * 4;
-  uint32_t P[16];
-#pragma unroll
-  for (int b = 0; b < 16; ++b) P[b] = 0;
-  for (int j0 = 0; j0 < COLUMNS; j0 += FOLD_BATCH) {
-    const int j = j0 + warp;
-    if (j < COLUMNS) {
-      uint4 v = lane < live_words ? table[((uint64_t)j << rl) + 4 * m0 + lane] : make_uint4(0, 0, 0, 0);
-      uint32_t keep[4] = {0, 0, 0, 0};
-#pragma unroll
-      for (int b = 0; b < 128; ++b) {
-        uint32_t word = b < 32 ? v.x : b < 64 ? v.y : b < 96 ? v.z : v.w;
-        uint32_t m = __ballot_sync(0xffffffffu, (word >> (b & 31)) & 1);
-        if (lane == (b & 31)) keep[b >> 5] = m;
-      }
-#pragma unroll
-      for (int i = 0; i < 4; ++i) vec[warp][32 * i + lane] = keep[i];
-      cpos[warp][lane] = ch[j].positions[lane];
-      if (lane == 0) csign[warp] = ch[j].signs;
-    }
-    __syncthreads();
-    if (tid < RAW_Y) {
-      const int nb = min(FOLD_BATCH, COLUMNS - j0);
-      for (int c = 0; c < nb; ++c) {
-        const uint32_t sg = csign[c];
-        for (int t = 0; t < WEIGHT; ++t) {
-          const int pos = cpos[c][t];
-          const int p = tid - pos;
-          if ((unsigned)p >= 128u) continue;
-          uint32_t x = vec[c][p];
-          if (!x) continue;
-          const bool neg = (((sg >> t) & 1) ^ (pos & 1)) != 0;
-          if (neg) {
-#pragma unroll
-            for (int b = 0; b < 16; ++b) {
-              uint32_t t2 = ~P[b] & x;
-              P[b] ^= x;
-              x = t2;
-              if (!x) break;
-            }
-          } else {
-#pragma unroll
-            for (int b = 0; b < 16; ++b) {
-              uint32_t t2 = P[b] & x;
-              P[b] ^= x;
-              x = t2;
-              if (!x) break;
-            }
-          }
-        }
-      }
-    }
-    __syncthreads();
-  }
-  if (tid < RAW_Y) {
-    for (int l = 0; l < 32; ++l) {
-      int32_t v = 0;
-#pragma unroll
-      for (int b = 0; b < 16; ++b) v |= (int32_t)((P[b] >> l) & 1) << b;
-      v = (v ^ 0x8000) - 0x8000;
-      raw[l][tid] = v;
-    }
+// Strip of column j: core e holds element (r, i) = C_j[303 - (8 e + r + i)] / 2 as bf16.
+__global__ void __launch_bounds__(128) k_fold_cores(const Challenge* __restrict__ ch, uint8_t* __restrict__ strips) {
+  __shared__ uint16_t dense[N162];
+  const int j = blockIdx.x, tid = threadIdx.x;
+  for (int i = tid; i < N162; i += 128) dense[i] = 0;
+  __syncthreads();
+  if (tid < WEIGHT) {
+    const int pos = ch[j].positions[tid];
+    const bool neg = (((ch[j].signs >> tid) & 1) ^ (pos & 1)) != 0;
+    dense[pos] = neg ? 0xBF00 : 0x3F00;  // -0.5 / +0.5
   }
   __syncthreads();
-  if (tid < 32) {
-    int32_t* r = raw[tid];
-    for (int y = RAW_Y - 1; y >= N162; --y) {
-      int32_t v = r[y];
-      r[y - 81] += v;
-      r[y - N162] -= v;
-    }
-  }
-  __syncthreads();
-  for (int idx = tid; idx < (live_words / 4) * 648; idx += FOLD_THREADS) {
-    const int m = idx / 648, c = idx % 648, y = c >> 2, k = c & 3;
-    const int32_t v = raw[4 * m + k][y];
-    if (v < -32768 || v > 32767) atomicExch(status, 2);
-    out[(m0 + m) * 648 + c] = v;
+  uint32_t* out = reinterpret_cast<uint32_t*>(strips + (size_t)j * FT_STRIP);
+  for (int u = tid; u < FT_STRIP / 4; u += 128) {  // two elements per u32
+    const int e = u >> 5, r = (u >> 2) & 7, i0 = 2 * (u & 3);
+    const int y0 = 303 - (8 * e + r + i0), y1 = y0 - 1;
+    const uint32_t lo = (y0 >= 0 && y0 < N162) ? dense[y0] : 0u;
+    const uint32_t hi = (y1 >= 0 && y1 < N162) ? dense[y1] : 0u;
+    out[u] = lo | (hi << 16);
   }
 }
 
-// Fold, carry-save version. A block folds 16 elements (64 table words: two 32-bit bit-slices per
-// thread) over a share of the columns; thread y owns raw position y. Per column the 128 bit
-// vectors of the 64 words sit in shared memory zero-padded to positions -161..288, so term t of
-// a challenge contributes vec[y - pos_t] with no range test. A negative term contributes the
-// complemented vector: sum_t s_t x_t = sum_{t+} x_t + sum_{t-} ~x_t - (number of negative terms),
-// and that count does not depend on y or on the lane, so it is subtracted once at the end.
-// The inputs (28 per column, 8 columns per step = 14 groups of 16) go through Harley-Seal
-// carry-save adders into a 16-plane counter. Shares of columns are summed with atomicAdd.
-constexpr int F2_BATCH = 8;                 // columns per step, one transposing warp each
-constexpr int F2_THREADS = 320;
-constexpr int F2_PAD = 161;                 // vec index = p + 161, p in [-161, 288]
-constexpr int F2_VEC = 450;
-constexpr int F2_INPUTS = F2_BATCH * WEIGHT;  // 224 = 14 x 16
-
-__device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32_t b, uint32_t c) {
-  uint32_t u = a ^ b;
-  h = (a & b) | (u & c);
-  l = u ^ c;
+// Word -> row r of an A tile, bits in natural order: u32 s of chunk q holds bits 8q + 2s (low
+// bf16) and 8q + 2s + 1 (high bf16) as 2.0 or 0.
+__device__ __forceinline__ void fold_write_row(uint8_t* tile, int r, uint4 v) {
+  const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const uint32_t x = xs[q >> 2];
+    uint32_t u[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int b0 = 8 * (q & 3) + 2 * t;  // bit of x for the low half; b0 + 1 for the high half
+      const uint32_t lo = b0 <= 14 ? x << (14 - b0) : x >> (b0 - 14);
+      const uint32_t hi = b0 <= 29 ? x << (29 - b0) : x >> (b0 - 29);
+      u[t] = (lo & 0x4000u) | (hi & 0x40000000u);
+    }
+    *reinterpret_cast<uint4*>(tile + (r >> 3) * 2048 + q * 128 + (r & 7) * 16) = make_uint4(u[0], u[1], u[2], u[3]);
+  }
 }
 
-__global__ void __launch_bounds__(F2_THREADS) k_fold2(const uint4* __restrict__ table, int rl, uint64_t ring_elements,
-                                                     const Challenge* __restrict__ ch, int col_share,
-                                                     int32_t* __restrict__ out) {
-  extern __shared__ __align__(16) uint8_t f2smem[];
-  uint2* vec = reinterpret_cast<uint2*>(f2smem);                                      // [F2_BATCH][F2_VEC]
-  int* toff = reinterpret_cast<int*>(f2smem + F2_BATCH * F2_VEC * 8);                  // [F2_INPUTS]
-  uint32_t* tmask = reinterpret_cast<uint32_t*>(toff + F2_INPUTS);                     // [F2_INPUTS]
-  __shared__ int neg_total;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint64_t m0 = (uint64_t)blockIdx.x * 16;
-  const int live = (int)min((uint64_t)16, ring_elements - m0) * 4;  // live words of the 64
-  const int c_begin = blockIdx.y * col_share, c_end = min(COLUMNS, c_begin + col_share);
-  for (int i = tid; i < F2_BATCH * F2_VEC; i += F2_THREADS) vec[i] = make_uint2(0, 0);
-  if (tid == 0) neg_total = 0;
-  uint32_t ones[2] = {0, 0}, twos[2] = {0, 0}, fours[2] = {0, 0}, eights[2] = {0, 0};
-  uint32_t P[2][12];
-#pragma unroll
-  for (int h = 0; h < 2; ++h)
-#pragma unroll
-    for (int b = 0; b < 12; ++b) P[h][b] = 0;
+// Block = 128 table words (32 ring elements) x a run of columns; out: part[split][m][4 y + k]
+// for the block's elements, the column run's share of the fold.
+__global__ void __launch_bounds__(FT_THREADS, 1)
+    k_fold_tc(const uint4* __restrict__ table, int rl, uint64_t ring_elements, const uint4* __restrict__ strips,
+              int cols_per_split, int32_t* __restrict__ part, int* status) {
+  extern __shared__ __align__(1024) uint8_t fsm[];
+  uint8_t* sS = fsm;                                   // [stage][FT_STRIP] (first: reads past a strip stay in smem)
+  uint8_t* sA = fsm + FT_STAGES * FT_STRIP;            // [stage][FT_TILE]
+  uint64_t* done = reinterpret_cast<uint64_t*>(fsm + FT_STAGES * (FT_TILE + FT_STRIP));  // [FT_STAGES]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + FT_STAGES);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint64_t words = 4 * ring_elements;
+  const uint64_t w0 = (uint64_t)blockIdx.x * 128;  // first word (row) of the block
+  const int split = blockIdx.y;
+  const int c_begin = split * cols_per_split, c_end = min(COLUMNS, c_begin + cols_per_split);
+  const bool live = w0 + tid < words;
+  if (tid == 0) {
+    *abort_flag = 0;
+    for (int i = 0; i < FT_STAGES; ++i) tc::mbar_init(&done[i], 1);
+    tc::mbar_init_fence();
+  }
+  if (warp == 0) tc::tmem_alloc(tslot, 512);
+  tc::fence_before_sync();
   __syncthreads();
-  for (int j0 = c_begin; j0 < c_end; j0 += F2_BATCH) {
-    const int nb = min(F2_BATCH, c_end - j0);
-    if (warp < nb) {
-      const int j = j0 + warp;
-      const uint4* w = table + ((uint64_t)j << rl) + 4 * m0;
-      uint4 v0 = lane < live ? w[lane] : make_uint4(0, 0, 0, 0);
-      uint4 v1 = lane + 32 < live ? w[lane + 32] : make_uint4(0, 0, 0, 0);
-      uint32_t keep0[4] = {0, 0, 0, 0}, keep1[4] = {0, 0, 0, 0};
-#pragma unroll
-      for (int b = 0; b < 128; ++b) {
-        const uint32_t a0 = b < 32 ? v0.x : b < 64 ? v0.y : b < 96 ? v0.z : v0.w;
-        const uint32_t a1 = b < 32 ? v1.x : b < 64 ? v1.y : b < 96 ? v1.z : v1.w;
-        const uint32_t m0b = __ballot_sync(0xffffffffu, (a0 >> (b & 31)) & 1);
-        const uint32_t m1b = __ballot_sync(0xffffffffu, (a1 >> (b & 31)) & 1);
-        if (lane == (b & 31)) keep0[b >> 5] = m0b, keep1[b >> 5] = m1b;
-      }
-#pragma unroll
-      for (int i = 0; i < 4; ++i) vec[warp * F2_VEC + F2_PAD + 32 * i + lane] = make_uint2(keep0[i], keep1[i]);
-      if (lane < WEIGHT) {
-        const int pos = ch[j].positions[lane];
-        const bool neg = (((ch[j].signs >> lane) & 1) ^ (pos & 1)) != 0;
-        toff[warp * WEIGHT + lane] = warp * F2_VEC + F2_PAD - pos;
-        tmask[warp * WEIGHT + lane] = neg ? 0xffffffffu : 0u;
-        const unsigned nn = __ballot_sync(0x0fffffffu, neg);
-        if (lane == 0) atomicAdd(&neg_total, __popc(nn));
-      }
-    } else if (warp < F2_BATCH) {
-      // columns past the end of the share: zero vectors, no negative terms
-#pragma unroll
-      for (int i = 0; i < 4; ++i) vec[warp * F2_VEC + F2_PAD + 32 * i + lane] = make_uint2(0, 0);
-      if (lane < WEIGHT) {
-        toff[warp * WEIGHT + lane] = warp * F2_VEC + F2_PAD;
-        tmask[warp * WEIGHT + lane] = 0u;
+  tc::fence_after_sync();
+  const uint32_t tbase = *tslot;
+  const uint32_t id160 = tc::idesc_bf16_f32(128, 160) | (1u << 16);  // B MN-major
+  const uint32_t id144 = tc::idesc_bf16_f32(128, 144) | (1u << 16);
+
+  int last = -1;
+  uint4 w = (live && c_begin < c_end) ? table[((uint64_t)c_begin << rl) + w0 + tid] : make_uint4(0, 0, 0, 0);
+  for (int c = c_begin; c < c_end; ++c) {
+    const int it = c - c_begin, s = it % FT_STAGES;
+    if (it >= FT_STAGES) {
+      const bool r = tc::mbar_wait(&done[s], ((it / FT_STAGES) - 1) & 1, abort_flag, FT_WAIT_CYCLES);
+      if (!__all_sync(0xffffffffu, r)) {
+        *abort_flag = 1;
+        atomicExch(status, 5);
       }
     }
+    const bool go = !*abort_flag;
+    if (go) {
+      const uint4* src = strips + (size_t)c * (FT_STRIP / 16);
+      for (int i = tid; i < FT_STRIP / 16; i += FT_THREADS) tc::cp_async16(sS + s * FT_STRIP + 16 * i, src + i);
+      fold_write_row(sA + s * FT_TILE, tid, w);
+    }
+    if (c + 1 < c_end) w = live ? table[((uint64_t)(c + 1) << rl) + w0 + tid] : make_uint4(0, 0, 0, 0);
+    tc::cp_async_wait_all();
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
     __syncthreads();
-    if (tid < RAW_Y) {
+    tc::fence_after_sync();
+    if (tid == 0 && go && !*abort_flag) {
+      const uint32_t a0 = tc::smem_u32(sA + s * FT_TILE), b0 = tc::smem_u32(sS + s * FT_STRIP);
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk) {
+        const uint64_t ad = tc::sdesc(a0 + kk * 256, 128, 2048);
+        const uint32_t acc = (it | kk) ? 1u : 0u;
+        tc::mma_bf16(tbase, ad, tc::sdesc(b0 + (2 * kk) * 128, 128, 128), id160, acc);
+        tc::mma_bf16(tbase + 160, ad, tc::sdesc(b0 + (2 * kk + 20) * 128, 128, 128), id144, acc);
+      }
+      tc::mma_commit(&done[s]);
+      last = it;
+    }
+  }
+  if (tid == 0 && last >= 0) {  // drain: the last commit covers every MMA
+    const long long t0 = clock64();
+    while (!tc::mbar_try_wait(&done[last % FT_STAGES], (last / FT_STAGES) & 1) && clock64() - t0 < FT_WAIT_CYCLES) {
+    }
+  }
+  const int ncols = c_end - c_begin;
+  bool ok = !*abort_flag;
+  if (ok && ncols > 0) {
+    const int lt = ncols - 1;
+    ok = __all_sync(0xffffffffu, tc::mbar_wait(&done[lt % FT_STAGES], (lt / FT_STAGES) & 1, abort_flag,
+                                                FT_WAIT_CYCLES));
+  }
+  ok = __syncthreads_and(ok);
+  tc::fence_after_sync();
+  // Ring reduction per row into shared memory (the stages are free now): fin[row][i], i < 162.
+  int32_t* fin = reinterpret_cast<int32_t*>(fsm);
+  const int FS = N162 + 1;
+  for (int i = 0; i < N162; ++i) fin[tid * FS + i] = 0;
+  if (ok && ncols > 0) {
 #pragma unroll 1
-      for (int g = 0; g < F2_INPUTS / 16; ++g) {
-        uint32_t x[2][16];
+    for (int n0 = 0; n0 < 304; n0 += 16) {
+      uint32_t v[16];
+      tc::tmem_ld_x16(tbase + ((uint32_t)(32 * warp) << 16) + n0, v);
+      tc::tmem_wait_ld(v);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const int k = 16 * g + i;
-          const uint2 v = vec[toff[k] + tid];
-          const uint32_t m = tmask[k];
-          x[0][i] = v.x ^ m, x[1][i] = v.y ^ m;
-        }
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, sixteens;
-          csa(twosA, ones[h], ones[h], x[h][0], x[h][1]);
-          csa(twosB, ones[h], ones[h], x[h][2], x[h][3]);
-          csa(foursA, twos[h], twos[h], twosA, twosB);
-          csa(twosA, ones[h], ones[h], x[h][4], x[h][5]);
-          csa(twosB, ones[h], ones[h], x[h][6], x[h][7]);
-          csa(foursB, twos[h], twos[h], twosA, twosB);
-          csa(eightsA, fours[h], fours[h], foursA, foursB);
-          csa(twosA, ones[h], ones[h], x[h][8], x[h][9]);
-          csa(twosB, ones[h], ones[h], x[h][10], x[h][11]);
-          csa(foursA, twos[h], twos[h], twosA, twosB);
-          csa(twosA, ones[h], ones[h], x[h][12], x[h][13]);
-          csa(twosB, ones[h], ones[h], x[h][14], x[h][15]);
-          csa(foursB, twos[h], twos[h], twosA, twosB);
-          csa(eightsB, fours[h], fours[h], foursA, foursB);
-          csa(sixteens, eights[h], eights[h], eightsA, eightsB);
-          uint32_t c = sixteens;
-#pragma unroll
-          for (int b = 0; b < 12; ++b) {
-            const uint32_t t = P[h][b] & c;
-            P[h][b] ^= c;
-            c = t;
-          }
+      for (int i = 0; i < 16; ++i) {
+        const int y = 303 - (n0 + i);
+        if (y >= RAW_Y) continue;
+        const int32_t raw = (int32_t)__float2int_rn(__uint_as_float(v[i]));
+        if (y < N162) {
+          fin[tid * FS + y] += raw;
+        } else if (y < N162 + 81) {
+          fin[tid * FS + y - 81] += raw;
+          fin[tid * FS + y - N162] -= raw;
+        } else {
+          fin[tid * FS + y - 243] -= raw;
         }
       }
     }
-    __syncthreads();
-  }
-  // Un-slice: raw[lane][y] for the 64 words, then the ring reduction Y^162 = Y^81 - 1 per word.
-  int32_t* raw = reinterpret_cast<int32_t*>(f2smem);  // [64][RAW_Y + 1], reuses the vectors' space
-  const int ntot = neg_total;
-  if (tid < RAW_Y) {
-#pragma unroll
-    for (int h = 0; h < 2; ++h)
-      for (int l = 0; l < 32; ++l) {
-        int32_t v = (int32_t)((ones[h] >> l) & 1) | ((int32_t)((twos[h] >> l) & 1) << 1) |
-                    ((int32_t)((fours[h] >> l) & 1) << 2) | ((int32_t)((eights[h] >> l) & 1) << 3);
-#pragma unroll
-        for (int b = 0; b < 12; ++b) v |= (int32_t)((P[h][b] >> l) & 1) << (b + 4);
-        raw[(32 * h + l) * (RAW_Y + 1) + tid] = v - ntot;
-      }
   }
   __syncthreads();
-  if (tid < 64) {
-    int32_t* r = raw + tid * (RAW_Y + 1);
-    for (int y = RAW_Y - 1; y >= N162; --y) {
-      const int32_t v = r[y];
-      r[y - 81] += v;
-      r[y - N162] -= v;
+  if (ok) {
+    // row = 4 m + k; part[split][(w0 / 4 + m) * 648 + 4 i + k], coalesced over the block's elements
+    const uint64_t m0 = w0 / 4;
+    const int nel = (int)min((uint64_t)32, ring_elements - m0);
+    int32_t* dst = part + ((uint64_t)split * ring_elements + m0) * 648;
+    for (int idx = tid; idx < nel * 648; idx += FT_THREADS) {
+      const int m = idx / 648, cc = idx % 648;
+      dst[idx] = fin[(4 * m + (cc & 3)) * FS + (cc >> 2)];
     }
+  } else if (tid == 0) {
+    atomicExch(status, 5);
   }
+  tc::fence_before_sync();
   __syncthreads();
-  for (int idx = tid; idx < (live / 4) * 648; idx += F2_THREADS) {
-    const int m = idx / 648, c = idx % 648, y = c >> 2, k = c & 3;
-    atomicAdd(&out[(m0 + m) * 648 + c], raw[(4 * m + k) * (RAW_Y + 1) + y]);
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tbase, 512);
+}
+
+// out = sum over the column runs; every coefficient must fit the wire's i16 range (status 2).
+__global__ void k_fold_sum(const int32_t* __restrict__ part, int splits, uint64_t n, int32_t* __restrict__ out,
+                           int* status) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    int32_t v = 0;
+    for (int s = 0; s < splits; ++s) v += part[(uint64_t)s * n + i];
+    out[i] = v;
+    if (v < -32768 || v > 32767) atomicExch(status, 2);
   }
 }
 
-__global__ void k_fold_range(const int32_t* __restrict__ out, uint64_t n, int* status) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-    if (out[i] < -32768 || out[i] > 32767) atomicExch(status, 2);
+// Column runs of the fold: blocks = ceil(words / 128) x splits should fill whole waves of the SMs.
+int fold_splits(uint64_t ring_elements, int sms) {
+  const uint64_t blocks = (4 * ring_elements + 127) / 128;
+  int best = 1;
+  double best_eff = -1;
+  for (int s = 1; s <= 32; ++s) {
+    const uint64_t total = blocks * s, waves = (total + sms - 1) / sms;
+    const double eff = (double)total / (double)(waves * sms) - 0.004 * s;  // small cost per extra run
+    if (eff > best_eff) best_eff = eff, best = s;
+  }
+  return best;
 }
 
-void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Challenge* ch, int32_t* out, int* status,
-                 cudaStream_t s) {
-  const int smem_vec = F2_BATCH * F2_VEC * 8 + 2 * F2_INPUTS * 4;
-  const int smem_raw = 64 * (RAW_Y + 1) * 4;
-  const int smem = smem_vec > smem_raw ? smem_vec : smem_raw;
+void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Challenge* ch, uint8_t* strips,
+                 int32_t* part, int splits, int32_t* out, int* status, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_fold2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_fold_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, FT_SMEM);
     attr = true;
   }
-  const unsigned blocks = (unsigned)((ring_elements + 15) / 16);
-  // Enough blocks to cover the SMs: split the columns when there are few element blocks.
-  int shares = 1;
-  while (blocks * shares < 2 * 152 && shares < 64) shares *= 2;
-  const int col_share = COLUMNS / shares;
-  cudaMemsetAsync(out, 0, ring_elements * 648 * 4, s);
-  k_fold2<<<dim3(blocks, shares), F2_THREADS, smem, s>>>(table, rl, ring_elements, ch, col_share, out);
-  k_fold_range<<<256, 256, 0, s>>>(out, ring_elements * 648, status);
+  k_fold_cores<<<COLUMNS, 128, 0, s>>>(ch, strips);
+  const unsigned blocks = (unsigned)((4 * ring_elements + 127) / 128);
+  const int per = (COLUMNS + splits - 1) / splits;
+  k_fold_tc<<<dim3(blocks, splits), FT_THREADS, FT_SMEM, s>>>(table, rl, ring_elements,
+                                                              reinterpret_cast<const uint4*>(strips), per, part, status);
+  k_fold_sum<<<1024, 256, 0, s>>>(part, splits, ring_elements * 648, out, status);
 }
 
 // ---------------------------------------------------------------------------------------------
