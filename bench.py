@@ -247,10 +247,12 @@ def commit_roofline(log_vars, commit_ms):
             peak, kind = float(json.load(f)["bf16_tflops_sustained"]), "measured (sustained)"
     except (OSError, KeyError, ValueError):
         peak = 1700.0
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "k_commit_tc_traffic.json")
-    if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get("bytes_per_launch")
+    traffic = None  # dram bytes read + written per launch, from the committed ncu summary
+    tpath = os.path.join(ROOT, "profiles", "k_commit_tc_2p31.md")
+    if log_vars == 31 and os.path.exists(tpath):
+        for line in open(tpath):
+            if line.startswith("traffic_bytes_per_launch:"):
+                traffic = int(line.split(":")[1])
     return {"kernel": "k_commit_tc", "bound": "tensor", "achieved": round(achieved, 1), "peak": peak,
             "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": kind,
             "flops_per_launch": flops}

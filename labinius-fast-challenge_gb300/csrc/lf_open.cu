@@ -232,9 +232,11 @@ constexpr int RAW_Y = 128 + 161;                // 289 raw positions
 constexpr int FT_CORES = 53;                    // cores per column strip
 constexpr int FT_STRIP = FT_CORES * 128;        // 6784 bytes
 constexpr int FT_TILE = 128 * 128 * 2;          // A tile: 128 words x 128 bits, bf16
-constexpr int FT_STAGES = 4;
+constexpr int FT_STAGES = 4;                    // A tiles (read by the MMAs)
+constexpr int FT_RING = 8;                      // strips and raw words, loaded FT_AHEAD columns early
+constexpr int FT_AHEAD = 3;
 constexpr int FT_THREADS = 128;
-constexpr int FT_SMEM = FT_STAGES * (FT_TILE + FT_STRIP) + 64;
+constexpr int FT_SMEM = FT_RING * FT_STRIP + FT_STAGES * FT_TILE + FT_RING * 128 * 16 + 64;
 constexpr long long FT_WAIT_CYCLES = 2000000000LL;
 
 // Strip of column j: core e holds element (r, i) = C_j[303 - (8 e + r + i)] / 2 as bf16.
@@ -284,9 +286,10 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
     k_fold_tc(const uint4* __restrict__ table, int rl, uint64_t ring_elements, const uint4* __restrict__ strips,
               int cols_per_split, int32_t* __restrict__ part, int* status) {
   extern __shared__ __align__(1024) uint8_t fsm[];
-  uint8_t* sS = fsm;                                   // [stage][FT_STRIP] (first: reads past a strip stay in smem)
-  uint8_t* sA = fsm + FT_STAGES * FT_STRIP;            // [stage][FT_TILE]
-  uint64_t* done = reinterpret_cast<uint64_t*>(fsm + FT_STAGES * (FT_TILE + FT_STRIP));  // [FT_STAGES]
+  uint8_t* sS = fsm;                                   // [FT_RING][FT_STRIP] (first: reads past a strip stay in smem)
+  uint8_t* sA = fsm + FT_RING * FT_STRIP;              // [FT_STAGES][FT_TILE]
+  uint4* sW = reinterpret_cast<uint4*>(sA + FT_STAGES * FT_TILE);  // [FT_RING][128] raw words
+  uint64_t* done = reinterpret_cast<uint64_t*>(sW + FT_RING * 128);  // [FT_STAGES]
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + FT_STAGES);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -308,10 +311,24 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   const uint32_t id160 = tc::idesc_bf16_f32(128, 160) | (1u << 16);  // B MN-major
   const uint32_t id144 = tc::idesc_bf16_f32(128, 144) | (1u << 16);
 
+  // Column c's strip and this thread's word go to ring slot c % FT_RING, one commit group per
+  // column (empty past the run), FT_AHEAD columns before they are used.
+  if (!live) sW[tid] = make_uint4(0, 0, 0, 0);  // never copied: zero rows (only slot 0 is read then)
+  auto fetch = [&](int c) {
+    if (c < c_end) {
+      const int slot = (c - c_begin) % FT_RING;
+      const uint4* src = strips + (size_t)c * (FT_STRIP / 16);
+      for (int i = tid; i < FT_STRIP / 16; i += FT_THREADS) tc::cp_async16(sS + slot * FT_STRIP + 16 * i, src + i);
+      if (live) tc::cp_async16(sW + slot * 128 + tid, table + ((uint64_t)c << rl) + w0 + tid);
+    }
+    tc::cp_async_commit();
+  };
+  for (int a = 0; a < FT_AHEAD; ++a) fetch(c_begin + a);
   int last = -1;
-  uint4 w = (live && c_begin < c_end) ? table[((uint64_t)c_begin << rl) + w0 + tid] : make_uint4(0, 0, 0, 0);
   for (int c = c_begin; c < c_end; ++c) {
-    const int it = c - c_begin, s = it % FT_STAGES;
+    const int it = c - c_begin, s = it % FT_STAGES, slot = it % FT_RING;
+    // A stage s was read by the MMAs of column it - FT_STAGES; the strip slot that fetch() is
+    // about to fill was read by those of it + FT_AHEAD - FT_RING, which are older.
     if (it >= FT_STAGES) {
       const bool r = tc::mbar_wait(&done[s], ((it / FT_STAGES) - 1) & 1, abort_flag, FT_WAIT_CYCLES);
       if (!__all_sync(0xffffffffu, r)) {
@@ -319,20 +336,16 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
         atomicExch(status, 5);
       }
     }
+    fetch(c + FT_AHEAD);
+    tc::cp_async_wait<FT_AHEAD>();  // column c's group has landed
     const bool go = !*abort_flag;
-    if (go) {
-      const uint4* src = strips + (size_t)c * (FT_STRIP / 16);
-      for (int i = tid; i < FT_STRIP / 16; i += FT_THREADS) tc::cp_async16(sS + s * FT_STRIP + 16 * i, src + i);
-      fold_write_row(sA + s * FT_TILE, tid, w);
-    }
-    if (c + 1 < c_end) w = live ? table[((uint64_t)(c + 1) << rl) + w0 + tid] : make_uint4(0, 0, 0, 0);
-    tc::cp_async_wait_all();
+    if (go) fold_write_row(sA + s * FT_TILE, tid, live ? sW[slot * 128 + tid] : make_uint4(0, 0, 0, 0));
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     if (tid == 0 && go && !*abort_flag) {
-      const uint32_t a0 = tc::smem_u32(sA + s * FT_TILE), b0 = tc::smem_u32(sS + s * FT_STRIP);
+      const uint32_t a0 = tc::smem_u32(sA + s * FT_TILE), b0 = tc::smem_u32(sS + slot * FT_STRIP);
 #pragma unroll
       for (int kk = 0; kk < 8; ++kk) {
         const uint64_t ad = tc::sdesc(a0 + kk * 256, 128, 2048);
@@ -344,6 +357,7 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
       last = it;
     }
   }
+  tc::cp_async_wait<0>();
   if (tid == 0 && last >= 0) {  // drain: the last commit covers every MMA
     const long long t0 = clock64();
     while (!tc::mbar_try_wait(&done[last % FT_STAGES], (last / FT_STAGES) & 1) && clock64() - t0 < FT_WAIT_CYCLES) {
