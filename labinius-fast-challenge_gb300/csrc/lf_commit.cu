@@ -13,6 +13,7 @@
 //
 // Results modulo each prime are recombined by Garner's CRT. For Q = 3889*9721*17497 (the three
 // primes of solution-arm/proof_generate/src/ntt.rs:37-40) the recombination is already modulo Q.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 
@@ -312,9 +313,10 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
 // The transform of a table word (128 bits = the Y-coefficients 0..127 of one residue class of X
 // mod 4) at leaf s is the evaluation sum_j bit_j zeta_s^j (mod p), zeta_s the leaf's root: a
 // product with the Vandermonde matrix V[s][j] = zeta_s^j. On the tensor core it is exact:
-//   A (M = 128 table columns x 128 bits) holds each bit as bf16 2.0 or 0 and is read twice;
-//   B (N = 64 x K = 256) holds per leaf (V mod 256) / 2 against the first reading and
-//   (V >> 8) * 128 against the second (both exact in bf16), so the f32 accumulator is
+//   A (M = 128 table columns x 128 bits) holds each set bit as a power of two a_kappa (bf16 with
+//   one exponent bit, see commit_write_row) and is read twice;
+//   B (N = 64 x K = 256) holds per leaf (V mod 256) / a against the first reading and
+//   (V >> 8) * 256 / a against the second (both exact in bf16), so the f32 accumulator is
 //   sum_j bit_j V[s][j] < 2^22, an exact integer.
 // The epilogue reduces that sum mod p in f32 (every intermediate is an integer below 2^24), then
 // does the 4x4 base multiplication with the key on the integer pipe.
@@ -332,6 +334,27 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
 // (about a second); a timeout sets *status = 3 and the block skips its remaining work but keeps
 // the barrier count, so every thread drains.
 // ------------------------------------------------------------------------------------------------
+// Word -> row c of an A slot, K order as tc::write_row (u32 o holds bits o % 16 and o % 16 + 16
+// of word o / 16), but a set bit is the bf16 with the single exponent bit 11 + (o & 3): 2^-111,
+// 2^-95, 2^-63 or 2. One shift of the source serves four outputs through four masks; the B tiles
+// carry the inverse powers of two, so every product is the same integer as before.
+__device__ __forceinline__ void commit_write_row(uint8_t* tile, int c, uint4 v) {
+  const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const uint32_t x = xs[q >> 2];
+    const int t0 = (q & 3) * 4;
+    const uint32_t y = t0 < 12 ? x << (11 - t0) : x >> 1;
+    *reinterpret_cast<uint4*>(tile + (c >> 3) * 2048 + q * 128 + (c & 7) * 16) =
+        make_uint4(y & 0x08000800u, y & 0x10001000u, y & 0x20002000u, y & 0x40004000u);
+  }
+}
+// Value of a set bit at K position kappa (0..127) of a commit_write_row row.
+static double commit_bit_value(int kappa) {
+  const int b = (kappa >> 1) & 3;
+  return b == 3 ? 2.0 : b == 2 ? ldexp(1.0, -63) : b == 1 ? ldexp(1.0, -95) : ldexp(1.0, -111);
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_commit_tc(const uint4* __restrict__ table, const uint32_t* __restrict__ key, const uint4* __restrict__ btiles,
                 uint32_t* __restrict__ partial, int rl, int elements, int per_split, int nprimes, int* status) {
@@ -403,7 +426,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     };
     auto store_pre = [&](int e, uint4 u) {  // ... into the A slots / the key ring
       if (expander) {
-        tc::write_row(sA + (tid >> 7) * TC_A_BYTES, tid & (TC_COLS - 1), u);
+        commit_write_row(sA + (tid >> 7) * TC_A_BYTES, tid & (TC_COLS - 1), u);
       } else if (keyer) {
         int4 v;  // centred into (-p/2, p/2]
         v.x = (int)u.x > half ? (int)u.x - (int)p : (int)u.x;
@@ -536,7 +559,8 @@ static void fill_btiles(const PrimePlan& pl, const PrimeConst& c, uint16_t* out 
         for (int kappa = 0; kappa < TC_K; ++kappa) {
           const int limb = kappa >> 7;
           const uint64_t V = pw[tc::row_bit(kappa & 127)];
-          const float f = limb == 0 ? (float)(V & 255) * 0.5f : (float)(V >> 8) * 128.0f;
+          const double scale = 1.0 / commit_bit_value(kappa & 127);  // exact power of two
+          const float f = (float)(limb == 0 ? (double)(V & 255) * scale : (double)(V >> 8) * 256.0 * scale);
           uint32_t u;
           memcpy(&u, &f, 4);
           const size_t off = (size_t)(n >> 3) * 4096 + (kappa >> 3) * 128 + (n & 7) * 16 + (kappa & 7) * 2;

@@ -161,16 +161,21 @@ class Prover:
         if rc != LF_OK:
             raise LfError(rc, self.lib.lf_last_error(self.ctx).decode())
 
-    def prove(self, seed, table, log_vars, q=BASELINE_Q):
-        """Proof bytes for a host table (bytes, bytearray, memoryview or numpy array)."""
+    def prove(self, seed, table, log_vars, q=BASELINE_Q, out=None):
+        """Proof bytes for a host table (bytes, bytearray, memoryview, numpy array or ctypes buffer).
+        With `out` (a ctypes buffer of at least proof_size bytes, reused across calls) the proof is
+        written there and (out, length) is returned instead of a bytes copy."""
         mv = memoryview(table).cast("B")
         cap = proof_size(q, log_vars)
-        out = (ctypes.c_uint8 * max(cap, 1))()
+        keep = out
+        out = out if out is not None else (ctypes.c_uint8 * max(cap, 1))()
         n = ctypes.c_size_t()
         buf = (ctypes.c_uint8 * len(mv)).from_buffer_copy(mv) if mv.readonly else (ctypes.c_uint8 * len(mv)).from_buffer(mv)
         rc = self.lib.lf_prove(self.ctx, bytes(seed), q_bytes(q), log_vars, ctypes.cast(buf, ctypes.c_void_p),
                                len(mv), out, cap, ctypes.byref(n))
         self._check(rc)
+        if keep is not None:
+            return out, n.value
         return ctypes.string_at(out, n.value)
 
     def prove_device(self, seed, table_dev, log_vars, q=BASELINE_Q, out=None):
