@@ -278,10 +278,11 @@ void phase_tables(std::vector<double>& re, std::vector<double>& im) {
 // copied from the host), the commitment's split partial sums, the partial-sum blocks, the
 // transcript stream, the fold output and the smaller work buffers, plus the transient buffers of
 // a key build. Used for admission against the context's HBM budget.
-size_t proof_footprint(const Shape& sh, bool host_table, int sms) {
-  const size_t key = (size_t)3 * sh.ring_elements * LEAVES * 64;
-  const size_t build = (size_t)3 * sh.ring_elements * (RING_N + 4 * LEAVES) * 4;
-  const size_t partial = (size_t)commit_splits(sh.ring_elements, 3, sms) * 3 * COLUMNS * LEAVES * 16;
+size_t proof_footprint(const Shape& sh, bool host_table, int sms, int nprimes) {
+  const size_t key = (size_t)nprimes * sh.ring_elements * LEAVES * 64;
+  const size_t build = (size_t)nprimes * sh.ring_elements * (RING_N + 4 * LEAVES) * 4;
+  const size_t partial =
+      (size_t)commit_splits(sh.ring_elements, nprimes, sms) * nprimes * COLUMNS * LEAVES * 16;
   const size_t blocks = (sh.words / 4096) * (128 * 16 + 16);
   const size_t stream = STREAM_PREFIX + (size_t)12 * COLUMNS * RING_N + 1024;
   const size_t fold = (size_t)4 * RING_N * sh.ring_elements;
@@ -289,9 +290,17 @@ size_t proof_footprint(const Shape& sh, bool host_table, int sms) {
   return (host_table ? sh.words * 16 : 0) + key + build + partial + blocks + stream + fold + small;
 }
 
-int admit(lf_ctx* ctx, const Shape& sh, bool host_table) {
+// Primes of the commitment for modulus q (3 for the baseline, else about one per 14.9 bits of
+// the coefficient bound).
+int primes_for(u128 q, const Shape& sh) {
+  if (q == (u128)3889 * 9721 * 17497) return 3;
+  const double bits = std::log2((double)sh.ring_elements) + std::log2(1296.0) + std::log2((double)(q - 1)) + 1.0;
+  return std::min(MAX_PRIMES, (int)std::ceil(bits / 14.9));
+}
+
+int admit(lf_ctx* ctx, u128 q, const Shape& sh, bool host_table) {
   if (ctx->budget == 0) return LF_OK;
-  const size_t need = proof_footprint(sh, host_table, ctx->sms);
+  const size_t need = proof_footprint(sh, host_table, ctx->sms, primes_for(q, sh));
   if (need > ctx->budget)
     return fail(ctx, LF_E_ADMISSION, "request needs " + std::to_string(need >> 20) + " MiB of device memory, budget " +
                                          std::to_string(ctx->budget >> 20) + " MiB");
@@ -305,7 +314,7 @@ int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh) {
   if (!ctx->key) {
     std::string e;
     ModulusPlan mp;
-    if (!make_modulus_plan(q, mp, e)) return fail(ctx, LF_E_MODULUS, e);
+    if (!make_modulus_plan(q, sh.ring_elements, mp, e)) return fail(ctx, LF_E_MODULUS, e);
     // Evict least recently used shapes: beyond the count limit, or while the cached keys and
     // this proof would exceed the budget.
     auto cached = [&]() {
@@ -313,7 +322,7 @@ int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh) {
       for (auto& k : ctx->keys) b += k->bytes();
       return b;
     };
-    const size_t need = proof_footprint(sh, true, ctx->sms);
+    const size_t need = proof_footprint(sh, true, ctx->sms, mp.nprimes);
     while (!ctx->keys.empty() &&
            (ctx->keys.size() >= MAX_KEYS || (ctx->budget && cached() + need > ctx->budget))) {
       auto oldest = std::min_element(ctx->keys.begin(), ctx->keys.end(),
@@ -672,7 +681,7 @@ int check_job(lf_ctx* ctx, const lf_job& j, u128& q, Shape& sh) {
   if (rc) return rc;
   if (!j.table_on_device && j.table_bytes != sh.words * 16)
     return fail(ctx, LF_E_TABLE_LEN, "witness table has the wrong length");
-  return admit(ctx, sh, !j.table_on_device);
+  return admit(ctx, q, sh, !j.table_on_device);
 }
 
 using clk = std::chrono::steady_clock;
@@ -925,7 +934,7 @@ int lf_prove_device(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16],
   Shape sh;
   int rc = check_request(ctx, q_le, log_vars, proof, proof_cap, proof_len, q, sh);
   if (rc) return rc;
-  if ((rc = admit(ctx, sh, false))) return rc;
+  if ((rc = admit(ctx, q, sh, false))) return rc;
   cudaSetDevice(ctx->device);
   auto t0 = std::chrono::steady_clock::now();
   ctx->prof = lf_profile{};
@@ -944,7 +953,7 @@ int lf_prove(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32
   int rc = check_request(ctx, q_le, log_vars, proof, proof_cap, proof_len, q, sh);
   if (rc) return rc;
   if (table_bytes != sh.words * 16) return fail(ctx, LF_E_TABLE_LEN, "witness table has the wrong length");
-  if ((rc = admit(ctx, sh, true))) return rc;
+  if ((rc = admit(ctx, q, sh, true))) return rc;
   cudaSetDevice(ctx->device);
   auto t0 = std::chrono::steady_clock::now();
   ctx->prof = lf_profile{};

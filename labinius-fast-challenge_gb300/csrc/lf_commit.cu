@@ -35,7 +35,6 @@ constexpr int TC_A_BYTES = TC_COLS * 128 * 2;        // 32 KB per A slot (one ta
 constexpr int TC_B_BYTES = TC_N * TC_K * 2;          // 32 KB
 constexpr int TC_KEY_INTS = TC_LEAVES * 16;          // one element's key rows for the block's leaves
 constexpr int TC_SMEM = 4 * TC_A_BYTES + TC_B_BYTES + 4 * TC_KEY_INTS * 4 + 2 * 8 + 16;
-constexpr int TC_REDUCE_EVERY = 6;                   // elements between accumulator reductions
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;   // ~1 s at 2 GHz
 
 static void fill_btiles(const PrimePlan& pl, const PrimeConst& c, uint16_t* out);
@@ -109,6 +108,12 @@ static void fill_consts(const PrimePlan& pl, PrimeConst& c) {
   c.w = (uint32_t)pw(81);
   c.w5 = (uint32_t)pw(405);
   c.inv_split = inv_mod((c.w + p - c.w5) % p, p);
+  {
+    // |r| <= (p - 1) / 2 + 1, |key| <= (p - 1) / 2, 4 products per element; stay inside int32
+    const uint64_t h = (p - 1) / 2, per = 4 * (h + 1) * h;
+    uint64_t r = (0x7fffffffull - p) / per;
+    c.reduce_every = (uint32_t)(r < 1 ? 1 : r);
+  }
   for (int s = 0; s < LEAVES; ++s) c.leaf_root[s] = (uint32_t)pw(pl.leaf_e[s]);
 }
 
@@ -118,7 +123,14 @@ static uint32_t bits_of(u128 x) {
   return n;
 }
 
-bool make_modulus_plan(u128 q, ModulusPlan& mp, std::string& err) {
+static bool is_prime32(uint32_t n) {
+  if (n < 2) return false;
+  for (uint32_t d = 2; d * d <= n; ++d)
+    if (n % d == 0) return false;
+  return true;
+}
+
+bool make_modulus_plan(u128 q, uint64_t elements, ModulusPlan& mp, std::string& err) {
   mp = ModulusPlan();
   mp.q = q;
   mp.bits = bits_of(q - 1);
@@ -129,8 +141,37 @@ bool make_modulus_plan(u128 q, ModulusPlan& mp, std::string& err) {
     mp.primes[0] = 3889, mp.primes[1] = 9721, mp.primes[2] = 17497;
     mp.exact_lift = false;
   } else {
-    err = "this build commits only under Q = 661473542593 (3889*9721*17497)";
-    return false;
+    // |c| <= elements * 2 * 648 * (q - 1): per element each reduced coefficient takes at most
+    // 2 x 648 products a_i w_k (X^648 = X^324 - 1, X^972 = -1). Need prod(p) > 2 |c| + 1.
+    // Compare in log2 with a margin (the product itself may exceed 128 bits).
+    const double need = std::log2((double)elements) + std::log2(1296.0) + std::log2((double)(q - 1)) + 1.0 + 0.01;
+    double have = 0;
+    mp.exact_lift = true;
+    for (uint32_t p = 32767; p > 486 && have <= need; --p) {
+      if (p % 486 != 1 || !is_prime32(p)) continue;
+      if (mp.nprimes == MAX_PRIMES) break;
+      mp.primes[mp.nprimes++] = p;
+      have += std::log2((double)p);
+    }
+    if (have <= need) {
+      err = "no set of transform primes covers this modulus";
+      return false;
+    }
+    // product mod q, and floor(product / 2) in the mixed radix of the primes (digit k in [0, p_k))
+    u128 pm = 1 % q;
+    for (int i = 0; i < mp.nprimes; ++i) pm = pm * mp.primes[i] % q;  // pm < 2^96, p < 2^15
+    mp.p_mod_q = pm;
+    // halving a mixed-radix number: digits from the most significant down, carrying remainders
+    uint64_t rem = 0;
+    std::vector<uint32_t> d(mp.nprimes, 0);
+    // the product itself has digits (0, ..., 0, 1) one place above the top; halve that
+    rem = 1;
+    for (int k = mp.nprimes - 1; k >= 0; --k) {
+      const uint64_t cur = rem * mp.primes[k];  // value of the remainder in units of the next digit
+      d[k] = (uint32_t)(cur / 2);
+      rem = cur % 2;
+    }
+    for (int k = 0; k < mp.nprimes; ++k) mp.half_digits[k] = d[k];
   }
   mp.consts.resize(mp.nprimes);
   mp.btiles.assign((size_t)mp.nprimes * 3 * (TC_B_BYTES / 2), 0);
@@ -504,7 +545,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             acc[i][3] += kv.w * ri;
           }
         }
-        if (++since == TC_REDUCE_EVERY) {
+        if (++since == (int)P.reduce_every) {
           since = 0;
 #pragma unroll
           for (int i = 0; i < 9; ++i)
@@ -612,7 +653,10 @@ void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, c
 struct FinishArgs {
   int nprimes, splits;
   uint32_t width;
+  int exact;                     // 1: lift to the signed integer, then mod q
+  uint64_t q_lo, q_hi, pq_lo, pq_hi;  // q and (product of the primes) mod q
   uint32_t primes[MAX_PRIMES];
+  uint32_t half[MAX_PRIMES];     // floor(product / 2), mixed radix
   uint32_t ginv[MAX_PRIMES][MAX_PRIMES];
 };
 
@@ -674,7 +718,24 @@ __global__ void __launch_bounds__(256) k_commit_finish(FinishArgs a, const uint3
       digit[k] = t;
     }
     u128 val = 0;
-    for (int k = a.nprimes - 1; k >= 0; --k) val = val * a.primes[k] + digit[k];
+    if (!a.exact) {
+      // the primes' product is q itself: the mixed-radix value is the coefficient in [0, q)
+      for (int k = a.nprimes - 1; k >= 0; --k) val = val * a.primes[k] + digit[k];
+    } else {
+      // signed integer in (-P/2, P/2]: negative when the digits exceed floor(P/2)'s
+      bool neg = false;
+      for (int k = a.nprimes - 1; k >= 0; --k)
+        if (digit[k] != a.half[k]) {
+          neg = digit[k] > a.half[k];
+          break;
+        }
+      const u128 q = ((u128)a.q_hi << 64) | a.q_lo;
+      for (int k = a.nprimes - 1; k >= 0; --k) val = (val * a.primes[k] + digit[k]) % q;  // < 2^111 before %
+      if (neg) {
+        const u128 pq = ((u128)a.pq_hi << 64) | a.pq_lo;
+        val = (val + q - pq) % q;
+      }
+    }
     uint8_t* o = out + ((size_t)col * RING_N + i) * a.width;
     for (uint32_t b = 0; b < a.width; ++b) o[b] = (uint8_t)(val >> (8 * b));
   }
@@ -688,8 +749,12 @@ void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t
   a.nprimes = mp.nprimes;
   a.splits = splits;
   a.width = mp.width;
+  a.exact = mp.exact_lift ? 1 : 0;
+  a.q_lo = (uint64_t)mp.q, a.q_hi = (uint64_t)(mp.q >> 64);
+  a.pq_lo = (uint64_t)mp.p_mod_q, a.pq_hi = (uint64_t)(mp.p_mod_q >> 64);
   for (int i = 0; i < mp.nprimes; ++i) {
     a.primes[i] = mp.primes[i];
+    a.half[i] = mp.half_digits[i];
     for (int j = 0; j < i; ++j) a.ginv[i][j] = mp.garner_inv[i][j];
   }
   k_commit_finish<<<COLUMNS, 256, 0, s>>>(a, partial, out);

@@ -57,6 +57,7 @@ struct PrimeConst {
   uint32_t w, w5, inv_split;       // eta^81, eta^405, 1/(eta^81 - eta^405)
   uint32_t fw[80][2];              // forward twiddles per internal node (key transform)
   uint32_t leaf_root[LEAVES];      // eta^leaf_e[s]
+  uint32_t reduce_every;           // elements the commitment epilogue may accumulate before reducing
 };
 
 struct ModulusPlan {
@@ -65,6 +66,8 @@ struct ModulusPlan {
   int nprimes = 0;
   uint32_t primes[MAX_PRIMES];
   bool exact_lift = false;         // true: CRT gives the integer product, reduced mod q after
+  u128 p_mod_q = 0;                // product of the primes mod q (exact lift: negative values)
+  uint32_t half_digits[MAX_PRIMES];  // floor(product / 2) in the primes' mixed radix (sign test)
   std::vector<PrimeConst> consts;
   // Per prime and third of its leaves, the Vandermonde limbs of the tensor-core commitment
   // (bf16 bits in the MMA's shared-memory layout).
@@ -72,7 +75,11 @@ struct ModulusPlan {
   // Garner constants: inv[i][j] = p_j^-1 mod p_i for j < i
   uint32_t garner_inv[MAX_PRIMES][MAX_PRIMES];
 };
-bool make_modulus_plan(u128 q, ModulusPlan& mp, std::string& err);
+// The commitment's primes for modulus q at `elements` ring elements per column: for the baseline
+// Q = 3889 * 9721 * 17497 its three factors (CRT gives the value mod q directly); for any other
+// q, primes p = 1 (mod 486) below 2^15, largest first, until their product exceeds twice the
+// largest |coefficient| of the integer product (elements * 1296 * (q - 1)).
+bool make_modulus_plan(u128 q, uint64_t elements, ModulusPlan& mp, std::string& err);
 
 struct ProveProfile {
   double key_ms, commit_ms, finish_ms, transcript_ms, partials_ms, switch_ms, row_ms, challenges_ms,

@@ -29,6 +29,23 @@ def test_proof_matches_oracle(prover, oracle, log_vars, seed):
     assert ok, msg
 
 
+# Moduli other than 3889*9721*17497 commit through an exact integer lift over more transform
+# primes (main.rs:2255-2266 proves under 9721*2917*4861; the gate admits any 35..96-bit Q).
+OTHER_Q = [9721 * 2917 * 4861, 1 << 40, (1 << 64) - 59, (1 << 96) - 17]
+
+
+@pytest.mark.parametrize("q", OTHER_Q, ids=["3primes", "2^40", "2^64-59", "2^96-17"])
+@pytest.mark.parametrize("log_vars", [19, 20])
+def test_other_moduli_match_oracle(prover, oracle, log_vars, q):
+    seed = SEEDS[2]
+    table = oracle.write_table(seed, log_vars)
+    got = prover.prove(seed, table, log_vars, q=q)
+    want = oracle.prove(seed, table, log_vars, q=q)
+    assert got == want, f"fields differ: {_first_diff(got, want, log_vars, oracle)}"
+    ok, msg = oracle.verify(seed, got, log_vars, table)
+    assert ok, msg
+
+
 def test_wrong_seed_rejected(prover, oracle):
     # solution/proof_generate/src/main.rs:2244-2253: a proof for seed 42 fails under seed 43.
     log_vars = 20
