@@ -31,6 +31,7 @@ extern "C" {
 #define LF_E_LIMIT (-10)    /* the request exceeds a fixed-size scratch (lf_sample_challenges_noalloc) */
 #define LF_E_TIMEOUT (-11)  /* lf_poll: the job has not finished within the wait */
 #define LF_E_TICKET (-12)   /* lf_poll: no such ticket (never issued, or its result was already taken) */
+#define LF_E_REJECT (-13)   /* lf_verify: the proof does not verify; lf_last_error names the check */
 
 typedef struct lf_ctx lf_ctx;
 
@@ -133,6 +134,15 @@ int lf_prove_batch(lf_ctx* ctx, size_t n, const lf_job* jobs, lf_result* results
  * progress and reports LF_E_INTERNAL for jobs still queued. No counterpart in the reference. */
 int lf_submit(lf_ctx* ctx, const lf_job* job, uint64_t* ticket);
 int lf_poll(lf_ctx* ctx, uint64_t ticket, uint32_t wait_ms, lf_result* out);
+
+/* The checker (verifier/proof_verify/src/main.rs:293-409: check_proof_shape, check_field_switch,
+ * check_opening) on the GPU: LF_OK if the proof verifies against the table (host memory, or
+ * NULL to regenerate the seed's table with the table PRG as main.rs:143-153 does), LF_E_REJECT
+ * with the failing check in lf_last_error otherwise. lf_verify_device takes a device table. */
+int lf_verify(lf_ctx* ctx, const uint8_t seed[32], uint32_t log_vars, const void* table, size_t table_bytes,
+              const uint8_t* proof, size_t proof_len);
+int lf_verify_device(lf_ctx* ctx, const uint8_t seed[32], uint32_t log_vars, const void* table_dev, const uint8_t* proof,
+                     size_t proof_len);
 
 /* Diagnostics: n folding challenges sampled on the device from Transcript::new(domain) after
  * absorb_bytes(prefix) (challenge.rs:240-259, 707-737), 40 bytes each as above. */

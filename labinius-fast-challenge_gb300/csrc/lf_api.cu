@@ -184,6 +184,7 @@ struct DevBuf {
 struct KeyCache {
   u128 q = 0;
   uint64_t elements = 0;
+  int extra_bits = 0;  // lift margin beyond a binary witness (the verifier's a_times_v: 15)
   uint64_t last_use = 0;
   ModulusPlan mp;
   DevBuf key;     // u32 [prime][element][leaf][k][l]: the 4x4 base-multiplication matrix per leaf
@@ -204,7 +205,7 @@ struct lf_ctx {
   lf_profile prof{};
   std::vector<std::unique_ptr<KeyCache>> keys;  // per shape, least recently used evicted first
   KeyCache* key = nullptr;                      // the key of the proof in progress
-  u128 consts_q = 0;                            // modulus whose prime constants are on the device
+  const KeyCache* consts_of = nullptr;          // key whose prime constants are on the device
   uint64_t key_clock = 0;
   DevBuf table, stream_buf, partial, sblk, ehi, elo, lo_planes, rhi, vparts, psi, batch, soa, msg, p0, eqt, row,
       hasher, chal, fold, cvs, cvs_scratch, subtrees, status, phase, scratch_small, wbuf, rbuf;
@@ -307,14 +308,15 @@ int admit(lf_ctx* ctx, u128 q, const Shape& sh, bool host_table) {
   return LF_OK;
 }
 
-int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh) {
+int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh, int extra_bits = 0) {
   ctx->key = nullptr;
   for (auto& k : ctx->keys)
-    if (k->q == q && k->elements == sh.ring_elements) ctx->key = k.get();
+    if (k->q == q && k->elements == sh.ring_elements && (k->extra_bits == extra_bits || !k->mp.exact_lift))
+      ctx->key = k.get();
   if (!ctx->key) {
     std::string e;
     ModulusPlan mp;
-    if (!make_modulus_plan(q, sh.ring_elements, mp, e)) return fail(ctx, LF_E_MODULUS, e);
+    if (!make_modulus_plan(q, sh.ring_elements, extra_bits, mp, e)) return fail(ctx, LF_E_MODULUS, e);
     // Evict least recently used shapes: beyond the count limit, or while the cached keys and
     // this proof would exceed the budget.
     auto cached = [&]() {
@@ -340,7 +342,7 @@ int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh) {
     CK(kc->btiles.ensure(mp.btiles.size() * 2));
     CK(cudaMemcpyAsync(kc->btiles.p, mp.btiles.data(), mp.btiles.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
     upload_prime_consts(mp, ctx->stream);
-    ctx->consts_q = q;
+    ctx->consts_of = nullptr;  // set below once the entry exists
     launch_matrix_expand(mp, E, ared.as<uint32_t>(), ctx->stream);
     launch_key_transform(mp, E, ared.as<uint32_t>(), leaf.as<uint32_t>(), kc->key.as<uint32_t>(), ctx->stream);
     CKL("key build");
@@ -350,13 +352,15 @@ int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh) {
     kc->mp = mp;
     kc->q = q;
     kc->elements = E;
+    kc->extra_bits = extra_bits;
     ctx->keys.push_back(std::move(kc));
     ctx->key = ctx->keys.back().get();
+    ctx->consts_of = ctx->key;
   }
   ctx->key->last_use = ++ctx->key_clock;
-  if (ctx->consts_q != q) {
+  if (ctx->consts_of != ctx->key) {  // another key's primes are in the constant bank
     upload_prime_consts(ctx->key->mp, ctx->stream);
-    ctx->consts_q = q;
+    ctx->consts_of = ctx->key;
   }
   return LF_OK;
 }
@@ -368,6 +372,36 @@ float ev_ms(lf_ctx* ctx, int a, int b) {
 }
 
 void put_u64(uint8_t* p, uint64_t x) { memcpy(p, &x, 8); }
+
+// v[c] = sum_j bit_c(pi0[j]) eq(r_hi)[j] over the table (crossfield.rs:548-573): GF(2) products
+// per block of 4096 words against E_lo on the tensor cores, then 2^(LP-12) GHASH products with
+// E_hi. Shared by the prover and the verifier's trusted recomputation (main.rs:308-320).
+int device_partials(lf_ctx* ctx, const uint4* table, const Shape& sh, const std::vector<b128>& hi,
+                    std::vector<b128>& partials) {
+  cudaStream_t st = ctx->stream;
+  const int LB = 12, HB = sh.lp - 12;
+  const uint64_t nblocks = 1ull << HB;
+  CK(ctx->rhi.ensure(64 * 16));
+  CK(ctx->elo.ensure(4096 * 16));
+  CK(ctx->ehi.ensure(nblocks * 16));
+  CK(ctx->lo_planes.ensure(4096 * 256));  // E_lo expanded to bf16 rows (32 tiles of 128)
+  CK(ctx->sblk.ensure(nblocks * 128 * 16));
+  CK(ctx->vparts.ensure(256 * 8));
+  CK(ctx->status.ensure(16));
+  CK(cudaMemcpyAsync(ctx->rhi.p, hi.data(), 16 * hi.size(), cudaMemcpyHostToDevice, st));
+  launch_eq_b128(ctx->rhi.as<b128>() + HB, LB, ctx->elo.as<b128>(), st);
+  launch_eq_b128(ctx->rhi.as<b128>(), HB, ctx->ehi.as<b128>(), st);
+  launch_expand_rows(ctx->elo.as<b128>(), 4096, ctx->lo_planes.as<uint8_t>(), st);
+  launch_sblock(table, nblocks, ctx->lo_planes.as<uint8_t>(), ctx->sblk.as<uint8_t>(), ctx->status.as<int>(), st);
+  CK(cudaMemsetAsync(ctx->vparts.p, 0, 256 * 8, st));
+  launch_partials_combine(ctx->ehi.as<b128>(), ctx->sblk.as<uint8_t>(), (int)nblocks,
+                          ctx->vparts.as<unsigned long long>(), st);
+  CKL("partials");
+  partials.assign(128, b128{0, 0});
+  CK(cudaMemcpyAsync(partials.data(), ctx->vparts.p, 128 * 16, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return LF_OK;
+}
 
 // The proof of one table already on the device.
 int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, const uint4* table, uint8_t* proof,
@@ -462,26 +496,9 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   // ---- point and partials (main.rs:177-189; crossfield.rs:548-573) ----
   std::vector<b128> lo = t.sample_b128("r-lo", 7);
   std::vector<b128> hi = t.sample_b128("r-hi", sh.lp);
-  const int LB = 12, HB = sh.lp - 12;
-  const uint64_t nblocks = 1ull << HB;
-  CK(ctx->rhi.ensure(64 * 16));
-  CK(ctx->elo.ensure(4096 * 16));
-  CK(ctx->ehi.ensure(nblocks * 16));
-  CK(ctx->lo_planes.ensure(4096 * 256));  // E_lo expanded to bf16 rows (32 tiles of 128)
-  CK(ctx->sblk.ensure(nblocks * 128 * 16));
-  CK(ctx->vparts.ensure(256 * 8));
-  CK(cudaMemcpyAsync(ctx->rhi.p, hi.data(), 16 * hi.size(), cudaMemcpyHostToDevice, st));
-  launch_eq_b128(ctx->rhi.as<b128>() + HB, LB, ctx->elo.as<b128>(), st);
-  launch_eq_b128(ctx->rhi.as<b128>(), HB, ctx->ehi.as<b128>(), st);
-  launch_expand_rows(ctx->elo.as<b128>(), 4096, ctx->lo_planes.as<uint8_t>(), st);
-  launch_sblock(table, nblocks, ctx->lo_planes.as<uint8_t>(), ctx->sblk.as<uint8_t>(), ctx->status.as<int>(), st);
-  CK(cudaMemsetAsync(ctx->vparts.p, 0, 256 * 8, st));
-  launch_partials_combine(ctx->ehi.as<b128>(), ctx->sblk.as<uint8_t>(), (int)nblocks,
-                          ctx->vparts.as<unsigned long long>(), st);
-  CKL("partials");
-  std::vector<b128> partials(128);
-  CK(cudaMemcpyAsync(partials.data(), ctx->vparts.p, 128 * 16, cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
+  const int HB = sh.lp - 12;
+  std::vector<b128> partials;
+  if ((rc = device_partials(ctx, table, sh, hi, partials))) return rc;
   cudaEventRecord(ctx->ev[5], st);
   b128 claim = {0, 0};
   {
@@ -737,6 +754,333 @@ void serve_loop(lf_ctx* ctx) {
     }
     ctx->qcv.notify_all();
   }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Verifier (verifier/proof_verify/src/main.rs:293-409: check_proof_shape, check_field_switch,
+// check_opening). The table passes and ring products run on the device: the trusted partials
+// (the prover's partial-sum kernels), a_times_v (K2 over the folded witness's transform) and the
+// challenge combination; the transcript replay, the sumcheck recurrence and the small F162 sums
+// run on the host.
+// ---------------------------------------------------------------------------------------------
+struct ProofParts {
+  u128 q = 0;
+  const uint8_t* commit = nullptr;
+  size_t commit_len = 0;
+  std::vector<b128> partials;
+  std::vector<f162> rounds;  // e0, einf per round
+  f162 opened = {0, 0, 0};
+  const uint8_t* row = nullptr;
+  size_t row_len = 0;
+  const uint8_t* folded = nullptr;
+  size_t folded_len = 0;
+};
+uint64_t rd64(const uint8_t* p) {
+  uint64_t x;
+  memcpy(&x, p, 8);
+  return x;
+}
+// bincode fixint layout of main.rs:98-124, no trailing bytes.
+bool decode_proof(const uint8_t* b, size_t len, ProofParts& p, std::string& err) {
+  size_t at = 0;
+  auto need = [&](uint64_t n) {
+    if (at > len || len - at < n) {
+      err = "truncated proof";
+      return false;
+    }
+    return true;
+  };
+  auto vec = [&](const uint8_t*& ptr, size_t& n) {
+    if (!need(8)) return false;
+    const uint64_t k = rd64(b + at);
+    at += 8;
+    if (!need(k)) return false;
+    ptr = b + at, n = (size_t)k;
+    at += k;
+    return true;
+  };
+  if (!need(20)) return false;
+  if (b[0] != 1 || b[1] || b[2] || b[3]) {
+    err = "unsupported proof version";
+    return false;
+  }
+  p.q = q_from_le(b + 4);
+  at = 20;
+  if (!vec(p.commit, p.commit_len)) return false;
+  if (!need(8)) return false;
+  const uint64_t np = rd64(b + at);
+  at += 8;
+  if (np > (len - at) / 16) return (err = "truncated proof", false);
+  p.partials.resize(np);
+  for (uint64_t i = 0; i < np; ++i, at += 16) p.partials[i] = {rd64(b + at), rd64(b + at + 8)};
+  if (!need(8)) return false;
+  const uint64_t nr = rd64(b + at);
+  at += 8;
+  if (nr > (len - at) / 48) return (err = "truncated proof", false);
+  p.rounds.resize(2 * nr);
+  for (uint64_t i = 0; i < 2 * nr; ++i, at += 24) p.rounds[i] = {rd64(b + at), rd64(b + at + 8), rd64(b + at + 16)};
+  if (!need(24)) return false;
+  p.opened = {rd64(b + at), rd64(b + at + 8), rd64(b + at + 16)};
+  at += 24;
+  if (!vec(p.row, p.row_len) || !vec(p.folded, p.folded_len)) return false;
+  if (at != len) return (err = "trailing bytes", false);
+  return true;
+}
+
+const f162 F_ZERO = {0, 0, 0}, F_ONE = {1, 0, 0};
+bool canonical(f162 x) { return (x.w2 >> 34) == 0; }
+
+// eq table (eval.rs:50-64): out[j] = prod_k (bit k of j ? p_k : 1 + p_k).
+std::vector<f162> eq_table_host(const std::vector<f162>& ps) {
+  std::vector<f162> out(1, F_ONE);
+  for (const f162& pk : ps) {
+    f162 pk1 = pk;
+    pk1.w0 ^= 1;
+    std::vector<f162> nx(2 * out.size());
+    for (size_t j = 0; j < out.size(); ++j) {
+      nx[j] = f162_mul(out[j], pk1);
+      nx[j + out.size()] = f162_mul(out[j], pk);
+    }
+    out.swap(nx);
+  }
+  return out;
+}
+
+// The transparent coefficient (crossfield.rs:10-65, 139-148): prod_i (1 + v_i + h_i) as a
+// 128-vector over F162 (coordinate k = coefficient of x^k in GHASH), h_i = r_hi[i] acting by
+// GHASH multiplication, folded against batch.
+f162 transparent_coeff(const std::vector<b128>& r_hi, const std::vector<f162>& r_pp, const std::vector<f162>& batch) {
+  std::vector<f162> t(128, F_ZERO), hs(128), vs(128);
+  t[0] = F_ONE;
+  for (size_t i = 0; i < r_pp.size(); ++i) {
+    for (int k = 0; k < 128; ++k) vs[k] = f162_mul(t[k], r_pp[i]);
+    std::fill(hs.begin(), hs.end(), F_ZERO);
+    for (int k = 127; k >= 0; --k) {
+      // hs <- hs * x in GHASH (x^128 = x^7 + x^2 + x + 1), then + t if bit k of r_hi[i]
+      const f162 top = hs[127];
+      for (int x = 127; x > 0; --x) hs[x] = hs[x - 1];
+      hs[0] = F_ZERO;
+      for (int x : {0, 1, 2, 7}) hs[x] = f162_add(hs[x], top);
+      if (b128_bit(r_hi[i], k))
+        for (int x = 0; x < 128; ++x) hs[x] = f162_add(hs[x], t[x]);
+    }
+    for (int k = 0; k < 128; ++k) t[k] = f162_add(f162_add(t[k], vs[k]), hs[k]);
+  }
+  f162 acc = F_ZERO;
+  for (int k = 0; k < 128; ++k) acc = f162_add(acc, f162_mul(t[k], batch[k]));
+  return acc;
+}
+
+// slice_sum (crossfield.rs:637-649): sum_k lift(u_k) batch[k], bit i of u_k = bit k of v[i].
+f162 slice_sum(const std::vector<b128>& v, const std::vector<f162>& batch) {
+  f162 s = F_ZERO;
+  for (int k = 0; k < 128; ++k) {
+    b128 u = {0, 0};
+    for (int i = 0; i < 128; ++i)
+      if (b128_bit(v[i], k)) (i < 64 ? u.lo : u.hi) |= 1ull << (i & 63);
+    s = f162_add(s, f162_mul(f162_lift(u), batch[k]));
+  }
+  return s;
+}
+
+b128 claim_of(const std::vector<b128>& partials, const std::vector<b128>& lo) {  // main.rs:184-189
+  std::vector<b128> e = eq_expand_b128(lo);
+  b128 acc = {0, 0};
+  for (int i = 0; i < 128; ++i) acc = b128_add(acc, b128_mul(partials[i], e[i]));
+  return acc;
+}
+
+bool unpack_row(const uint8_t* b, size_t len, std::vector<f162>& out) {  // wire/mod.rs:96-140
+  if (len != ((size_t)COLUMNS * 162 + 7) / 8) return false;
+  out.assign(COLUMNS, F_ZERO);
+  size_t bit = 0;
+  auto get = [&](int n) {
+    uint64_t x = 0;
+    for (int i = 0; i < n; ++i, ++bit) x |= (uint64_t)((b[bit >> 3] >> (bit & 7)) & 1) << i;
+    return x;
+  };
+  for (int i = 0; i < COLUMNS; ++i) out[i] = {get(64), get(64), get(34)};
+  return true;
+}
+
+f162 challenge_f162(const Challenge& c) {  // challenge.rs:454-461
+  f162 x = F_ZERO;
+  for (uint32_t i = 0; i < c.weight; ++i) {
+    const int pos = c.positions[i];
+    (pos < 64 ? x.w0 : pos < 128 ? x.w1 : x.w2) |= 1ull << (pos & 63);
+  }
+  return x;
+}
+
+u128 rem_euclid(__int128 a, u128 q) {
+  const __int128 m = (__int128)q;
+  __int128 r = a % m;
+  return (u128)(r < 0 ? r + m : r);
+}
+
+// The whole check of one proof against a table already on the device (main.rs:293-409).
+int verify_device(lf_ctx* ctx, const uint8_t seed[32], const Shape& sh, const uint4* table, const uint8_t* proof,
+                  size_t len) {
+  cudaStream_t st = ctx->stream;
+  auto reject = [&](const std::string& why) { return fail(ctx, LF_E_REJECT, why); };
+  if (len > (size_t)64 << 20) return reject("proof too large");
+  ProofParts pr;
+  std::string e;
+  if (!decode_proof(proof, len, pr, e)) return reject(e);
+  if (pr.partials.size() != 128) return reject("128 partial evaluations");
+  if (pr.rounds.size() != 2 * (size_t)sh.lp) return reject("one switch round per packed coordinate");
+  const u128 q = pr.q;
+  if (!accept_modulus(q, sh)) return reject("invalid commitment modulus");
+  Transcript t;  // main.rs:166-174
+  t.init("labinius-fast/v1");
+  t.absorb_bytes(seed, 32);
+  t.absorb_u64((uint64_t)sh.log_vars);
+  t.absorb_u64((uint64_t)COLUMN_LOG);
+  uint8_t qb[16];
+  for (int i = 0; i < 16; ++i) qb[i] = (uint8_t)(q >> (8 * i));
+  t.absorb_bytes(qb, 16);
+  t.absorb_bytes(pr.commit, pr.commit_len);
+  // ---- check_field_switch ----
+  std::vector<b128> lo = t.sample_b128("r-lo", 7);
+  std::vector<b128> hi = t.sample_b128("r-hi", sh.lp);
+  std::vector<b128> trusted;
+  int rc = device_partials(ctx, table, sh, hi, trusted);
+  if (rc) return rc;
+  const b128 value = claim_of(trusted, lo);
+  t.absorb_b128(&value, 1);
+  t.absorb_b128(pr.partials.data(), 128);
+  const std::vector<f162> batch = eq_expand_f162(t.sample_f162("switch-batch", 7));
+  const b128 claimed = claim_of(pr.partials, lo);
+  if (claimed.lo != value.lo || claimed.hi != value.hi) return reject("partial evaluation mismatch");
+  f162 sum = slice_sum(pr.partials, batch);
+  std::vector<f162> coords;
+  for (int r = 0; r < sh.lp; ++r) {
+    const f162 e0 = pr.rounds[2 * r], einf = pr.rounds[2 * r + 1];
+    if (!canonical(e0) || !canonical(einf)) return reject("noncanonical F162 element");
+    t.absorb_f162(&pr.rounds[2 * r], 2);
+    const f162 ch = t.sample_f162("switch-round", 1)[0];
+    const f162 e1 = f162_add(sum, e0);
+    sum = f162_add(f162_add(e0, f162_mul(ch, f162_add(f162_add(e0, e1), einf))), f162_mul(f162_mul(ch, ch), einf));
+    coords.push_back(ch);
+  }
+  if (!canonical(pr.opened)) return reject("noncanonical F162 element");
+  const f162 d = transparent_coeff(hi, coords, batch);
+  if (f162_eq(d, F_ZERO)) return reject("the switch left the opened value unbound");
+  if (!f162_eq(sum, f162_mul(d, pr.opened))) return reject("sumcheck final check failed");
+  t.absorb_f162(&pr.opened, 1);
+  // ---- check_opening ----
+  const std::vector<f162> p0(coords.rbegin(), coords.rend() - COLUMN_LOG);  // main.rs:257-264
+  const std::vector<f162> p1(coords.rend() - COLUMN_LOG, coords.rend());
+  std::vector<f162> row;
+  if (!unpack_row(pr.row, pr.row_len, row)) return reject("malformed row evaluation");
+  const size_t nv = (size_t)RING_N * sh.ring_elements;
+  if (pr.folded_len != 4 * nv) return reject("malformed folded witness");
+  std::vector<int32_t> v(nv);
+  memcpy(v.data(), pr.folded, 4 * nv);
+  for (int32_t w : v)
+    if (w < -32768 || w > 32767) return reject("malformed folded witness");
+  {  // RowEvaluation::absorb (scheme/commitment.rs:320-331)
+    const char* label = "labinius/row-evaluation";
+    t.absorb_bytes(label, strlen(label));
+    t.absorb_bytes(row.data(), row.size() * 24);
+  }
+  CK(ctx->hasher.ensure(sizeof(bk::Hasher)));
+  CK(ctx->chal.ensure(COLUMNS * sizeof(Challenge)));
+  CK(ctx->status.ensure(16));
+  CK(cudaMemcpyAsync(ctx->hasher.p, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(ctx->status.p, 0, 16, st));
+  launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.as<double>(), ctx->phase.as<double>() + 162 * 88,
+                    ctx->chal.as<Challenge>(), COLUMNS, ctx->status.as<int>(), st);
+  t.counter += COLUMNS;
+  CKL("challenges");
+  std::vector<Challenge> ch(COLUMNS);
+  CK(cudaMemcpyAsync(ch.data(), ctx->chal.p, COLUMNS * sizeof(Challenge), cudaMemcpyDeviceToHost, st));
+  int status[4];
+  CK(cudaMemcpyAsync(status, ctx->status.p, 16, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (status[0] != 0) return fail(ctx, LF_E_INTERNAL, "challenge sampling exceeded its attempt bound");
+  {
+    const std::vector<f162> e1 = eq_table_host(p1);
+    f162 acc = F_ZERO;
+    for (int j = 0; j < COLUMNS; ++j) acc = f162_add(acc, f162_mul(e1[j], row[j]));
+    if (!f162_eq(acc, pr.opened)) return reject("the row evaluation does not reduce to the opened value");
+  }
+  uint64_t normsq = 0, worst = 0;
+  for (int32_t c : v) {
+    const uint64_t m = (uint64_t)(c < 0 ? -(int64_t)c : c);
+    normsq += m * m;
+    worst = std::max(worst, m);
+  }
+  if (normsq > fold_cap(sh)) return reject("the fold is longer than the cap");
+  if ((u128)worst > (q - 1) / 2) return reject("the fold is not centered");
+  const size_t w = coefficient_bytes(q);
+  if (pr.commit_len != w * COLUMNS * RING_N) return reject("malformed commitment");
+  for (size_t i = 0; i < (size_t)COLUMNS * RING_N; ++i) {
+    u128 x = 0;
+    for (size_t b = w; b-- > 0;) x = (x << 8) | pr.commit[i * w + b];
+    if (x >= q) return reject("malformed commitment");
+  }
+  // a_times_v == challenge_combination (rq.rs:188-256), both on the device
+  rc = ensure_key(ctx, q, sh, 15);
+  if (rc) return rc;
+  const ModulusPlan& mp = ctx->key->mp;
+  const uint64_t E = sh.ring_elements;
+  DevBuf vdev, vred, vhat, part, atv, commit_dev, chpart;
+  CK(vdev.ensure(4 * nv));
+  CK(vred.ensure((size_t)mp.nprimes * nv * 4));
+  CK(vhat.ensure((size_t)mp.nprimes * E * 4 * LEAVES * 4));
+  CK(part.ensure((size_t)mp.nprimes * COLUMNS * LEAVES * 16));
+  CK(atv.ensure(RING_N * w + 64));
+  CK(commit_dev.ensure(pr.commit_len));
+  CK(chpart.ensure((size_t)32 * (2 * RING_N - 1) * 16));
+  CK(cudaMemcpyAsync(vdev.p, v.data(), 4 * nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(commit_dev.p, pr.commit, pr.commit_len, cudaMemcpyHostToDevice, st));
+  launch_a_times_v(mp, sh, vdev.as<int32_t>(), ctx->key->key.as<uint32_t>(), vred.as<uint32_t>(),
+                   vhat.as<uint32_t>(), part.as<uint32_t>(), atv.as<uint8_t>(), st);
+  launch_challenge_combination(commit_dev.as<uint8_t>(), (uint32_t)w, ctx->chal.as<Challenge>(),
+                               chpart.as<unsigned long long>(), st);
+  CKL("a_times_v / challenge_combination");
+  std::vector<uint8_t> atv_host(RING_N * w);
+  std::vector<unsigned long long> chp((size_t)32 * (2 * RING_N - 1) * 2);
+  CK(cudaMemcpyAsync(atv_host.data(), atv.p, RING_N * w, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(chp.data(), chpart.p, chp.size() * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  {
+    // sum the column runs, then X^648 = X^324 - 1 from the top (rq.rs fold into the ring)
+    std::vector<__int128> raw(2 * RING_N - 1, 0);
+    for (int run = 0; run < 32; ++run)
+      for (int r = 0; r < 2 * RING_N - 1; ++r) {
+        const size_t i = 2 * ((size_t)run * (2 * RING_N - 1) + r);
+        const u128 u = ((u128)chp[i + 1] << 64) | chp[i];
+        raw[r] = (__int128)rem_euclid(raw[r] + (__int128)u, q);
+      }
+    for (int k = 2 * RING_N - 2; k >= RING_N; --k) {
+      const __int128 x = (__int128)rem_euclid(raw[k], q);
+      raw[k] = 0;
+      raw[k - RING_N / 2] += x;
+      raw[k - RING_N] -= x;
+    }
+    for (int i = 0; i < RING_N; ++i) {
+      const u128 want = rem_euclid(raw[i], q);
+      u128 got = 0;
+      for (size_t b = w; b-- > 0;) got = (got << 8) | atv_host[i * w + b];
+      if (got != want) return reject("the fold does not open the folded commitment");
+    }
+  }
+  {  // main.rs:266-289: the fold's parity against the challenges' combination of the row
+    const std::vector<f162> e0 = eq_table_host(p0);
+    f162 left = F_ZERO, right = F_ZERO;
+    for (uint64_t m = 0; m < E; ++m)
+      for (int k = 0; k < 4; ++k) {
+        f162 x = F_ZERO;  // components_mod_2 (main.rs:268-280)
+        for (int pp = 0; pp < RING_N / 4; ++pp)
+          if (v[m * RING_N + 4 * pp + k] & 1) (pp < 64 ? x.w0 : pp < 128 ? x.w1 : x.w2) |= 1ull << (pp & 63);
+        left = f162_add(left, f162_mul(e0[4 * m + k], x));
+      }
+    for (int j = 0; j < COLUMNS; ++j) right = f162_add(right, f162_mul(challenge_f162(ch[j]), row[j]));
+    if (!f162_eq(left, right)) return reject("the fold does not match the folded row evaluation");
+  }
+  return LF_OK;
 }
 
 // Table PRG (verifier/table_writer/src/main.rs:14-22): keyed BLAKE3 XOF of the context string.
@@ -1146,6 +1490,40 @@ int lf_sample_challenges_noalloc(int device, const char* domain, const uint8_t* 
   return rc;
 }
 
+int lf_verify_device(lf_ctx* ctx, const uint8_t seed[32], uint32_t log_vars, const void* table_dev, const uint8_t* proof,
+                     size_t proof_len) {
+  if (!ctx || !seed || !table_dev || !proof) return fail(ctx, LF_E_ARGS, "null argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  Shape sh;
+  if (!sh.set(log_vars) || sh.lp < 12) return fail(ctx, LF_E_SHAPE, "unsupported LOG_VARS");
+  cudaSetDevice(ctx->device);
+  return verify_device(ctx, seed, sh, reinterpret_cast<const uint4*>(table_dev), proof, proof_len);
+}
+
+int lf_verify(lf_ctx* ctx, const uint8_t seed[32], uint32_t log_vars, const void* table, size_t table_bytes,
+              const uint8_t* proof, size_t proof_len) {
+  if (!ctx || !seed || !proof) return fail(ctx, LF_E_ARGS, "null argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  Shape sh;
+  if (!sh.set(log_vars) || sh.lp < 12) return fail(ctx, LF_E_SHAPE, "unsupported LOG_VARS");
+  cudaSetDevice(ctx->device);
+  CK(ctx->table.ensure(sh.words * 16));
+  if (table) {
+    if (table_bytes != sh.words * 16) return fail(ctx, LF_E_TABLE_LEN, "witness table has the wrong length");
+    CK(cudaMemcpyAsync(ctx->table.p, table, table_bytes, cudaMemcpyHostToDevice, ctx->stream));
+  } else {  // the table of the seed, as the checker regenerates it (main.rs:143-153)
+    bk::Hasher h;
+    h.init_keyed(seed);
+    const char* c = "labinius-fast/binary-table/v1";
+    h.absorb((const uint8_t*)c, strlen(c));
+    const bk::Pending root = h.finish();
+    const uint64_t blocks = (sh.words * 16) / 64;
+    k_table_prg<<<(unsigned)((blocks + 255) / 256), 256, 0, ctx->stream>>>(root, blocks, ctx->table.as<uint4>());
+    CKL("table PRG");
+  }
+  return verify_device(ctx, seed, sh, ctx->table.as<uint4>(), proof, proof_len);
+}
+
 int lf_last_profile(lf_ctx* ctx, lf_profile* out) {
   if (!ctx || !out) return LF_E_ARGS;
   *out = ctx->prof;
@@ -1166,6 +1544,7 @@ const char* lf_strerror(int code) {
     case LF_E_ADMISSION: return "request exceeds the HBM budget";
     case LF_E_TIMEOUT: return "the job has not finished yet";
     case LF_E_TICKET: return "no such ticket";
+    case LF_E_REJECT: return "the proof does not verify";
     case LF_E_LIMIT: return "request exceeds the fixed scratch of lf_sample_challenges_noalloc (4096 challenges)";
     default: return "unknown error";
   }

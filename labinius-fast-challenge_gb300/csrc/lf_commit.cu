@@ -130,7 +130,7 @@ static bool is_prime32(uint32_t n) {
   return true;
 }
 
-bool make_modulus_plan(u128 q, uint64_t elements, ModulusPlan& mp, std::string& err) {
+bool make_modulus_plan(u128 q, uint64_t elements, int extra_bits, ModulusPlan& mp, std::string& err) {
   mp = ModulusPlan();
   mp.q = q;
   mp.bits = bits_of(q - 1);
@@ -144,7 +144,8 @@ bool make_modulus_plan(u128 q, uint64_t elements, ModulusPlan& mp, std::string& 
     // |c| <= elements * 2 * 648 * (q - 1): per element each reduced coefficient takes at most
     // 2 x 648 products a_i w_k (X^648 = X^324 - 1, X^972 = -1). Need prod(p) > 2 |c| + 1.
     // Compare in log2 with a margin (the product itself may exceed 128 bits).
-    const double need = std::log2((double)elements) + std::log2(1296.0) + std::log2((double)(q - 1)) + 1.0 + 0.01;
+    const double need =
+        std::log2((double)elements) + std::log2(1296.0) + std::log2((double)(q - 1)) + 1.0 + extra_bits + 0.01;
     double have = 0;
     mp.exact_lift = true;
     for (uint32_t p = 32767; p > 486 && have <= need; --p) {
@@ -742,7 +743,7 @@ __global__ void __launch_bounds__(256) k_commit_finish(FinishArgs a, const uint3
 }
 
 void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t* partial, int splits, uint8_t* out,
-                          cudaStream_t s) {
+                          cudaStream_t s, int ncols) {
   (void)sh;
   FinishArgs a;
   memset(&a, 0, sizeof a);
@@ -757,7 +758,83 @@ void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t
     a.half[i] = mp.half_digits[i];
     for (int j = 0; j < i; ++j) a.ginv[i][j] = mp.garner_inv[i][j];
   }
-  k_commit_finish<<<COLUMNS, 256, 0, s>>>(a, partial, out);
+  k_commit_finish<<<ncols, 256, 0, s>>>(a, partial, out);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Verifier: a_times_v (rq.rs:188-217) = sum_m A_m v_m in R_Q for the folded witness v (|v| <= 2^15):
+// v mod p -> the same forward transform as the key (k_key_forward), base multiplication with the
+// key's 4x4 matrices summed over the elements (one thread per prime, leaf and coefficient l),
+// then K2 on that single column.
+// ------------------------------------------------------------------------------------------------
+__global__ void k_atv_reduce(int nprimes, uint64_t elements, const int32_t* __restrict__ v, uint32_t* __restrict__ vred) {
+  const uint64_t n = (uint64_t)nprimes * elements * RING_N;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const int pi = (int)(i / (elements * RING_N));
+    const int64_t p = c_prime[pi].p;
+    const int64_t x = v[i % (elements * RING_N)];
+    vred[i] = (uint32_t)(((x % p) + p) % p);
+  }
+}
+
+__global__ void k_atv_mac(int nprimes, uint64_t elements, const uint32_t* __restrict__ key,
+                          const uint32_t* __restrict__ vhat, uint32_t* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;  // (prime, leaf, l)
+  if (t >= nprimes * LEAVES * 4) return;
+  const int pi = t / (LEAVES * 4), s = (t / 4) % LEAVES, l = t % 4;
+  const uint64_t p = c_prime[pi].p;
+  uint64_t acc = 0;  // < 4 elements x p^2 < 2^30 per term: no overflow below 2^34 elements
+  for (uint64_t m = 0; m < elements; ++m) {
+    const uint32_t* M = key + (((size_t)pi * elements + m) * LEAVES + s) * 16;
+    const uint32_t* x = vhat + (((size_t)pi * elements + m) * 4) * LEAVES + s;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc += (uint64_t)M[4 * k + l] * x[k * LEAVES];
+  }
+  // K2's input layout with one element split: [split 0][prime][column 0][leaf][l]
+  out[((size_t)pi * COLUMNS) * LEAVES * 4 + s * 4 + l] = (uint32_t)(acc % p);
+}
+
+void launch_a_times_v(const ModulusPlan& mp, const Shape& sh, const int32_t* v, const uint32_t* key, uint32_t* vred,
+                      uint32_t* vhat, uint32_t* partial, uint8_t* out, cudaStream_t s) {
+  const uint64_t E = sh.ring_elements;
+  k_atv_reduce<<<1024, 256, 0, s>>>(mp.nprimes, E, v, vred);
+  const uint64_t total = (uint64_t)mp.nprimes * E * 4;
+  k_key_forward<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(mp.nprimes, E, vred, vhat);
+  const int threads = mp.nprimes * LEAVES * 4;
+  k_atv_mac<<<(threads + 127) / 128, 128, 0, s>>>(mp.nprimes, E, key, vhat, partial);
+  launch_commit_finish(mp, sh, partial, 1, out, s, 1);
+}
+
+// challenge_combination (rq.rs:226-256): raw[r] = sum_j sum_t sign_{j,t} C_j[r - 4 pos_{j,t}],
+// the challenge sitting in R_Q as c(-X^4), sign = (-1)^(sign bit + pos). One thread per raw index
+// and run of 32 columns; partial sums as signed 128-bit integers (|.| < 32 x 28 x 2^96),
+// [run][raw index] -> (lo, hi), added and folded into the ring by the host.
+__global__ void k_chcomb(const uint8_t* __restrict__ commit, uint32_t width, const Challenge* __restrict__ ch,
+                         unsigned long long* __restrict__ part) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int run = blockIdx.y;
+  if (r >= 2 * RING_N - 1) return;
+  __int128 acc = 0;
+  for (int j = 32 * run; j < 32 * run + 32; ++j) {
+    const Challenge c = ch[j];
+    for (uint32_t t = 0; t < c.weight; ++t) {
+      const int m = c.positions[t];
+      const int i = r - 4 * m;
+      if (i < 0 || i >= RING_N) continue;
+      const uint8_t* b = commit + ((size_t)j * RING_N + i) * width;
+      unsigned __int128 x = 0;
+      for (int k = (int)width - 1; k >= 0; --k) x = (x << 8) | b[k];
+      const bool neg = (((c.signs >> t) & 1) ^ (m & 1)) != 0;
+      acc += neg ? -(__int128)x : (__int128)x;
+    }
+  }
+  part[2 * ((size_t)run * (2 * RING_N - 1) + r)] = (unsigned long long)(unsigned __int128)acc;
+  part[2 * ((size_t)run * (2 * RING_N - 1) + r) + 1] = (unsigned long long)((unsigned __int128)acc >> 64);
+}
+
+void launch_challenge_combination(const uint8_t* commit, uint32_t width, const Challenge* ch,
+                                  unsigned long long* part, cudaStream_t s) {
+  k_chcomb<<<dim3((2 * RING_N - 1 + 127) / 128, COLUMNS / 32), 128, 0, s>>>(commit, width, ch, part);
 }
 
 }  // namespace lf

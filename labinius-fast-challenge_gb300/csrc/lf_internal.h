@@ -79,7 +79,8 @@ struct ModulusPlan {
 // Q = 3889 * 9721 * 17497 its three factors (CRT gives the value mod q directly); for any other
 // q, primes p = 1 (mod 486) below 2^15, largest first, until their product exceeds twice the
 // largest |coefficient| of the integer product (elements * 1296 * (q - 1)).
-bool make_modulus_plan(u128 q, uint64_t elements, ModulusPlan& mp, std::string& err);
+// extra_bits widens the bound (the verifier's a_times_v multiplies by |v| <= 2^15).
+bool make_modulus_plan(u128 q, uint64_t elements, int extra_bits, ModulusPlan& mp, std::string& err);
 
 struct ProveProfile {
   double key_ms, commit_ms, finish_ms, transcript_ms, partials_ms, switch_ms, row_ms, challenges_ms,
@@ -147,7 +148,13 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
 int commit_splits(uint64_t elements, int nprimes, int sms);
 void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint32_t* key,
                    const uint16_t* btiles, uint32_t* partial, int splits, int* status, cudaStream_t s);
-void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t* partial, int splits,
-                          uint8_t* out, cudaStream_t s);
+void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t* partial, int splits, uint8_t* out,
+                          cudaStream_t s, int ncols = COLUMNS);
+// Verifier pieces (lf_commit.cu): a_times_v into `out` (648 coefficients of `width` bytes) and
+// challenge_combination's partial sums [32 column runs][1295] as signed 128-bit (lo, hi).
+void launch_a_times_v(const ModulusPlan& mp, const Shape& sh, const int32_t* v, const uint32_t* key, uint32_t* vred,
+                      uint32_t* vhat, uint32_t* partial, uint8_t* out, cudaStream_t s);
+void launch_challenge_combination(const uint8_t* commit, uint32_t width, const Challenge* ch,
+                                  unsigned long long* part, cudaStream_t s);
 
 }  // namespace lf

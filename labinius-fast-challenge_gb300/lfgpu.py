@@ -17,8 +17,9 @@ LF_OK = 0
 ERRORS = {
     -1: "LF_E_ARGS", -2: "LF_E_SHAPE", -3: "LF_E_MODULUS", -4: "LF_E_TABLE_LEN", -5: "LF_E_CAP",
     -6: "LF_E_OOM", -7: "LF_E_CUDA", -8: "LF_E_INTERNAL", -9: "LF_E_ADMISSION", -10: "LF_E_LIMIT",
-    -11: "LF_E_TIMEOUT", -12: "LF_E_TICKET",
+    -11: "LF_E_TIMEOUT", -12: "LF_E_TICKET", -13: "LF_E_REJECT",
 }
+LF_E_REJECT = -13
 LF_E_TIMEOUT = -11
 NOALLOC_MAX_CHALLENGES = 4096
 EXPORTS = [
@@ -26,6 +27,7 @@ EXPORTS = [
     "lf_prove_device", "lf_write_table_device", "lf_device_alloc", "lf_device_free", "lf_memcpy_h2d",
     "lf_last_profile", "lf_strerror", "lf_last_error", "lf_last_challenges",
     "lf_sample_challenges", "lf_sample_challenges_noalloc", "lf_prove_batch", "lf_submit", "lf_poll",
+    "lf_verify", "lf_verify_device",
 ]
 
 
@@ -95,6 +97,8 @@ def load(path=LIB_PATH):
     lib.lf_last_error.restype = ctypes.c_char_p
     lib.lf_last_challenges.argtypes = [p, u8p, sz]
     lib.lf_sample_challenges.argtypes = [p, ctypes.c_char_p, ctypes.c_char_p, sz, ctypes.c_uint32, u8p]
+    lib.lf_verify.argtypes = [p, ctypes.c_char_p, ctypes.c_uint32, p, sz, ctypes.c_char_p, sz]
+    lib.lf_verify_device.argtypes = [p, ctypes.c_char_p, ctypes.c_uint32, p, ctypes.c_char_p, sz]
     lib.lf_prove_batch.argtypes = [p, sz, ctypes.POINTER(Job), ctypes.POINTER(Result)]
     lib.lf_submit.argtypes = [p, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_uint64)]
     lib.lf_poll.argtypes = [p, ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(Result)]
@@ -189,6 +193,32 @@ class Prover:
 
     def key_prepare(self, log_vars, q=BASELINE_Q):
         self._check(self.lib.lf_key_prepare(self.ctx, q_bytes(q), log_vars))
+
+    def verify(self, seed, proof, log_vars, table=None):
+        """(accepted, message) from the GPU checker. `table` is host bytes, or None to regenerate the
+        seed's table on the device. Errors other than a rejection raise."""
+        if table is None:
+            rc = self.lib.lf_verify(self.ctx, bytes(seed), log_vars, None, 0, bytes(proof), len(proof))
+        else:
+            mv = memoryview(table).cast("B")
+            buf = (ctypes.c_uint8 * len(mv)).from_buffer_copy(mv) if mv.readonly else (ctypes.c_uint8 * len(mv)).from_buffer(mv)
+            rc = self.lib.lf_verify(self.ctx, bytes(seed), log_vars, ctypes.cast(buf, ctypes.c_void_p), len(mv),
+                                    bytes(proof), len(proof))
+        if rc == LF_OK:
+            return True, ""
+        if rc == LF_E_REJECT:
+            return False, self.lib.lf_last_error(self.ctx).decode()
+        self._check(rc)
+
+    def verify_device(self, seed, proof, log_vars, table_dev):
+        """(accepted, message) from the GPU checker for a device-resident table."""
+        rc = self.lib.lf_verify_device(self.ctx, bytes(seed), log_vars, ctypes.c_void_p(table_dev), bytes(proof),
+                                       len(proof))
+        if rc == LF_OK:
+            return True, ""
+        if rc == LF_E_REJECT:
+            return False, self.lib.lf_last_error(self.ctx).decode()
+        self._check(rc)
 
     def make_job(self, seed, table, log_vars, q=BASELINE_Q, on_device=False, nbytes=None):
         """A job and the buffers it points to (kept alive on the returned object). `table` is bytes /
