@@ -78,17 +78,23 @@ int main(int argc, char** argv) {
   lf_ctx* ctx = nullptr;
   if (lf_ctx_create(&cfg, &ctx) != LF_OK) return die("no CUDA device");
   auto t2 = std::chrono::steady_clock::now();
+  // The proof is encoded straight into the output file, mapped and pre-faulted at its final size
+  // (the reference maps its output the same way, solution/proof_generate/src/main.rs:1427-1569).
   size_t cap = lf_proof_size(q_le, log_vars);
-  std::vector<uint8_t> proof(cap);
+  int pfd = open(proof_path.c_str(), O_RDWR | O_CREAT | O_TRUNC, 0644);
+  if (pfd < 0 || ftruncate(pfd, (off_t)cap) != 0) return die("write proof");
+  void* pmap = mmap(nullptr, cap, PROT_READ | PROT_WRITE, MAP_SHARED | MAP_POPULATE, pfd, 0);
+  if (pmap == MAP_FAILED) return die("write proof");
   size_t len = 0;
-  int rc = lf_prove(ctx, seed, q_le, log_vars, table, want, proof.data(), cap, &len);
+  int rc = lf_prove(ctx, seed, q_le, log_vars, table, want, static_cast<uint8_t*>(pmap), cap, &len);
   if (rc != LF_OK) {
     fprintf(stderr, "labinius-fast: %s: %s\n", lf_strerror(rc), lf_last_error(ctx));
+    unlink(proof_path.c_str());
     return 1;
   }
   auto t3 = std::chrono::steady_clock::now();
-  FILE* f = fopen(proof_path.c_str(), "wb");
-  if (!f || fwrite(proof.data(), 1, len, f) != len || fclose(f) != 0) return die("write proof");
+  if (len != cap && ftruncate(pfd, (off_t)len) != 0) return die("write proof");
+  if (munmap(pmap, cap) != 0 || close(pfd) != 0) return die("write proof");
   auto t4 = std::chrono::steady_clock::now();
   lf_profile p;
   lf_last_profile(ctx, &p);

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -214,6 +215,7 @@ struct lf_ctx {
   cudaEvent_t ev[16];
   // batches: a second table buffer and a copy stream, so the next table uploads during a proof
   DevBuf table2, fold_strips, fold_part;
+  lf_ctx* lane = nullptr;  // a second context on the same device for batches (own stream, buffers, keys)
   cudaStream_t upload_stream = nullptr;
   cudaEvent_t uploaded[2] = {nullptr, nullptr};
   // serving: FIFO of submitted jobs, drained by one worker thread
@@ -1225,6 +1227,7 @@ void lf_ctx_destroy(lf_ctx* ctx) {
   }
   ctx->qcv.notify_all();
   if (ctx->worker.joinable()) ctx->worker.join();
+  if (ctx->lane) lf_ctx_destroy(ctx->lane);
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   DevBuf* bufs[] = {&ctx->table, &ctx->stream_buf, &ctx->partial, &ctx->sblk, &ctx->ehi, &ctx->elo, &ctx->lo_planes,
@@ -1385,6 +1388,31 @@ int lf_sample_challenges_traced(lf_ctx* ctx, const char* domain, const uint8_t* 
   return LF_OK;
 }
 
+// One lane of a batch: takes the next job index until none is left, copies a host table on its
+// own stream and proves it.
+void batch_lane(lf_ctx* c, const lf_job* jobs, lf_result* results, const std::vector<int>& pre,
+                std::atomic<size_t>& next, size_t n, clk::time_point t_batch) {
+  cudaSetDevice(c->device);
+  for (size_t i = next++; i < n; i = next++) {
+    lf_result& r = results[i];
+    r = lf_result{};
+    const auto start = clk::now();
+    r.queue_ms = ms_between(t_batch, start);
+    const lf_job& j = jobs[i];
+    r.status = pre[i];
+    const uint4* table = reinterpret_cast<const uint4*>(j.table);
+    if (r.status == LF_OK && !j.table_on_device) {
+      if (c->table.ensure(j.table_bytes) != cudaSuccess ||
+          cudaMemcpyAsync(c->table.p, j.table, j.table_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+        r.status = fail(c, LF_E_CUDA, "table upload failed");
+      table = c->table.as<uint4>();
+    }
+    // (the caller holds the batch context's lock; the lane belongs to that context alone)
+    if (r.status == LF_OK) r.status = run_job(c, j, table, &r.proof_len);
+    r.run_ms = ms_between(start, clk::now());
+  }
+}
+
 int lf_prove_batch(lf_ctx* ctx, size_t n, const lf_job* jobs, lf_result* results) {
   if (!ctx || (n && (!jobs || !results))) return LF_E_ARGS;
   std::lock_guard<std::mutex> g(ctx->mu);
@@ -1395,13 +1423,34 @@ int lf_prove_batch(lf_ctx* ctx, size_t n, const lf_job* jobs, lf_result* results
     CK(cudaEventCreateWithFlags(&ctx->uploaded[1], cudaEventDisableTiming));
   }
   const auto t_batch = clk::now();
-  DevBuf* tb[2] = {&ctx->table, &ctx->table2};
   std::vector<int> pre(n, LF_OK);  // per-job check before any device work
+  bool baseline_only = n >= 2;
   for (size_t i = 0; i < n; ++i) {
     u128 q;
     Shape sh;
     pre[i] = check_job(ctx, jobs[i], q, sh);
+    if (pre[i] == LF_OK && q != (u128)3889 * 9721 * 17497) baseline_only = false;
   }
+  int first = LF_OK;
+  if (baseline_only) {
+    // Two lanes: small proofs wait on the host between switch rounds, so a second context on its
+    // own stream fills those gaps. Only under the baseline modulus, whose three primes are the
+    // same for every shape (the prime constants live in one constant bank per device).
+    if (!ctx->lane) {
+      lf_config cfg = {ctx->device, ctx->budget};
+      if (lf_ctx_create(&cfg, &ctx->lane) != LF_OK) ctx->lane = nullptr;
+    }
+    if (ctx->lane) {
+      std::atomic<size_t> next{0};
+      std::thread other(batch_lane, ctx->lane, jobs, results, std::cref(pre), std::ref(next), n, t_batch);
+      batch_lane(ctx, jobs, results, pre, next, n, t_batch);
+      other.join();
+      for (size_t i = 0; i < n; ++i)
+        if (results[i].status != LF_OK && first == LF_OK) first = results[i].status;
+      return first;
+    }
+  }
+  DevBuf* tb[2] = {&ctx->table, &ctx->table2};
   // Copy a host table into buffer b on the copy stream (job i), marking its completion.
   auto upload = [&](size_t i, int b) -> int {
     const lf_job& j = jobs[i];
@@ -1411,7 +1460,6 @@ int lf_prove_batch(lf_ctx* ctx, size_t n, const lf_job* jobs, lf_result* results
     CK(cudaEventRecord(ctx->uploaded[b], ctx->upload_stream));
     return LF_OK;
   };
-  int first = LF_OK;
   int up = n ? upload(0, 0) : LF_OK;
   for (size_t i = 0; i < n; ++i) {
     lf_result& r = results[i];
