@@ -277,21 +277,76 @@ def batched_leg(lfgpu, prover, n=32, seed=20260):
         hosts[i] = h
         jobs.append(prover.make_job(s, h.data_ptr(), lv, nbytes=h.numel()))
     torch.cuda.synchronize()
-    prover.prove_batch(jobs)  # keys for every shape, pages touched
+    prover.prove_batch(jobs)  # buffers of every lane grown, pages touched
+    for lv in sorted(set(shapes)):
+        prover.key_prepare(lv)  # every lane holds every shape's key
     t0 = time.perf_counter()
     res = prover.prove_batch(jobs)
     dt = time.perf_counter() - t0
     bad = [r.status for r in res if r.status != 0]
     if bad:
         raise RuntimeError(f"batched proofs failed: {bad}")
+    # the plain path on the same jobs: one lf_prove_batch call per job runs it alone on the
+    # context's own stream (host table uploaded, proven, proof downloaded), one after another
+    t1 = time.perf_counter()
+    for j in jobs:
+        r = prover.prove_batch([j])[0]
+        if r.status != 0:
+            raise RuntimeError(f"plain proof failed: {r.status}")
+    dt_plain = time.perf_counter() - t1
     return {"proofs_per_s": round(n / dt, 1), "jobs": n, "total_ms": round(dt * 1e3, 2),
-            "log_vars": shapes, "tables": "page-locked host memory, H2D inside the timed batch"}
+            "plain_proofs_per_s": round(n / dt_plain, 1), "vs_plain": round(dt_plain / dt, 2),
+            "lanes": prover.lanes or 4, "log_vars": shapes,
+            "tables": "page-locked host memory, H2D inside the timed batch"}
+
+
+def micro_leg(lfgpu, prover, stream):
+    """The kernel microbenchmark: 2^16 ring products in R_Q for the baseline prime product, Q = 2^64
+    and a three-prime Q near 2^93 (operands from the device's public-matrix expansion, uniform in
+    [0, Q)); 2^28 GHASH products of random pairs; a_times_v of the 4096-element matrix with v
+    uniform in [-2^10, 2^10]. Device time of each call (CUDA events on the prover's stream, median
+    of 3 after one warm call)."""
+    import torch
+
+    def med(fn):
+        fn(0)
+        return statistics.median(timed(stream, fn, 1) for _ in range(3))
+
+    out = {}
+    n = 1 << 16
+    half = 16 * 648 * n
+    ring = {}
+    for name, q in (("baseline", lfgpu.BASELINE_Q), ("2^64", 1 << 64),
+                    ("q93", 2147478481 * 2147449321 * 2147429881)):
+        m = torch.empty(2 * half, dtype=torch.uint8, device="cuda")
+        c = torch.empty(half, dtype=torch.uint8, device="cuda")
+        prover.ajtai_matrix_device(q, 2 * n, m.data_ptr())
+        ms = med(lambda i: prover.ring_mul(q, n, m.data_ptr(), m.data_ptr() + half, c.data_ptr()))
+        ring[name] = {"ms": round(ms, 3), "products_per_s": round(n / ms * 1e3), "gbs": round(3 * half / ms / 1e6, 1)}
+        del m, c
+    out["ring_products_2^16"] = ring
+    g = torch.Generator(device="cuda").manual_seed(5)
+    ng = 1 << 28
+    a = torch.randint(-2 ** 63, 2 ** 63 - 1, (2 * ng,), dtype=torch.int64, device="cuda", generator=g)
+    b = torch.randint(-2 ** 63, 2 ** 63 - 1, (2 * ng,), dtype=torch.int64, device="cuda", generator=g)
+    c = torch.empty_like(a)
+    torch.cuda.synchronize()
+    ms = med(lambda i: prover.ghash_mul(ng, a.data_ptr(), b.data_ptr(), c.data_ptr()))
+    out["ghash_2^28"] = {"ms": round(ms, 3), "products_per_s": round(ng / ms * 1e3), "gbs": round(48 * ng / ms / 1e6, 1)}
+    del a, b, c
+    v = torch.randint(-(1 << 10), (1 << 10) + 1, (4096 * 648,), dtype=torch.int16, device="cuda", generator=g)
+    torch.cuda.synchronize()
+    prover.a_times_v(lfgpu.BASELINE_Q, 4096, v.data_ptr())  # key build
+    ms = med(lambda i: prover.a_times_v(lfgpu.BASELINE_Q, 4096, v.data_ptr()))
+    out["a_times_v_4096"] = {"ms": round(ms, 3), "schoolbook_macs_per_s": round(4096 * 648 * 648 / ms * 1e3)}
+    return out
 
 
 def serving_leg(lfgpu, prover, requests=100, rate=8.0, seed=20261):
     """Poisson arrivals at `rate`/s, L uniform over the integers 22..31 (log-uniform table sizes),
     a fresh seed per request, one page-locked table per shape; latency = queueing + proving as
-    the server reports it. p50/p99 over the requests."""
+    the server reports it. p50/p99 over the requests, for the context's lanes and, on the same
+    arrivals, for a one-lane context (the plain one-at-a-time path behind the same queue)."""
     import random
 
     import torch
@@ -304,35 +359,44 @@ def serving_leg(lfgpu, prover, requests=100, rate=8.0, seed=20261):
         h.copy_(dev)
         pool[lv] = h
     torch.cuda.synchronize()
-    warm = [prover.make_job(seeds(1, 400 + lv)[0], pool[lv].data_ptr(), lv, nbytes=pool[lv].numel())
-            for lv in range(22, 32)]
-    prover.prove_batch(warm)  # keys for every shape
     arrivals, t = [], 0.0
     for _ in range(requests):
         t += rng.expovariate(rate)
         arrivals.append(t)
     shapes = [rng.randint(22, 31) for _ in range(requests)]
-    jobs, tickets = [], []
-    t0 = time.perf_counter()
-    for i, (at, lv) in enumerate(zip(arrivals, shapes)):
-        delay = at - (time.perf_counter() - t0)
-        if delay > 0:
-            time.sleep(delay)
-        j = prover.make_job(seeds(1, 1000 + i)[0], pool[lv].data_ptr(), lv, nbytes=pool[lv].numel())
-        jobs.append(j)
-        tickets.append(prover.submit(j))
-    lat = []
-    for t_ in tickets:
-        rc, r = prover.poll(t_, 120000)
-        if rc != 0 or r.status != 0:
-            raise RuntimeError(f"served request failed: {rc} {r.status}")
-        lat.append(r.queue_ms + r.run_ms)
-    wall = time.perf_counter() - t0
-    lat.sort()
-    pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))]
-    return {"p50_ms": round(pct(0.50), 3), "p99_ms": round(pct(0.99), 3), "requests": requests,
-            "rate_per_s": rate, "log_vars": "uniform 22..31", "wall_s": round(wall, 2),
-            "latency": "queue + prove, host tables (H2D included)"}
+
+    def run(p):
+        warm = [p.make_job(seeds(1, 400 + lv)[0], pool[lv].data_ptr(), lv, nbytes=pool[lv].numel())
+                for lv in [31] * 8 + list(range(22, 32))]
+        p.prove_batch(warm)  # every lane's buffers grown to the largest shape
+        for lv in range(22, 32):
+            p.key_prepare(lv)  # every lane holds every shape's key
+        jobs, tickets = [], []
+        t0 = time.perf_counter()
+        for i, (at, lv) in enumerate(zip(arrivals, shapes)):
+            delay = at - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            j = p.make_job(seeds(1, 1000 + i)[0], pool[lv].data_ptr(), lv, nbytes=pool[lv].numel())
+            jobs.append(j)
+            tickets.append(p.submit(j))
+        lat = []
+        for t_ in tickets:
+            rc, r = p.poll(t_, 120000)
+            if rc != 0 or r.status != 0:
+                raise RuntimeError(f"served request failed: {rc} {r.status}")
+            lat.append(r.queue_ms + r.run_ms)
+        wall = time.perf_counter() - t0
+        lat.sort()
+        pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))]
+        return round(pct(0.50), 3), round(pct(0.99), 3), round(requests / wall, 2), round(wall, 2)
+
+    p50, p99, pps, wall = run(prover)
+    with lfgpu.Prover(prover.device, lanes=1) as one:
+        p50_1, p99_1, _, _ = run(one)
+    return {"p50_ms": p50, "p99_ms": p99, "proofs_per_s": pps, "requests": requests, "rate_per_s": rate,
+            "lanes": prover.lanes or 4, "plain": {"p50_ms": p50_1, "p99_ms": p99_1, "lanes": 1},
+            "log_vars": "uniform 22..31", "wall_s": wall, "latency": "queue + prove, host tables (H2D included)"}
 
 
 def main():
@@ -349,6 +413,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched (lf_prove_batch) leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving (lf_submit/lf_poll) leg")
     ap.add_argument("--serve-requests", type=int, default=100, help="requests of the serving leg (Poisson, 8/s)")
+    ap.add_argument("--lanes", type=int, default=0, help="proofs in flight per context (0 = the library default)")
+    ap.add_argument("--no-micro", action="store_true", help="skip the ring / GHASH / a_times_v microbenchmark")
     args = ap.parse_args()
     rank, world, local = dist_init(args.gpus)
     if args.impl == "reference":
@@ -362,7 +428,7 @@ def main():
 
     log_vars = args.log_vars
     tbytes = (1 << log_vars) // 8
-    prover = lfgpu.Prover(local)
+    prover = lfgpu.Prover(local, lanes=args.lanes)
     stream = torch.cuda.ExternalStream(prover.stream())
     ss = seeds(args.tables, rank)
     tables = [device_table(prover, s, log_vars) for s in ss]
@@ -392,10 +458,13 @@ def main():
     value = ms_per_step / world
     med = {k: statistics.median(p[k] for p in profs) for k in profs[0]}
     phases = {k: round(v, 4) for k, v in med.items() if k.endswith("_ms")}
-    if args.no_e2e:
+    if args.no_e2e:  # a short line: the device-resident value, and the batched leg unless skipped
         if rank == 0:
-            print(json.dumps({"metric": METRIC, "value": round(value, 3), "unit": "ms/proof", "phases_ms": phases,
-                              "gpu_launches": int(med["launches"]) * args.steps, "clocks": clk.summary()}))
+            short = {"metric": METRIC, "value": round(value, 3), "unit": "ms/proof", "phases_ms": phases,
+                     "gpu_launches": int(med["launches"]) * args.steps, "clocks": clk.summary()}
+            if not args.no_batch:
+                short["batched"] = batched_leg(lfgpu, prover)
+            print(json.dumps(short))
         return
 
     # ---- e2e: pinned host table through lf_prove (H2D of the table and D2H of the proof timed) ----
@@ -441,6 +510,12 @@ def main():
             serving = serving_leg(lfgpu, prover, requests=args.serve_requests)
         except Exception as e:  # reported, not fatal
             serving = f"failed: {e}"
+    micro = None
+    if not args.no_micro:
+        try:
+            micro = micro_leg(lfgpu, prover, stream)
+        except Exception as e:  # reported, not fatal
+            micro = f"failed: {e}"
     cpu = None
     if not args.no_cpu:
         cms, cores = cpu_baseline(log_vars, bytes(host.numpy()), e2e_seed, proof)
@@ -463,6 +538,7 @@ def main():
         "verify_ms": round(vms, 3),
         "batched": batched,
         "serving": serving,
+        "micro": micro,
         "phases_ms": phases,
         "roofline": commit_roofline(log_vars, med["commit_ms"]),
         "cpu_baseline": cpu,

@@ -38,6 +38,8 @@ typedef struct lf_ctx lf_ctx;
 typedef struct lf_config {
   int device;             /* CUDA ordinal */
   size_t hbm_budget;      /* bytes the context may hold on the device; 0 = no limit */
+  int lanes;              /* proofs a batch or the serving queue may run at once, each on its own
+                             stream and host thread (1..8); 0 = the default, 4 */
 } lf_config;
 
 /* Per-phase device times of the last lf_prove* call on a context, in milliseconds
@@ -118,21 +120,30 @@ typedef struct lf_result {
   double run_ms;    /* start of the proof to its bytes in the proof buffer */
 } lf_result;
 
-/* Proves n independent jobs (any mix of shapes; each shape's key is built once and cached on
- * the context) in order on the context's GPU. The next job's host table is copied to the device
- * on a second stream while the current job is proven. results[i] receives job i's outcome;
- * the return value is LF_OK if every job succeeded, else the first failing job's code.
+/* Proves n independent jobs (any mix of shapes and moduli; each (Q, shape) key is built once and
+ * cached) on the context's GPU. With two or more jobs they run on the lanes of the context
+ * (lf_config.lanes, four by default: one stream and host thread each, taking jobs in order from
+ * one counter), so one proof's host work overlaps other proofs' kernels; with one lane the next
+ * job's host table is copied on a second stream while the current job is proven. results[i] receives job i's outcome; the return value
+ * is LF_OK if every job succeeded, else the first failing job's code.
  * The reference proves one table per process (solution/proof_generate/src/main.rs:2050-2090);
  * this is the batched form of that call. */
 int lf_prove_batch(lf_ctx* ctx, size_t n, const lf_job* jobs, lf_result* results);
 
-/* Serving: lf_submit queues a job (FIFO, one at a time on the context's GPU, on a worker thread
- * of the context) and returns a ticket; a job whose device footprint exceeds the context's HBM
- * budget is refused here with LF_E_ADMISSION. lf_poll waits up to wait_ms (0 = just look) for the
+/* Serving: lf_submit queues a job (FIFO) and returns a ticket. One worker thread per lane of the
+ * context (lf_config.lanes) takes requests from the queue: the front request starts when no
+ * other request is in flight or when the device footprints (lf_request_footprint) of those in
+ * flight and its own fit the context's HBM budget together, so requests that arrive while others
+ * are on the GPU overlap them as lanes and memory allow. A job whose own footprint exceeds the budget is refused here with LF_E_ADMISSION.
+ * lf_poll waits up to wait_ms (0 = just look) for the
  * ticket: LF_OK with *out filled (the ticket is then retired), LF_E_TIMEOUT while the job is
  * queued or running, LF_E_TICKET for an unknown ticket. lf_ctx_destroy completes the job in
  * progress and reports LF_E_INTERNAL for jobs still queued. No counterpart in the reference. */
 int lf_submit(lf_ctx* ctx, const lf_job* job, uint64_t* ticket);
+/* Device bytes one request of this shape and modulus holds while it is proven on this context's
+ * GPU (table copy when host_table, key, work buffers, transient key-build buffers): the figure
+ * admission compares with the budget. 0 for an unsupported shape or modulus. */
+size_t lf_request_footprint(lf_ctx* ctx, const uint8_t q_le[16], uint32_t log_vars, int host_table);
 int lf_poll(lf_ctx* ctx, uint64_t ticket, uint32_t wait_ms, lf_result* out);
 
 /* The checker (verifier/proof_verify/src/main.rs:293-409: check_proof_shape, check_field_switch,
@@ -143,6 +154,26 @@ int lf_verify(lf_ctx* ctx, const uint8_t seed[32], uint32_t log_vars, const void
               const uint8_t* proof, size_t proof_len);
 int lf_verify_device(lf_ctx* ctx, const uint8_t seed[32], uint32_t log_vars, const void* table_dev, const uint8_t* proof,
                      size_t proof_len);
+
+/* The arithmetic under the commitment, batched on the device (all pointers device memory; each
+ * call returns when its work is done on the context's stream).
+ *
+ * lf_ring_mul: c[i] = a[i] * b[i] in R_Q = Z_Q[X]/(X^648 - X^324 + 1) for i < n, elements of 648
+ * little-endian u128 coefficients in [0, Q), any 2 <= Q < 2^96: rq::mul and fold_into_ring
+ * (verifier/proof_verify/src/rq.rs:146-186) over many independent pairs. LF_E_ARGS if an operand
+ * coefficient is not below Q, LF_E_MODULUS outside the range.
+ * lf_ghash_mul: c[i] = a[i] * b[i] in GF(2^128) (GHASH, 16-byte little-endian elements;
+ * solution-arm/labinius/crates/pcs/src/fields/scalar.rs:61-72).
+ * lf_ajtai_matrix_device: rq::ajtai_matrix(Q, elements) (rq.rs:114-148), elements * 648 u128
+ * little-endian coefficients into out_dev.
+ * lf_a_times_v: rq::a_times_v (rq.rs:188-217) of ajtai_matrix(Q, elements) and the signed
+ * coefficients v_dev (elements * 648 int16), elements a power of two up to 2^15, 2 <= Q < 2^96;
+ * `out` (host) receives 648 u128 little-endian coefficients in [0, Q). The key of (Q, elements)
+ * is built on first use and cached with the proof keys. */
+int lf_ring_mul(lf_ctx* ctx, const uint8_t q_le[16], size_t n, const void* a_dev, const void* b_dev, void* c_dev);
+int lf_ghash_mul(lf_ctx* ctx, size_t n, const void* a_dev, const void* b_dev, void* c_dev);
+int lf_ajtai_matrix_device(lf_ctx* ctx, const uint8_t q_le[16], uint64_t elements, void* out_dev);
+int lf_a_times_v(lf_ctx* ctx, const uint8_t q_le[16], uint64_t elements, const int16_t* v_dev, uint8_t* out);
 
 /* Diagnostics: n folding challenges sampled on the device from Transcript::new(domain) after
  * absorb_bytes(prefix) (challenge.rs:240-259, 707-737), 40 bytes each as above. */

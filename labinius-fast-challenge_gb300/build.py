@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(OUT, "liblabinius_gpu.so")
 CLI = os.path.join(OUT, "labinius-fast")
-UNITS = ["lf_commit.cu", "lf_switch.cu", "lf_open.cu", "lf_api.cu"]
+UNITS = ["lf_commit.cu", "lf_switch.cu", "lf_open.cu", "lf_ring.cu", "lf_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

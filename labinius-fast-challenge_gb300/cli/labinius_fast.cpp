@@ -74,7 +74,7 @@ int main(int argc, char** argv) {
   if (table == MAP_FAILED) return die("map witness table");
   auto t1 = std::chrono::steady_clock::now();
 
-  lf_config cfg = {0, 0};
+  lf_config cfg = {0, 0, 1};
   lf_ctx* ctx = nullptr;
   if (lf_ctx_create(&cfg, &ctx) != LF_OK) return die("no CUDA device");
   auto t2 = std::chrono::steady_clock::now();

@@ -21,6 +21,7 @@
 #include "../../include/labinius_gpu.h"
 #include "lf_blake3.cuh"
 #include "lf_internal.h"
+#include "lf_ring.h"
 
 using namespace lf;
 
@@ -190,9 +191,18 @@ struct KeyCache {
   ModulusPlan mp;
   DevBuf key;     // u32 [prime][element][leaf][k][l]: the 4x4 base-multiplication matrix per leaf
   DevBuf btiles;  // bf16 [prime][third][64 x 256]: Vandermonde limbs of the commitment kernel
-  size_t bytes() const { return key.cap + btiles.cap; }
+  DevBuf consts;  // PrimeConst [prime]: the plan's per-prime constants, read by every kernel of the key
+  size_t bytes() const { return key.cap + btiles.cap + consts.cap; }
 };
 constexpr size_t MAX_KEYS = 12;  // shapes cached per context (log_vars 19..30 fit)
+
+// The factor-tree plan of one ring modulus for lf_ring_mul, with its prime constants on the device.
+struct RingCache {
+  u128 q = 0;
+  RingPlan plan;
+  DevBuf rps;
+};
+constexpr size_t MAX_RINGS = 8;
 
 }  // namespace
 
@@ -202,11 +212,12 @@ struct lf_ctx {
   size_t budget = 0;
   cudaStream_t stream = nullptr;
   std::mutex mu;
+  std::mutex errmu;  // err is written by worker threads and read by the caller
   std::string err;
   lf_profile prof{};
   std::vector<std::unique_ptr<KeyCache>> keys;  // per shape, least recently used evicted first
+  std::vector<std::unique_ptr<RingCache>> rings;  // lf_ring_mul plans, oldest evicted first
   KeyCache* key = nullptr;                      // the key of the proof in progress
-  const KeyCache* consts_of = nullptr;          // key whose prime constants are on the device
   uint64_t key_clock = 0;
   DevBuf table, stream_buf, partial, sblk, ehi, elo, lo_planes, rhi, vparts, psi, batch, soa, msg, p0, eqt, row,
       hasher, chal, fold, cvs, cvs_scratch, subtrees, status, phase, scratch_small, wbuf, rbuf;
@@ -215,20 +226,26 @@ struct lf_ctx {
   cudaEvent_t ev[16];
   // batches: a second table buffer and a copy stream, so the next table uploads during a proof
   DevBuf table2, fold_strips, fold_part;
-  lf_ctx* lane = nullptr;  // a second context on the same device for batches (own stream, buffers, keys)
+  int nlanes = 4;                // proofs in flight at once: this context and nlanes - 1 lanes
+  std::vector<lf_ctx*> lanes;    // contexts on the same device (own stream, buffers, keys)
+  std::mutex lanemu;             // guards lanes (created on first use, only added to)
+  bool is_lane = false;          // this context is another context's lane
   cudaStream_t upload_stream = nullptr;
   cudaEvent_t uploaded[2] = {nullptr, nullptr};
-  // serving: FIFO of submitted jobs, drained by one worker thread
+  // serving: FIFO of submitted jobs, drained by one worker thread per lane
   struct Queued {
     uint64_t ticket;
     lf_job job;
     std::chrono::steady_clock::time_point submitted;
+    size_t need;  // device footprint while in flight
   };
   struct Outcome {
     bool done = false;
     lf_result result{};
   };
-  std::thread worker;
+  std::vector<std::thread> workers;  // one per lane, this context first
+  int inflight = 0;             // requests being proven, and their footprint
+  size_t inflight_bytes = 0;
   std::mutex qmu;
   std::condition_variable qcv;
   std::deque<Queued> queue;
@@ -240,7 +257,10 @@ struct lf_ctx {
 namespace {
 
 int fail(lf_ctx* c, int code, const std::string& msg) {
-  if (c) c->err = msg;
+  if (c) {
+    std::lock_guard<std::mutex> g(c->errmu);
+    c->err = msg;
+  }
   return code;
 }
 
@@ -343,8 +363,10 @@ int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh, int extra_bits = 0) {
     CK(kc->key.ensure((size_t)mp.nprimes * E * LEAVES * 16 * 4));
     CK(kc->btiles.ensure(mp.btiles.size() * 2));
     CK(cudaMemcpyAsync(kc->btiles.p, mp.btiles.data(), mp.btiles.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
-    upload_prime_consts(mp, ctx->stream);
-    ctx->consts_of = nullptr;  // set below once the entry exists
+    CK(kc->consts.ensure(sizeof(PrimeConst) * mp.nprimes));
+    CK(cudaMemcpyAsync(kc->consts.p, mp.consts.data(), sizeof(PrimeConst) * mp.nprimes, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    mp.dconsts = kc->consts.as<PrimeConst>();
     launch_matrix_expand(mp, E, ared.as<uint32_t>(), ctx->stream);
     launch_key_transform(mp, E, ared.as<uint32_t>(), leaf.as<uint32_t>(), kc->key.as<uint32_t>(), ctx->stream);
     CKL("key build");
@@ -357,13 +379,8 @@ int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh, int extra_bits = 0) {
     kc->extra_bits = extra_bits;
     ctx->keys.push_back(std::move(kc));
     ctx->key = ctx->keys.back().get();
-    ctx->consts_of = ctx->key;
   }
   ctx->key->last_use = ++ctx->key_clock;
-  if (ctx->consts_of != ctx->key) {  // another key's primes are in the constant bank
-    upload_prime_consts(ctx->key->mp, ctx->stream);
-    ctx->consts_of = ctx->key;
-  }
   return LF_OK;
 }
 
@@ -718,44 +735,70 @@ int run_job(lf_ctx* ctx, const lf_job& j, const uint4* table_dev, size_t* proof_
   return prove_device(ctx, j.seed, q, sh, table_dev, j.proof, proof_len);
 }
 
-void serve_loop(lf_ctx* ctx) {
+// One serving lane: `c` (the owner or one of its lanes) proves requests from the owner's FIFO. The front
+// request starts when no request is in flight or when the footprints of those in flight and its
+// own fit the device-memory budget, so a second request overlaps the first on the device while
+// memory allows.
+void serve_loop(lf_ctx* owner, lf_ctx* c) {
   for (;;) {
     lf_ctx::Queued item;
     {
-      std::unique_lock<std::mutex> lk(ctx->qmu);
-      ctx->qcv.wait(lk, [&] { return ctx->stopping || !ctx->queue.empty(); });
-      if (ctx->queue.empty()) return;
-      item = ctx->queue.front();
-      ctx->queue.pop_front();
+      std::unique_lock<std::mutex> lk(owner->qmu);
+      owner->qcv.wait(lk, [&] {
+        if (owner->stopping) return true;
+        if (owner->queue.empty()) return false;
+        return owner->inflight == 0 || owner->budget == 0 ||
+               owner->inflight_bytes + owner->queue.front().need <= owner->budget;
+      });
+      if (owner->queue.empty()) return;
+      item = owner->queue.front();
+      owner->queue.pop_front();
+      ++owner->inflight;
+      owner->inflight_bytes += item.need;
     }
     lf_result r{};
     const auto start = clk::now();
     r.queue_ms = ms_between(item.submitted, start);
     {
-      std::lock_guard<std::mutex> g(ctx->mu);
+      std::lock_guard<std::mutex> g(c->mu);
       const lf_job& j = item.job;
       const uint4* table = reinterpret_cast<const uint4*>(j.table);
       r.status = LF_OK;
       if (!j.table_on_device) {
         Shape sh;
         if (sh.set(j.log_vars) && j.table_bytes == sh.words * 16) {
-          cudaSetDevice(ctx->device);
-          if (ctx->table.ensure(j.table_bytes) != cudaSuccess ||
-              cudaMemcpyAsync(ctx->table.p, j.table, j.table_bytes, cudaMemcpyHostToDevice, ctx->stream) !=
-                  cudaSuccess)
-            r.status = fail(ctx, LF_E_CUDA, "table upload failed");
-          table = ctx->table.as<uint4>();
+          cudaSetDevice(c->device);
+          if (c->table.ensure(j.table_bytes) != cudaSuccess ||
+              cudaMemcpyAsync(c->table.p, j.table, j.table_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+            r.status = fail(c, LF_E_CUDA, "table upload failed");
+          table = c->table.as<uint4>();
         }
       }
-      if (r.status == LF_OK) r.status = run_job(ctx, j, table, &r.proof_len);
+      if (r.status == LF_OK) r.status = run_job(c, j, table, &r.proof_len);
     }
     r.run_ms = ms_between(start, clk::now());
     {
-      std::lock_guard<std::mutex> lk(ctx->qmu);
-      ctx->outcomes[item.ticket] = lf_ctx::Outcome{true, r};
+      std::lock_guard<std::mutex> lk(owner->qmu);
+      owner->outcomes[item.ticket] = lf_ctx::Outcome{true, r};
+      --owner->inflight;
+      owner->inflight_bytes -= item.need;
     }
-    ctx->qcv.notify_all();
+    owner->qcv.notify_all();
   }
+}
+
+// The context's other lanes, created on first use with the same device and budget (fewer when
+// one cannot be made; the caller then runs on those there are, the context itself included).
+std::vector<lf_ctx*> lanes_of(lf_ctx* ctx) {
+  std::lock_guard<std::mutex> g(ctx->lanemu);
+  while (!ctx->is_lane && (int)ctx->lanes.size() + 1 < ctx->nlanes) {
+    lf_config cfg = {ctx->device, ctx->budget, 1};
+    lf_ctx* l = nullptr;
+    if (lf_ctx_create(&cfg, &l) != LF_OK) break;
+    l->is_lane = true;
+    ctx->lanes.push_back(l);
+  }
+  return ctx->lanes;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1182,6 +1225,11 @@ int lf_ctx_create(const lf_config* cfg, lf_ctx** out) {
   lf_ctx* ctx = new lf_ctx();
   ctx->device = cfg ? cfg->device : 0;
   ctx->budget = cfg ? cfg->hbm_budget : 0;
+  if (cfg && (cfg->lanes < 0 || cfg->lanes > 8)) {
+    delete ctx;
+    return LF_E_ARGS;
+  }
+  ctx->nlanes = cfg && cfg->lanes ? cfg->lanes : 4;
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) {
     delete ctx;
@@ -1226,8 +1274,9 @@ void lf_ctx_destroy(lf_ctx* ctx) {
     ctx->stopping = true;
   }
   ctx->qcv.notify_all();
-  if (ctx->worker.joinable()) ctx->worker.join();
-  if (ctx->lane) lf_ctx_destroy(ctx->lane);
+  for (auto& w : ctx->workers)
+    if (w.joinable()) w.join();
+  for (lf_ctx* l : ctx->lanes) lf_ctx_destroy(l);
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   DevBuf* bufs[] = {&ctx->table, &ctx->stream_buf, &ctx->partial, &ctx->sblk, &ctx->ehi, &ctx->elo, &ctx->lo_planes,
@@ -1270,7 +1319,14 @@ int lf_key_prepare(lf_ctx* ctx, const uint8_t q_le[16], uint32_t log_vars) {
   u128 q = q_from_le(q_le);
   if (!accept_modulus(q, s)) return fail(ctx, LF_E_MODULUS, "invalid commitment modulus");
   cudaSetDevice(ctx->device);
-  return ensure_key(ctx, q, s);
+  int rc = ensure_key(ctx, q, s);
+  for (lf_ctx* l : lanes_of(ctx)) {  // each lane keeps its own copy of the key
+    if (rc != LF_OK) break;
+    std::lock_guard<std::mutex> gl(l->mu);
+    rc = ensure_key(l, q, s);
+    if (rc) fail(ctx, rc, lf_last_error(l));
+  }
+  return rc;
 }
 
 int lf_prove_device(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars,
@@ -1390,8 +1446,12 @@ int lf_sample_challenges_traced(lf_ctx* ctx, const char* domain, const uint8_t* 
 
 // One lane of a batch: takes the next job index until none is left, copies a host table on its
 // own stream and proves it.
-void batch_lane(lf_ctx* c, const lf_job* jobs, lf_result* results, const std::vector<int>& pre,
+void batch_lane(lf_ctx* c, bool lock, const lf_job* jobs, lf_result* results, const std::vector<int>& pre,
                 std::atomic<size_t>& next, size_t n, clk::time_point t_batch) {
+  // The batch's own context is locked by the caller; a lane is locked here (a serving worker may
+  // share it).
+  std::unique_lock<std::mutex> g(c->mu, std::defer_lock);
+  if (lock) g.lock();
   cudaSetDevice(c->device);
   for (size_t i = next++; i < n; i = next++) {
     lf_result& r = results[i];
@@ -1407,7 +1467,6 @@ void batch_lane(lf_ctx* c, const lf_job* jobs, lf_result* results, const std::ve
         r.status = fail(c, LF_E_CUDA, "table upload failed");
       table = c->table.as<uint4>();
     }
-    // (the caller holds the batch context's lock; the lane belongs to that context alone)
     if (r.status == LF_OK) r.status = run_job(c, j, table, &r.proof_len);
     r.run_ms = ms_between(start, clk::now());
   }
@@ -1424,27 +1483,23 @@ int lf_prove_batch(lf_ctx* ctx, size_t n, const lf_job* jobs, lf_result* results
   }
   const auto t_batch = clk::now();
   std::vector<int> pre(n, LF_OK);  // per-job check before any device work
-  bool baseline_only = n >= 2;
   for (size_t i = 0; i < n; ++i) {
     u128 q;
     Shape sh;
     pre[i] = check_job(ctx, jobs[i], q, sh);
-    if (pre[i] == LF_OK && q != (u128)3889 * 9721 * 17497) baseline_only = false;
   }
   int first = LF_OK;
-  if (baseline_only) {
-    // Two lanes: small proofs wait on the host between switch rounds, so a second context on its
-    // own stream fills those gaps. Only under the baseline modulus, whose three primes are the
-    // same for every shape (the prime constants live in one constant bank per device).
-    if (!ctx->lane) {
-      lf_config cfg = {ctx->device, ctx->budget};
-      if (lf_ctx_create(&cfg, &ctx->lane) != LF_OK) ctx->lane = nullptr;
-    }
-    if (ctx->lane) {
+  if (n >= 2) {
+    // Lanes: a proof waits on the host between switch rounds and for its downloads, so other
+    // contexts on their own streams fill those gaps with the next jobs.
+    const std::vector<lf_ctx*> lanes = lanes_of(ctx);
+    if (!lanes.empty()) {
       std::atomic<size_t> next{0};
-      std::thread other(batch_lane, ctx->lane, jobs, results, std::cref(pre), std::ref(next), n, t_batch);
-      batch_lane(ctx, jobs, results, pre, next, n, t_batch);
-      other.join();
+      std::vector<std::thread> others;
+      for (size_t k = 0; k < lanes.size() && k + 1 < n; ++k)
+        others.emplace_back(batch_lane, lanes[k], true, jobs, results, std::cref(pre), std::ref(next), n, t_batch);
+      batch_lane(ctx, false, jobs, results, pre, next, n, t_batch);
+      for (auto& t : others) t.join();
       for (size_t i = 0; i < n; ++i)
         if (results[i].status != LF_OK && first == LF_OK) first = results[i].status;
       return first;
@@ -1487,21 +1542,34 @@ int lf_prove_batch(lf_ctx* ctx, size_t n, const lf_job* jobs, lf_result* results
 
 int lf_submit(lf_ctx* ctx, const lf_job* job, uint64_t* ticket) {
   if (!ctx || !job || !ticket) return LF_E_ARGS;
-  {
-    std::lock_guard<std::mutex> g(ctx->mu);
-    u128 q;
-    Shape sh;
-    int rc = check_job(ctx, *job, q, sh);
-    if (rc) return rc;
-  }
+  // Checked without the context's lock, which a worker holds while it proves: the checks read
+  // only what is fixed at creation (budget, SM count).
+  u128 q;
+  Shape sh;
+  int rc = check_job(ctx, *job, q, sh);
+  if (rc) return rc;
+  const size_t need = proof_footprint(sh, !job->table_on_device, ctx->sms, primes_for(q, sh));
+  const std::vector<lf_ctx*> lanes = lanes_of(ctx);
   std::lock_guard<std::mutex> lk(ctx->qmu);
   if (ctx->stopping) return LF_E_ARGS;
   *ticket = ctx->next_ticket++;
   ctx->outcomes[*ticket] = lf_ctx::Outcome{};
-  ctx->queue.push_back(lf_ctx::Queued{*ticket, *job, clk::now()});
-  if (!ctx->worker.joinable()) ctx->worker = std::thread(serve_loop, ctx);
+  ctx->queue.push_back(lf_ctx::Queued{*ticket, *job, clk::now(), need});
+  if (ctx->workers.empty()) {
+    ctx->workers.emplace_back(serve_loop, ctx, ctx);
+    for (lf_ctx* l : lanes) ctx->workers.emplace_back(serve_loop, ctx, l);
+  }
   ctx->qcv.notify_all();
   return LF_OK;
+}
+
+size_t lf_request_footprint(lf_ctx* ctx, const uint8_t q_le[16], uint32_t log_vars, int host_table) {
+  if (!ctx || !q_le) return 0;
+  Shape sh;
+  if (!sh.set(log_vars) || sh.lp < 12) return 0;
+  const u128 q = q_from_le(q_le);
+  if (!accept_modulus(q, sh)) return 0;
+  return proof_footprint(sh, host_table != 0, ctx->sms, primes_for(q, sh));
 }
 
 int lf_poll(lf_ctx* ctx, uint64_t ticket, uint32_t wait_ms, lf_result* out) {
@@ -1536,6 +1604,95 @@ int lf_sample_challenges_noalloc(int device, const char* domain, const uint8_t* 
     rc = noalloc_sample(d, domain, prefix, prefix_len, n, out, static_cast<cudaStream_t>(stream));
   cudaSetDevice(prev);
   return rc;
+}
+
+int lf_ring_mul(lf_ctx* ctx, const uint8_t q_le[16], size_t n, const void* a_dev, const void* b_dev, void* c_dev) {
+  if (!ctx || !q_le || (n && (!a_dev || !b_dev || !c_dev))) return fail(ctx, LF_E_ARGS, "null argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaSetDevice(ctx->device);
+  const u128 q = q_from_le(q_le);
+  RingCache* rc = nullptr;
+  for (auto& r : ctx->rings)
+    if (r->q == q) rc = r.get();
+  if (!rc) {
+    std::unique_ptr<RingCache> r(new RingCache());
+    std::string e;
+    if (!make_ring_plan(q, r->plan, e)) return fail(ctx, LF_E_MODULUS, e);
+    CK(r->rps.ensure(sizeof(RingPrimeDev) * r->plan.dev.size()));
+    CK(cudaMemcpyAsync(r->rps.p, r->plan.dev.data(), sizeof(RingPrimeDev) * r->plan.dev.size(),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    r->q = q;
+    if (ctx->rings.size() >= MAX_RINGS) ctx->rings.erase(ctx->rings.begin());
+    ctx->rings.push_back(std::move(r));
+    rc = ctx->rings.back().get();
+  }
+  if (!n) return LF_OK;
+  CK(ctx->status.ensure(16));
+  CK(cudaMemsetAsync(ctx->status.p, 0, 16, ctx->stream));
+  launch_ring_mul(rc->plan, rc->rps.as<RingPrimeDev>(), a_dev, b_dev, c_dev, n, ctx->status.as<int>(), ctx->stream);
+  CKL("ring products");
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, ctx->status.p, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (st & 1) return fail(ctx, LF_E_ARGS, "an operand coefficient is not below q");
+  return LF_OK;
+}
+
+int lf_ghash_mul(lf_ctx* ctx, size_t n, const void* a_dev, const void* b_dev, void* c_dev) {
+  if (!ctx || (n && (!a_dev || !b_dev || !c_dev))) return fail(ctx, LF_E_ARGS, "null argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaSetDevice(ctx->device);
+  launch_ghash_mul(a_dev, b_dev, c_dev, n, ctx->sms, ctx->stream);
+  CKL("GHASH products");
+  CK(cudaStreamSynchronize(ctx->stream));
+  return LF_OK;
+}
+
+int lf_ajtai_matrix_device(lf_ctx* ctx, const uint8_t q_le[16], uint64_t elements, void* out_dev) {
+  if (!ctx || !q_le || (elements && !out_dev)) return fail(ctx, LF_E_ARGS, "null argument");
+  const u128 q = q_from_le(q_le);
+  if (q < 2) return fail(ctx, LF_E_MODULUS, "a modulus is at least 2");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaSetDevice(ctx->device);
+  if (!elements) return LF_OK;
+  launch_matrix_raw(q, elements, out_dev, ctx->stream);
+  CKL("matrix expansion");
+  CK(cudaStreamSynchronize(ctx->stream));
+  return LF_OK;
+}
+
+int lf_a_times_v(lf_ctx* ctx, const uint8_t q_le[16], uint64_t elements, const int16_t* v_dev, uint8_t* out) {
+  if (!ctx || !q_le || !v_dev || !out) return fail(ctx, LF_E_ARGS, "null argument");
+  int lg = 0;
+  while (lg < 16 && ((uint64_t)1 << lg) < elements) ++lg;
+  if (elements == 0 || ((uint64_t)1 << lg) != elements || lg > 15)
+    return fail(ctx, LF_E_SHAPE, "elements must be a power of two up to 2^15");
+  Shape sh;
+  sh.set((uint32_t)(19 + lg));  // the proof shape whose columns have `elements` ring elements
+  const u128 q = q_from_le(q_le);
+  if (q < 2 || q >> 96) return fail(ctx, LF_E_MODULUS, "a_times_v covers moduli in [2, 2^96)");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaSetDevice(ctx->device);
+  int rc = ensure_key(ctx, q, sh, 15);  // |v| <= 2^15
+  if (rc) return rc;
+  const ModulusPlan& mp = ctx->key->mp;
+  const size_t nv = (size_t)elements * RING_N, w = mp.width;
+  DevBuf v32, vred, vhat, part, atv;
+  CK(v32.ensure(4 * nv));
+  CK(vred.ensure((size_t)mp.nprimes * nv * 4));
+  CK(vhat.ensure((size_t)mp.nprimes * elements * 4 * LEAVES * 4));
+  CK(part.ensure((size_t)mp.nprimes * COLUMNS * LEAVES * 16));
+  CK(atv.ensure(RING_N * w + 64));
+  launch_widen_i16(v_dev, v32.as<int32_t>(), nv, ctx->stream);
+  launch_a_times_v(mp, sh, v32.as<int32_t>(), ctx->key->key.as<uint32_t>(), vred.as<uint32_t>(), vhat.as<uint32_t>(),
+                   part.as<uint32_t>(), atv.as<uint8_t>(), ctx->stream);
+  CKL("a_times_v");
+  std::vector<uint8_t> packed(RING_N * w);
+  CK(cudaMemcpyAsync(packed.data(), atv.p, RING_N * w, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  memset(out, 0, RING_N * 16);
+  for (int i = 0; i < RING_N; ++i) memcpy(out + 16 * i, packed.data() + w * i, w);
+  return LF_OK;
 }
 
 int lf_verify_device(lf_ctx* ctx, const uint8_t seed[32], uint32_t log_vars, const void* table_dev, const uint8_t* proof,
@@ -1598,6 +1755,12 @@ const char* lf_strerror(int code) {
   }
 }
 
-const char* lf_last_error(lf_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+const char* lf_last_error(lf_ctx* ctx) {
+  if (!ctx) return "no context";
+  thread_local std::string copy;  // valid until this thread's next call
+  std::lock_guard<std::mutex> g(ctx->errmu);
+  copy = ctx->err;
+  return copy.c_str();
+}
 
 }  // extern "C"

@@ -23,7 +23,6 @@
 
 namespace lf {
 
-__constant__ PrimeConst c_prime[MAX_PRIMES];
 
 // Shape of K1 on the tensor cores (the kernel is described where it is defined).
 constexpr int TC_COLS = 128;                         // table columns per block (MMA M)
@@ -189,9 +188,6 @@ bool make_modulus_plan(u128 q, uint64_t elements, int extra_bits, ModulusPlan& m
   return true;
 }
 
-void upload_prime_consts(const ModulusPlan& mp, cudaStream_t s) {
-  cudaMemcpyToSymbolAsync(c_prime, mp.consts.data(), sizeof(PrimeConst) * mp.nprimes, 0, cudaMemcpyHostToDevice, s);
-}
 
 // ------------------------------------------------------------------------------------------------
 // Device arithmetic modulo a prime below 2^15
@@ -219,7 +215,8 @@ struct MatrixArgs {
   uint32_t two64[MAX_PRIMES];  // 2^64 mod p
 };
 
-__global__ void k_matrix_expand(MatrixArgs a, uint64_t elements, uint32_t* ared) {
+// With `raw` set, the coefficients themselves are written (u128 little-endian), else their residues.
+__global__ void k_matrix_expand(MatrixArgs a, uint64_t elements, uint32_t* ared, uint4* raw) {
   uint64_t m = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (m >= elements) return;
   bk::Hasher h;
@@ -256,6 +253,10 @@ __global__ void k_matrix_expand(MatrixArgs a, uint64_t elements, uint32_t* ared)
       if (v < q) break;
     }
     uint64_t lo = (uint64_t)v, hi = (uint64_t)(v >> 64);
+    if (raw) {
+      raw[m * RING_N + t] = make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
+      continue;
+    }
     for (int i = 0; i < a.nprimes; ++i) {
       uint64_t p = a.primes[i];
       uint64_t r = ((hi % p) * a.two64[i] + lo % p) % p;
@@ -277,7 +278,19 @@ void launch_matrix_expand(const ModulusPlan& mp, uint64_t elements, uint32_t* ar
     a.two64[i] = (uint32_t)powmod(powmod(2, 32, mp.primes[i]), 2, mp.primes[i]);
   }
   int threads = 64;
-  k_matrix_expand<<<(unsigned)((elements + threads - 1) / threads), threads, 0, s>>>(a, elements, ared);
+  k_matrix_expand<<<(unsigned)((elements + threads - 1) / threads), threads, 0, s>>>(a, elements, ared, nullptr);
+}
+
+void launch_matrix_raw(u128 q, uint64_t elements, void* out, cudaStream_t s) {
+  MatrixArgs a;
+  memset(&a, 0, sizeof a);
+  a.q_lo = (uint64_t)q;
+  a.q_hi = (uint64_t)(q >> 64);
+  a.bits = bits_of(q - 1);
+  a.width = (a.bits + 7) / 8;
+  int threads = 64;
+  k_matrix_expand<<<(unsigned)((elements + threads - 1) / threads), threads, 0, s>>>(a, elements, nullptr,
+                                                                                     reinterpret_cast<uint4*>(out));
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -309,7 +322,8 @@ __device__ void forward162(uint32_t* x, const PrimeConst& P) {
   }
 }
 
-__global__ void k_key_forward(int nprimes, uint64_t elements, const uint32_t* ared, uint32_t* leafvals) {
+__global__ void k_key_forward(const PrimeConst* __restrict__ pcs, int nprimes, uint64_t elements, const uint32_t* ared,
+                              uint32_t* leafvals) {
   uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   uint64_t total = (uint64_t)nprimes * elements * 4;
   if (tid >= total) return;
@@ -319,19 +333,20 @@ __global__ void k_key_forward(int nprimes, uint64_t elements, const uint32_t* ar
   const uint32_t* a = ared + ((size_t)pi * elements + m) * RING_N;
   uint32_t x[LEAVES];
   for (int p = 0; p < LEAVES; ++p) x[p] = a[4 * p + k];
-  forward162(x, c_prime[pi]);
+  forward162(x, pcs[pi]);
   uint32_t* o = leafvals + (((size_t)pi * elements + m) * 4 + k) * LEAVES;
   for (int s = 0; s < LEAVES; ++s) o[s] = x[s];
 }
 
-__global__ void k_key_leafform(int nprimes, uint64_t elements, const uint32_t* leafvals, uint32_t* key) {
+__global__ void k_key_leafform(const PrimeConst* __restrict__ pcs, int nprimes, uint64_t elements,
+                               const uint32_t* leafvals, uint32_t* key) {
   uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   uint64_t total = (uint64_t)nprimes * elements * LEAVES;
   if (tid >= total) return;
   int s = (int)(tid % LEAVES);
   uint64_t m = (tid / LEAVES) % elements;
   int pi = (int)(tid / LEAVES / elements);
-  const PrimeConst& P = c_prime[pi];
+  const PrimeConst& P = pcs[pi];
   const uint64_t p = P.p, c = P.leaf_root[s];
   const uint32_t* lv = leafvals + ((size_t)pi * elements + m) * 4 * LEAVES;
   uint64_t A[4];
@@ -344,9 +359,9 @@ __global__ void k_key_leafform(int nprimes, uint64_t elements, const uint32_t* l
 void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32_t* ared, uint32_t* leafvals,
                           uint32_t* key, cudaStream_t s) {
   uint64_t t1 = (uint64_t)mp.nprimes * elements * 4;
-  k_key_forward<<<(unsigned)((t1 + 127) / 128), 128, 0, s>>>(mp.nprimes, elements, ared, leafvals);
+  k_key_forward<<<(unsigned)((t1 + 127) / 128), 128, 0, s>>>(mp.dconsts, mp.nprimes, elements, ared, leafvals);
   uint64_t t2 = (uint64_t)mp.nprimes * elements * LEAVES;
-  k_key_leafform<<<(unsigned)((t2 + 127) / 128), 128, 0, s>>>(mp.nprimes, elements, leafvals, key);
+  k_key_leafform<<<(unsigned)((t2 + 127) / 128), 128, 0, s>>>(mp.dconsts, mp.nprimes, elements, leafvals, key);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -399,7 +414,8 @@ static double commit_bit_value(int kappa) {
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_commit_tc(const uint4* __restrict__ table, const uint32_t* __restrict__ key, const uint4* __restrict__ btiles,
-                uint32_t* __restrict__ partial, int rl, int elements, int per_split, int nprimes, int* status) {
+                const PrimeConst* __restrict__ pcs, uint32_t* __restrict__ partial, int rl, int elements,
+                int per_split, int nprimes, int* status) {
   extern __shared__ __align__(1024) uint8_t tsm[];
   uint8_t* sA = tsm;
   uint8_t* sB = tsm + 4 * TC_A_BYTES;
@@ -414,8 +430,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int m_begin = split * per_split;
   const int nelem = max(0, min(elements, m_begin + per_split) - m_begin);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const PrimeConst& P = c_prime[pi];
-  const uint32_t p = P.p;
+  const uint32_t p = pcs[pi].p, bar = pcs[pi].bar;
+  const int reduce_every = (int)pcs[pi].reduce_every;
 
   if (tid == 0) {
     *abort_flag = 0;
@@ -546,12 +562,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             acc[i][3] += kv.w * ri;
           }
         }
-        if (++since == (int)P.reduce_every) {
+        if (++since == reduce_every) {
           since = 0;
 #pragma unroll
           for (int i = 0; i < 9; ++i)
 #pragma unroll
-            for (int l = 0; l < 4; ++l) acc[i][l] = (int)reduce32((uint32_t)acc[i][l] + bias, P.bar, p);
+            for (int l = 0; l < 4; ++l) acc[i][l] = (int)reduce32((uint32_t)acc[i][l] + bias, bar, p);
         }
       }
     }
@@ -562,10 +578,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
       for (int i = 0; i < 9; ++i) {
         uint4 o;
-        o.x = reduce32((uint32_t)acc[i][0] + bias, P.bar, p);
-        o.y = reduce32((uint32_t)acc[i][1] + bias, P.bar, p);
-        o.z = reduce32((uint32_t)acc[i][2] + bias, P.bar, p);
-        o.w = reduce32((uint32_t)acc[i][3] + bias, P.bar, p);
+        o.x = reduce32((uint32_t)acc[i][0] + bias, bar, p);
+        o.y = reduce32((uint32_t)acc[i][1] + bias, bar, p);
+        o.z = reduce32((uint32_t)acc[i][2] + bias, bar, p);
+        o.w = reduce32((uint32_t)acc[i][3] + bias, bar, p);
         reinterpret_cast<uint4*>(out)[i] = o;
       }
     }
@@ -643,8 +659,8 @@ void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, c
     attr = true;
   }
   dim3 grid(mp.nprimes * 3, COLUMNS / TC_COLS, splits);
-  k_commit_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(table, key, reinterpret_cast<const uint4*>(btiles), partial, sh.rl,
-                                                 elements, per, mp.nprimes, status);
+  k_commit_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(table, key, reinterpret_cast<const uint4*>(btiles), mp.dconsts, partial,
+                                                 sh.rl, elements, per, mp.nprimes, status);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -661,8 +677,8 @@ struct FinishArgs {
   uint32_t ginv[MAX_PRIMES][MAX_PRIMES];
 };
 
-__global__ void __launch_bounds__(256) k_commit_finish(FinishArgs a, const uint32_t* __restrict__ partial,
-                                                       uint8_t* __restrict__ out) {
+__global__ void __launch_bounds__(256) k_commit_finish(FinishArgs a, const PrimeConst* __restrict__ pcs,
+                                                       const uint32_t* __restrict__ partial, uint8_t* __restrict__ out) {
   __shared__ uint32_t v[MAX_PRIMES][4][LEAVES];
   const int col = blockIdx.x;
   for (int e = threadIdx.x; e < a.nprimes * 4 * LEAVES; e += blockDim.x) {
@@ -680,7 +696,7 @@ __global__ void __launch_bounds__(256) k_commit_finish(FinishArgs a, const uint3
     for (int e = threadIdx.x; e < a.nprimes * 4 * per_t; e += blockDim.x) {
       int pi = e / (4 * per_t), rem = e % (4 * per_t), l = rem / per_t, r2 = rem % per_t;
       int n = r2 / sub, q = r2 % sub;
-      const PrimeConst& P = c_prime[pi];
+      const PrimeConst& P = pcs[pi];
       const uint64_t p = P.p;
       uint32_t* x = v[pi][l];
       int o = n * len + q;
@@ -698,7 +714,7 @@ __global__ void __launch_bounds__(256) k_commit_finish(FinishArgs a, const uint3
   }
   for (int e = threadIdx.x; e < a.nprimes * 4 * 81; e += blockDim.x) {
     int pi = e / (4 * 81), rem = e % (4 * 81), l = rem / 81, j = rem % 81;
-    const PrimeConst& P = c_prime[pi];
+    const PrimeConst& P = pcs[pi];
     const uint64_t p = P.p;
     uint32_t* x = v[pi][l];
     uint64_t u = x[j], w = x[j + 81];
@@ -758,7 +774,7 @@ void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t
     a.half[i] = mp.half_digits[i];
     for (int j = 0; j < i; ++j) a.ginv[i][j] = mp.garner_inv[i][j];
   }
-  k_commit_finish<<<ncols, 256, 0, s>>>(a, partial, out);
+  k_commit_finish<<<ncols, 256, 0, s>>>(a, mp.dconsts, partial, out);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -767,22 +783,23 @@ void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t
 // key's 4x4 matrices summed over the elements (one thread per prime, leaf and coefficient l),
 // then K2 on that single column.
 // ------------------------------------------------------------------------------------------------
-__global__ void k_atv_reduce(int nprimes, uint64_t elements, const int32_t* __restrict__ v, uint32_t* __restrict__ vred) {
+__global__ void k_atv_reduce(const PrimeConst* __restrict__ pcs, int nprimes, uint64_t elements,
+                             const int32_t* __restrict__ v, uint32_t* __restrict__ vred) {
   const uint64_t n = (uint64_t)nprimes * elements * RING_N;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     const int pi = (int)(i / (elements * RING_N));
-    const int64_t p = c_prime[pi].p;
+    const int64_t p = pcs[pi].p;
     const int64_t x = v[i % (elements * RING_N)];
     vred[i] = (uint32_t)(((x % p) + p) % p);
   }
 }
 
-__global__ void k_atv_mac(int nprimes, uint64_t elements, const uint32_t* __restrict__ key,
+__global__ void k_atv_mac(const PrimeConst* __restrict__ pcs, int nprimes, uint64_t elements, const uint32_t* __restrict__ key,
                           const uint32_t* __restrict__ vhat, uint32_t* __restrict__ out) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;  // (prime, leaf, l)
   if (t >= nprimes * LEAVES * 4) return;
   const int pi = t / (LEAVES * 4), s = (t / 4) % LEAVES, l = t % 4;
-  const uint64_t p = c_prime[pi].p;
+  const uint64_t p = pcs[pi].p;
   uint64_t acc = 0;  // < 4 elements x p^2 < 2^30 per term: no overflow below 2^34 elements
   for (uint64_t m = 0; m < elements; ++m) {
     const uint32_t* M = key + (((size_t)pi * elements + m) * LEAVES + s) * 16;
@@ -797,11 +814,11 @@ __global__ void k_atv_mac(int nprimes, uint64_t elements, const uint32_t* __rest
 void launch_a_times_v(const ModulusPlan& mp, const Shape& sh, const int32_t* v, const uint32_t* key, uint32_t* vred,
                       uint32_t* vhat, uint32_t* partial, uint8_t* out, cudaStream_t s) {
   const uint64_t E = sh.ring_elements;
-  k_atv_reduce<<<1024, 256, 0, s>>>(mp.nprimes, E, v, vred);
+  k_atv_reduce<<<1024, 256, 0, s>>>(mp.dconsts, mp.nprimes, E, v, vred);
   const uint64_t total = (uint64_t)mp.nprimes * E * 4;
-  k_key_forward<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(mp.nprimes, E, vred, vhat);
+  k_key_forward<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(mp.dconsts, mp.nprimes, E, vred, vhat);
   const int threads = mp.nprimes * LEAVES * 4;
-  k_atv_mac<<<(threads + 127) / 128, 128, 0, s>>>(mp.nprimes, E, key, vhat, partial);
+  k_atv_mac<<<(threads + 127) / 128, 128, 0, s>>>(mp.dconsts, mp.nprimes, E, key, vhat, partial);
   launch_commit_finish(mp, sh, partial, 1, out, s, 1);
 }
 

@@ -69,6 +69,7 @@ struct ModulusPlan {
   u128 p_mod_q = 0;                // product of the primes mod q (exact lift: negative values)
   uint32_t half_digits[MAX_PRIMES];  // floor(product / 2) in the primes' mixed radix (sign test)
   std::vector<PrimeConst> consts;
+  const PrimeConst* dconsts = nullptr;  // device copy of consts, owned by the key that holds the plan
   // Per prime and third of its leaves, the Vandermonde limbs of the tensor-core commitment
   // (bf16 bits in the MMA's shared-memory layout).
   std::vector<uint16_t> btiles;
@@ -139,9 +140,10 @@ void launch_subtrees(uint32_t* cvs, uint32_t* scratch, uint64_t nchunks, const u
                      uint32_t* out, cudaStream_t s);
 
 // ---- launch wrappers (lf_commit.cu) ----
-void upload_prime_consts(const ModulusPlan& mp, cudaStream_t s);
 // The public matrix reduced modulo each prime: ared[prime][m][648].
 void launch_matrix_expand(const ModulusPlan& mp, uint64_t elements, uint32_t* ared, cudaStream_t s);
+// The public matrix itself: elements x 648 coefficients in [0, q) as u128 little-endian.
+void launch_matrix_raw(u128 q, uint64_t elements, void* out, cudaStream_t s);
 // Leaf-form key: key[prime][m][162][16] u16.
 void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32_t* ared, uint32_t* leafvals,
                           uint32_t* key, cudaStream_t s);

@@ -19,6 +19,8 @@ ERRORS = {
     -6: "LF_E_OOM", -7: "LF_E_CUDA", -8: "LF_E_INTERNAL", -9: "LF_E_ADMISSION", -10: "LF_E_LIMIT",
     -11: "LF_E_TIMEOUT", -12: "LF_E_TICKET", -13: "LF_E_REJECT",
 }
+LF_E_ARGS = -1
+LF_E_MODULUS = -3
 LF_E_REJECT = -13
 LF_E_TIMEOUT = -11
 NOALLOC_MAX_CHALLENGES = 4096
@@ -27,7 +29,8 @@ EXPORTS = [
     "lf_prove_device", "lf_write_table_device", "lf_device_alloc", "lf_device_free", "lf_memcpy_h2d",
     "lf_last_profile", "lf_strerror", "lf_last_error", "lf_last_challenges",
     "lf_sample_challenges", "lf_sample_challenges_noalloc", "lf_prove_batch", "lf_submit", "lf_poll",
-    "lf_verify", "lf_verify_device",
+    "lf_verify", "lf_verify_device", "lf_request_footprint", "lf_ring_mul", "lf_ghash_mul", "lf_ajtai_matrix_device",
+    "lf_a_times_v",
 ]
 
 
@@ -38,7 +41,7 @@ class LfError(RuntimeError):
 
 
 class Config(ctypes.Structure):
-    _fields_ = [("device", ctypes.c_int), ("hbm_budget", ctypes.c_size_t)]
+    _fields_ = [("device", ctypes.c_int), ("hbm_budget", ctypes.c_size_t), ("lanes", ctypes.c_int)]
 
 
 class Job(ctypes.Structure):
@@ -102,6 +105,12 @@ def load(path=LIB_PATH):
     lib.lf_prove_batch.argtypes = [p, sz, ctypes.POINTER(Job), ctypes.POINTER(Result)]
     lib.lf_submit.argtypes = [p, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_uint64)]
     lib.lf_poll.argtypes = [p, ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(Result)]
+    lib.lf_request_footprint.argtypes = [p, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_int]
+    lib.lf_request_footprint.restype = sz
+    lib.lf_ring_mul.argtypes = [p, ctypes.c_char_p, sz, p, p, p]
+    lib.lf_ghash_mul.argtypes = [p, sz, p, p, p]
+    lib.lf_ajtai_matrix_device.argtypes = [p, ctypes.c_char_p, ctypes.c_uint64, p]
+    lib.lf_a_times_v.argtypes = [p, ctypes.c_char_p, ctypes.c_uint64, p, u8p]
     lib.lf_sample_challenges_noalloc.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p, sz, ctypes.c_uint32,
                                                  u8p, p]
     _lib = lib
@@ -142,10 +151,11 @@ def accept_modulus(q, log_vars):
 class Prover:
     """One device context (lf_ctx). Not thread-safe across calls; the C side serialises."""
 
-    def __init__(self, device=0, hbm_budget=0):
+    def __init__(self, device=0, hbm_budget=0, lanes=0):
         self.lib = load()
         self.ctx = ctypes.c_void_p()
-        cfg = Config(device, hbm_budget)
+        self.device, self.lanes = device, lanes
+        cfg = Config(device, hbm_budget, lanes)
         rc = self.lib.lf_ctx_create(ctypes.byref(cfg), ctypes.byref(self.ctx))
         if rc != LF_OK:
             raise LfError(rc, "context creation failed (no CUDA device?)")
@@ -253,6 +263,29 @@ class Prover:
         t = ctypes.c_uint64()
         self._check(self.lib.lf_submit(self.ctx, ctypes.byref(job), ctypes.byref(t)))
         return t.value
+
+    def footprint(self, log_vars, q=BASELINE_Q, host_table=True):
+        """Device bytes one request holds while proven (what admission compares with the budget)."""
+        return self.lib.lf_request_footprint(self.ctx, q_bytes(q), log_vars, 1 if host_table else 0)
+
+    def ring_mul(self, q, n, a_dev, b_dev, c_dev):
+        """c = a * b in R_q for n pairs of device elements (648 u128 LE coefficients each)."""
+        self._check(self.lib.lf_ring_mul(self.ctx, q_bytes(q), n, ctypes.c_void_p(a_dev), ctypes.c_void_p(b_dev),
+                                         ctypes.c_void_p(c_dev)))
+
+    def ghash_mul(self, n, a_dev, b_dev, c_dev):
+        self._check(self.lib.lf_ghash_mul(self.ctx, n, ctypes.c_void_p(a_dev), ctypes.c_void_p(b_dev),
+                                          ctypes.c_void_p(c_dev)))
+
+    def ajtai_matrix_device(self, q, elements, out_dev):
+        self._check(self.lib.lf_ajtai_matrix_device(self.ctx, q_bytes(q), elements, ctypes.c_void_p(out_dev)))
+
+    def a_times_v(self, q, elements, v_dev):
+        """rq::a_times_v of ajtai_matrix(q, elements) and the device int16 vector v: 648 ints."""
+        out = (ctypes.c_uint8 * (16 * 648))()
+        self._check(self.lib.lf_a_times_v(self.ctx, q_bytes(q), elements, ctypes.c_void_p(v_dev), out))
+        raw = bytes(out)
+        return [int.from_bytes(raw[16 * i:16 * i + 16], "little") for i in range(648)]
 
     def poll(self, ticket, wait_ms=0):
         """(code, Result): LF_OK with the result, LF_E_TIMEOUT while pending."""

@@ -1229,6 +1229,17 @@ int lfo_ajtai_matrix(const uint8_t q_le[16], uint64_t elements, uint8_t* out) {
   return LFO_OK;
 }
 
+int lfo_a_times_v(const uint8_t q_le[16], uint64_t elements, const int16_t* v, uint8_t* out) {
+  u128 q = q_from_le(q_le);
+  if (q < 2 || (q >> 96)) return LFO_E_MODULUS;
+  std::vector<u128> m = ajtai_matrix(q, elements);
+  std::vector<int16_t> vv(v, v + elements * N);
+  std::vector<u128> r = a_times_v(m, vv, q);
+  for (int i = 0; i < N; ++i)
+    for (int b = 0; b < 16; ++b) out[16 * i + b] = (uint8_t)(r[i] >> (8 * b));
+  return LFO_OK;
+}
+
 size_t lfo_proof_size(const uint8_t q_le[16], uint32_t log_vars) {
   Shape s;
   if (!s.set(log_vars)) return 0;

@@ -31,6 +31,9 @@ int lfo_b128_mul(const uint8_t* a, const uint8_t* b, uint8_t* out, size_t n);
 int lfo_f162_mul(const uint8_t* a, const uint8_t* b, uint8_t* out, size_t n);
 // The public matrix (rq::ajtai_matrix): elements*648 u128 LE.
 int lfo_ajtai_matrix(const uint8_t q_le[16], uint64_t elements, uint8_t* out);
+// rq::a_times_v (rq.rs:188-217): A v with A = ajtai_matrix(q, elements) and v the elements*648
+// signed coefficients; out = 648 u128 LE in [0, q).
+int lfo_a_times_v(const uint8_t q_le[16], uint64_t elements, const int16_t* v, uint8_t* out);
 // Bytes of one proof at this modulus and shape.
 size_t lfo_proof_size(const uint8_t q_le[16], uint32_t log_vars);
 // The commitment bytes of `table` (schoolbook when mode == 0, 3-prime transforms when mode == 1

@@ -35,6 +35,7 @@ def load():
     lib.lfo_b128_mul.argtypes = [c8, c8, u8p, ctypes.c_size_t]
     lib.lfo_f162_mul.argtypes = [c8, c8, u8p, ctypes.c_size_t]
     lib.lfo_ajtai_matrix.argtypes = [c8, ctypes.c_uint64, u8p]
+    lib.lfo_a_times_v.argtypes = [c8, ctypes.c_uint64, ctypes.c_void_p, u8p]
     lib.lfo_proof_size.argtypes = [c8, ctypes.c_uint32]
     lib.lfo_proof_size.restype = ctypes.c_size_t
     lib.lfo_commit.argtypes = [c8, ctypes.c_uint32, c8, ctypes.c_int, u8p]
@@ -96,6 +97,54 @@ def ajtai_matrix(q, elements):
     assert load().lfo_ajtai_matrix(qb(q), elements, out) == 0
     raw = bytes(out[: 16 * N * elements])
     return [int.from_bytes(raw[16 * i:16 * i + 16], "little") for i in range(N * elements)]
+
+
+def a_times_v(q, elements, v):
+    """rq::a_times_v (rq.rs:188-217) of ajtai_matrix(q, elements) and the signed vector v
+    (elements * 648 values in i16), through the C oracle; 648 ints in [0, q)."""
+    import array
+
+    vv = array.array("h", v)
+    assert len(vv) == elements * N
+    out = _buf(16 * N)
+    assert load().lfo_a_times_v(qb(q), elements, vv.buffer_info()[0], out) == 0
+    raw = bytes(out[: 16 * N])
+    return [int.from_bytes(raw[16 * i:16 * i + 16], "little") for i in range(N)]
+
+
+def fold_into_ring(raw, q):
+    """rq.rs:146-164: X^648 = X^324 - 1 from the top coefficient down, each reduced before it is
+    folded, then every coefficient into [0, q)."""
+    raw = list(raw)
+    assert len(raw) == 2 * N - 1
+    for k in range(2 * N - 2, N - 1, -1):
+        value = raw[k] % q
+        raw[k] = 0
+        raw[k - N // 2] += value
+        raw[k - N] -= value
+    return [x % q for x in raw[:N]]
+
+
+def ring_mul_schoolbook(a, b, q):
+    """rq::mul (rq.rs:171-186): the schoolbook raw product, then fold_into_ring. Pure Python,
+    for a handful of products."""
+    raw = [0] * (2 * N - 1)
+    for j, c in enumerate(b):
+        if c:
+            for i, x in enumerate(a):
+                raw[i + j] += x * c
+    return fold_into_ring(raw, q)
+
+
+def ring_mul(a, b, q):
+    """The same product with the raw coefficients from one big-integer multiplication (Kronecker
+    substitution: slots wide enough that no coefficient carries into the next)."""
+    slot = 8 * ((2 * (max(q, 2) - 1).bit_length() + 12) // 8 + 1)
+    big_a = int.from_bytes(b"".join(int(x).to_bytes(slot // 8, "little") for x in a), "little")
+    big_b = int.from_bytes(b"".join(int(x).to_bytes(slot // 8, "little") for x in b), "little")
+    prod = (big_a * big_b).to_bytes(slot // 8 * (2 * N), "little")
+    raw = [int.from_bytes(prod[i * slot // 8:(i + 1) * slot // 8], "little") for i in range(2 * N - 1)]
+    return fold_into_ring(raw, q)
 
 
 def proof_size(q, log_vars):

@@ -35,6 +35,55 @@ def test_batch_of_mixed_shapes_matches_single_proofs(prover, gpu_lib, oracle):
     assert ok, msg
 
 
+MIXED_Q = [661473542593, 9721 * 2917 * 4861, (1 << 64) - 59]
+
+
+def test_batch_of_mixed_moduli_matches_single_proofs(prover, oracle):
+    # Jobs of three moduli interleaved run on both lanes at once: each lane reads its own key's
+    # prime constants, so the bytes cannot depend on what the other lane is proving.
+    cases = _cases(oracle, [20, 19, 20, 19, 21, 19])
+    qs = [MIXED_Q[i % 3] for i in range(len(cases))]
+    alone = [prover.prove(s, t, lv, q=q) for (s, lv, t), q in zip(cases, qs)]
+    jobs = [prover.make_job(s, t, lv, q=q) for (s, lv, t), q in zip(cases, qs)]
+    res = prover.prove_batch(jobs)
+    assert [r.status for r in res] == [0] * len(jobs)
+    for j, r, want in zip(jobs, res, alone):
+        assert prover.job_proof(j, r) == want
+    ok, msg = oracle.verify(cases[1][0], alone[1], 19, cases[1][2])
+    assert ok, msg
+
+
+def test_served_mixed_moduli_match_alone(prover, oracle):
+    cases = _cases(oracle, [21, 19, 20, 19, 20, 21])
+    qs = [MIXED_Q[(i + 1) % 3] for i in range(len(cases))]
+    alone = [prover.prove(s, t, lv, q=q) for (s, lv, t), q in zip(cases, qs)]
+    jobs = [prover.make_job(s, t, lv, q=q) for (s, lv, t), q in zip(cases, qs)]
+    tickets = [prover.submit(j) for j in jobs]
+    for j, t, want in zip(jobs, tickets, alone):
+        rc, r = prover.poll(t, 60000)
+        assert rc == 0 and r.status == 0
+        assert prover.job_proof(j, r) == want
+
+
+def test_budget_for_one_request_serialises_the_queue(gpu_lib, oracle):
+    # A budget that holds one 2^21 request but not two: the second starts only after the first
+    # has finished (its queueing time covers the first's run), and both proofs are unchanged.
+    cases = _cases(oracle, [21, 21])
+    with gpu_lib.Prover(0) as free:
+        alone = [free.prove(s, t, lv) for s, lv, t in cases]
+        need = free.footprint(21)
+    with gpu_lib.Prover(0, hbm_budget=need + need // 2) as p:
+        jobs = [p.make_job(s, t, lv) for s, lv, t in cases]
+        tickets = [p.submit(j) for j in jobs]
+        res = []
+        for j, t, want in zip(jobs, tickets, alone):
+            rc, r = p.poll(t, 60000)
+            assert rc == 0 and r.status == 0
+            assert p.job_proof(j, r) == want
+            res.append(r)
+        assert res[1].queue_ms >= res[0].run_ms * 0.9
+
+
 def test_batch_failure_stays_with_its_job(prover, oracle):
     cases = _cases(oracle, [19, 20])
     good = [prover.make_job(s, t, lv) for s, lv, t in cases]
