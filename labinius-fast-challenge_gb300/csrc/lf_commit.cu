@@ -298,24 +298,26 @@ void launch_matrix_raw(u128 q, uint64_t elements, void* out, cudaStream_t s) {
 // base-multiplication matrix of every leaf: M[k][l] = A_{l-k}(c) for l >= k, c A_{l-k+4}(c) else.
 // ------------------------------------------------------------------------------------------------
 __device__ void forward162(uint32_t* x, const PrimeConst& P) {
-  const uint64_t p = P.p;
+  // residues below p < 2^15: every sum of products below stays under 2^32 before its reduction
+  const uint32_t p = P.p, bar = P.bar, w = P.w, w5 = P.w5;
+  const uint32_t om = P.om, om2 = reduce32(P.om * P.om, bar, p);
   for (int j = 0; j < 81; ++j) {
-    uint64_t a = x[j], b = x[j + 81];
-    x[j] = (uint32_t)((a + (uint64_t)P.w * b) % p);
-    x[j + 81] = (uint32_t)((a + (uint64_t)P.w5 * b) % p);
+    const uint32_t a = x[j], b = x[j + 81];
+    x[j] = reduce32(a + w * b, bar, p);
+    x[j + 81] = reduce32(a + w5 * b, bar, p);
   }
   int len = 81;
   for (int l = 1; l <= 4; ++l) {
     int sub = len / 3, nodes = 162 / len;
     for (int n = 0; n < nodes; ++n) {
       const uint32_t* tw = P.fw[node_off(l) + n];
+      const uint32_t t0 = tw[0], t1 = tw[1];
       for (int q = 0; q < sub; ++q) {
         int o = n * len + q;
-        uint64_t a0 = x[o], a1 = (uint64_t)x[o + sub] * tw[0] % p, a2 = (uint64_t)x[o + 2 * sub] * tw[1] % p;
-        uint64_t om = P.om, om2 = (uint64_t)P.om * P.om % p;
-        x[o] = (uint32_t)((a0 + a1 + a2) % p);
-        x[o + sub] = (uint32_t)((a0 + a1 * om + a2 * om2) % p);
-        x[o + 2 * sub] = (uint32_t)((a0 + a1 * om2 + a2 * om) % p);
+        const uint32_t a0 = x[o], a1 = reduce32(x[o + sub] * t0, bar, p), a2 = reduce32(x[o + 2 * sub] * t1, bar, p);
+        x[o] = reduce32(a0 + a1 + a2, bar, p);
+        x[o + sub] = reduce32(a0 + a1 * om + a2 * om2, bar, p);
+        x[o + 2 * sub] = reduce32(a0 + a1 * om2 + a2 * om, bar, p);
       }
     }
     len = sub;
@@ -794,21 +796,30 @@ __global__ void k_atv_reduce(const PrimeConst* __restrict__ pcs, int nprimes, ui
   }
 }
 
-__global__ void k_atv_mac(const PrimeConst* __restrict__ pcs, int nprimes, uint64_t elements, const uint32_t* __restrict__ key,
-                          const uint32_t* __restrict__ vhat, uint32_t* __restrict__ out) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;  // (prime, leaf, l)
-  if (t >= nprimes * LEAVES * 4) return;
-  const int pi = t / (LEAVES * 4), s = (t / 4) % LEAVES, l = t % 4;
+// One block per (prime, leaf): thread t takes output l = t % 4 over the elements m = t / 4 (mod 64);
+// the 64 partial sums (each below 64 x 4 x p^2 < 2^38) meet in shared memory.
+__global__ void __launch_bounds__(256) k_atv_mac(const PrimeConst* __restrict__ pcs, int nprimes, uint64_t elements,
+                                                 const uint32_t* __restrict__ key, const uint32_t* __restrict__ vhat,
+                                                 uint32_t* __restrict__ out) {
+  const int pi = blockIdx.x / LEAVES, s = blockIdx.x % LEAVES;
+  const int l = threadIdx.x & 3, lane4 = threadIdx.x >> 2;
   const uint64_t p = pcs[pi].p;
-  uint64_t acc = 0;  // < 4 elements x p^2 < 2^30 per term: no overflow below 2^34 elements
-  for (uint64_t m = 0; m < elements; ++m) {
+  uint64_t acc = 0;
+  for (uint64_t m = lane4; m < elements; m += 64) {
     const uint32_t* M = key + (((size_t)pi * elements + m) * LEAVES + s) * 16;
     const uint32_t* x = vhat + (((size_t)pi * elements + m) * 4) * LEAVES + s;
 #pragma unroll
     for (int k = 0; k < 4; ++k) acc += (uint64_t)M[4 * k + l] * x[k * LEAVES];
   }
+  __shared__ uint64_t part[256];
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w >= 4; w >>= 1) {
+    if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+    __syncthreads();
+  }
   // K2's input layout with one element split: [split 0][prime][column 0][leaf][l]
-  out[((size_t)pi * COLUMNS) * LEAVES * 4 + s * 4 + l] = (uint32_t)(acc % p);
+  if (threadIdx.x < 4) out[((size_t)pi * COLUMNS) * LEAVES * 4 + s * 4 + threadIdx.x] = (uint32_t)(part[threadIdx.x] % p);
 }
 
 void launch_a_times_v(const ModulusPlan& mp, const Shape& sh, const int32_t* v, const uint32_t* key, uint32_t* vred,
@@ -817,8 +828,7 @@ void launch_a_times_v(const ModulusPlan& mp, const Shape& sh, const int32_t* v, 
   k_atv_reduce<<<1024, 256, 0, s>>>(mp.dconsts, mp.nprimes, E, v, vred);
   const uint64_t total = (uint64_t)mp.nprimes * E * 4;
   k_key_forward<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(mp.dconsts, mp.nprimes, E, vred, vhat);
-  const int threads = mp.nprimes * LEAVES * 4;
-  k_atv_mac<<<(threads + 127) / 128, 128, 0, s>>>(mp.dconsts, mp.nprimes, E, key, vhat, partial);
+  k_atv_mac<<<mp.nprimes * LEAVES, 256, 0, s>>>(mp.dconsts, mp.nprimes, E, key, vhat, partial);
   launch_commit_finish(mp, sh, partial, 1, out, s, 1);
 }
 
