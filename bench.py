@@ -300,7 +300,7 @@ def batched_leg(lfgpu, prover, n=32, seed=20260):
             "tables": "page-locked host memory, H2D inside the timed batch"}
 
 
-def micro_leg(lfgpu, prover, stream):
+def micro_leg(lfgpu, prover, stream, ghash_log=28, moduli=("baseline", "2^64", "q93"), matvec=True):
     """The kernel microbenchmark: 2^16 ring products in R_Q for the baseline prime product, Q = 2^64
     and a three-prime Q near 2^93 (operands from the device's public-matrix expansion, uniform in
     [0, Q)); 2^28 GHASH products of random pairs; a_times_v of the 4096-element matrix with v
@@ -318,6 +318,8 @@ def micro_leg(lfgpu, prover, stream):
     ring = {}
     for name, q in (("baseline", lfgpu.BASELINE_Q), ("2^64", 1 << 64),
                     ("q93", 2147478481 * 2147449321 * 2147429881)):
+        if name not in moduli:
+            continue
         m = torch.empty(2 * half, dtype=torch.uint8, device="cuda")
         c = torch.empty(half, dtype=torch.uint8, device="cuda")
         prover.ajtai_matrix_device(q, 2 * n, m.data_ptr())
@@ -326,14 +328,16 @@ def micro_leg(lfgpu, prover, stream):
         del m, c
     out["ring_products_2^16"] = ring
     g = torch.Generator(device="cuda").manual_seed(5)
-    ng = 1 << 28
+    ng = 1 << ghash_log
     a = torch.randint(-2 ** 63, 2 ** 63 - 1, (2 * ng,), dtype=torch.int64, device="cuda", generator=g)
     b = torch.randint(-2 ** 63, 2 ** 63 - 1, (2 * ng,), dtype=torch.int64, device="cuda", generator=g)
     c = torch.empty_like(a)
     torch.cuda.synchronize()
     ms = med(lambda i: prover.ghash_mul(ng, a.data_ptr(), b.data_ptr(), c.data_ptr()))
-    out["ghash_2^28"] = {"ms": round(ms, 3), "products_per_s": round(ng / ms * 1e3), "gbs": round(48 * ng / ms / 1e6, 1)}
+    out[f"ghash_2^{ghash_log}"] = {"ms": round(ms, 3), "products_per_s": round(ng / ms * 1e3), "gbs": round(48 * ng / ms / 1e6, 1)}
     del a, b, c
+    if not matvec:
+        return out
     v = torch.randint(-(1 << 10), (1 << 10) + 1, (4096 * 648,), dtype=torch.int16, device="cuda", generator=g)
     torch.cuda.synchronize()
     prover.a_times_v(lfgpu.BASELINE_Q, 4096, v.data_ptr())  # key build
@@ -415,6 +419,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=100, help="requests of the serving leg (Poisson, 8/s)")
     ap.add_argument("--lanes", type=int, default=0, help="proofs in flight per context (0 = the library default)")
     ap.add_argument("--no-micro", action="store_true", help="skip the ring / GHASH / a_times_v microbenchmark")
+    ap.add_argument("--only-micro", action="store_true",
+                    help="run only a small microbenchmark (baseline ring products, 2^25 GHASH products) and exit")
     args = ap.parse_args()
     rank, world, local = dist_init(args.gpus)
     if args.impl == "reference":
@@ -430,6 +436,11 @@ def main():
     tbytes = (1 << log_vars) // 8
     prover = lfgpu.Prover(local, lanes=args.lanes)
     stream = torch.cuda.ExternalStream(prover.stream())
+    if args.only_micro:  # the profiling case of k_ring_mul and k_ghash_mul
+        if rank == 0:
+            print(json.dumps({"micro": micro_leg(lfgpu, prover, stream, ghash_log=25, moduli=("baseline",),
+                                                 matvec=False)}))
+        return
     ss = seeds(args.tables, rank)
     tables = [device_table(prover, s, log_vars) for s in ss]
     torch.cuda.synchronize()
