@@ -419,6 +419,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=100, help="requests of the serving leg (Poisson, 8/s)")
     ap.add_argument("--lanes", type=int, default=0, help="proofs in flight per context (0 = the library default)")
     ap.add_argument("--no-micro", action="store_true", help="skip the ring / GHASH / a_times_v microbenchmark")
+    ap.add_argument("--only-batch", action="store_true", help="run only the batched leg and exit")
     ap.add_argument("--only-micro", action="store_true",
                     help="run only a small microbenchmark (baseline ring products, 2^25 GHASH products) and exit")
     args = ap.parse_args()
@@ -436,6 +437,10 @@ def main():
     tbytes = (1 << log_vars) // 8
     prover = lfgpu.Prover(local, lanes=args.lanes)
     stream = torch.cuda.ExternalStream(prover.stream())
+    if args.only_batch:  # the profiling case of the batched leg
+        if rank == 0:
+            print(json.dumps({"batched": batched_leg(lfgpu, prover)}))
+        return
     if args.only_micro:  # the profiling case of k_ring_mul and k_ghash_mul
         if rank == 0:
             print(json.dumps({"micro": micro_leg(lfgpu, prover, stream, ghash_log=25, moduli=("baseline",),

@@ -832,6 +832,75 @@ void launch_a_times_v(const ModulusPlan& mp, const Shape& sh, const int32_t* v, 
   launch_commit_finish(mp, sh, partial, 1, out, s, 1);
 }
 
+// The checker's scans of the folded witness v (main.rs:266-289 and the norm / range tests): one
+// thread per (element m, residue k): bit 0 of v[m][4 pp + k] for pp < 162 packed into an F162 (the
+// fold mod 2, components_mod_2), times e0[4 m + k], XOR-summed; sum of v^2; max and min of v.
+// out: [0..2] the F162 sum, [3] sum v^2, [4] max v + 2^31, [5] 2^31 - min v (zeroed by the caller).
+__global__ void __launch_bounds__(256) k_fold_checks(const int32_t* __restrict__ v, uint64_t elements,
+                                                     const f162* __restrict__ e0, unsigned long long* __restrict__ out) {
+  const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  f162 acc = {0, 0, 0};
+  unsigned long long sq = 0, hi = 0, lo = 0;
+  if (t < 4 * elements) {
+    const uint64_t m = t >> 2;
+    const int k = (int)(t & 3);
+    const int32_t* src = v + m * RING_N + k;
+    f162 x = {0, 0, 0};
+    int32_t mx = INT32_MIN, mn = INT32_MAX;
+    for (int pp = 0; pp < RING_N / 4; ++pp) {
+      const int32_t c = src[4 * pp];
+      sq += (unsigned long long)((int64_t)c * c);
+      mx = max(mx, c), mn = min(mn, c);
+      const uint64_t bit = (uint64_t)(c & 1) << (pp & 63);
+      if (pp < 64) x.w0 |= bit;
+      else if (pp < 128) x.w1 |= bit;
+      else x.w2 |= bit;
+    }
+    acc = f162_mul(e0[t], x);
+    hi = (unsigned long long)((int64_t)mx + (1ll << 31));
+    lo = (unsigned long long)((1ll << 31) - (int64_t)mn);
+  }
+  for (int o = 16; o; o >>= 1) {
+    acc.w0 ^= __shfl_xor_sync(0xffffffffu, acc.w0, o);
+    acc.w1 ^= __shfl_xor_sync(0xffffffffu, acc.w1, o);
+    acc.w2 ^= __shfl_xor_sync(0xffffffffu, acc.w2, o);
+    sq += __shfl_xor_sync(0xffffffffu, sq, o);
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    lo = max(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicXor(out, (unsigned long long)acc.w0);
+    atomicXor(out + 1, (unsigned long long)acc.w1);
+    atomicXor(out + 2, (unsigned long long)acc.w2);
+    atomicAdd(out + 3, sq);
+    atomicMax(out + 4, hi);
+    atomicMax(out + 5, lo);
+  }
+}
+
+void launch_fold_checks(const int32_t* v, uint64_t elements, const f162* e0, unsigned long long* out, cudaStream_t s) {
+  const uint64_t n = 4 * elements;
+  k_fold_checks<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(v, elements, e0, out);
+}
+
+// *flag becomes nonzero when a commitment coefficient (w bytes little-endian) is not below q.
+__global__ void k_commit_range(const uint8_t* __restrict__ c, uint32_t w, uint64_t q_lo, uint64_t q_hi, uint64_t n,
+                               unsigned long long* __restrict__ flag) {
+  const u128 q = ((u128)q_hi << 64) | q_lo;
+  bool bad = false;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    u128 x = 0;
+    for (int b = (int)w - 1; b >= 0; --b) x = (x << 8) | c[i * w + b];
+    bad |= x >= q;
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
+}
+
+void launch_commit_range(const uint8_t* commit, uint32_t w, u128 q, uint64_t n, unsigned long long* flag,
+                         cudaStream_t s) {
+  k_commit_range<<<512, 256, 0, s>>>(commit, w, (uint64_t)q, (uint64_t)(q >> 64), n, flag);
+}
+
 // challenge_combination (rq.rs:226-256): raw[r] = sum_j sum_t sign_{j,t} C_j[r - 4 pos_{j,t}],
 // the challenge sitting in R_Q as c(-X^4), sign = (-1)^(sign bit + pos). One thread per raw index
 // and run of 32 columns; partial sums as signed 128-bit integers (|.| < 32 x 28 x 2^96),

@@ -158,5 +158,12 @@ void launch_a_times_v(const ModulusPlan& mp, const Shape& sh, const int32_t* v, 
                       uint32_t* vhat, uint32_t* partial, uint8_t* out, cudaStream_t s);
 void launch_challenge_combination(const uint8_t* commit, uint32_t width, const Challenge* ch,
                                   unsigned long long* part, cudaStream_t s);
+// The checker's scans of the folded witness (elements x 648 int32): out[0..2] = sum over (m, k) of
+// e0[4 m + k] times the F162 of bit 0 of v[m][4 pp + k], out[3] = sum v^2, out[4] = max v + 2^31,
+// out[5] = 2^31 - min v; out zeroed by the caller.
+void launch_fold_checks(const int32_t* v, uint64_t elements, const f162* e0, unsigned long long* out, cudaStream_t s);
+// *flag |= 1 when one of the n commitment coefficients (w bytes LE) is not below q.
+void launch_commit_range(const uint8_t* commit, uint32_t w, u128 q, uint64_t n, unsigned long long* flag,
+                         cudaStream_t s);
 
 }  // namespace lf
