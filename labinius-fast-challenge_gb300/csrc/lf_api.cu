@@ -297,6 +297,21 @@ void phase_tables(std::vector<double>& re, std::vector<double>& im) {
     }
 }
 
+// The challenge sampler's tables in one device buffer: PHASE re and im as f64 (the reference's
+// arithmetic) and the same values rounded to f32 (the sampler's fast norm estimate).
+cudaError_t upload_phase_tables(void* dst) {
+  std::vector<double> re, im;
+  phase_tables(re, im);
+  std::vector<float> re32(re.begin(), re.end()), im32(im.begin(), im.end());
+  uint8_t* d = static_cast<uint8_t*>(dst);
+  const size_t n = 162 * 88;
+  cudaError_t e = cudaMemcpy(d, re.data(), n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + n * 8, im.data(), n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + n * 16, re32.data(), n * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + n * 20, im32.data(), n * 4, cudaMemcpyHostToDevice);
+  return e;
+}
+
 // Device bytes one proof at this shape may hold beyond the cached keys: the table (when it is
 // copied from the host), the commitment's split partial sums, the partial-sum blocks, the
 // transcript stream, the fold output and the smaller work buffers, plus the transient buffers of
@@ -657,7 +672,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   CK(cudaMemcpyAsync(ctx->hasher.p, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, st));
   // status[0] was zeroed before the commitment: 3 = commitment pipeline timeout, 1 = sampling
   // bound, 2 = fold range.
-  launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.as<double>(), ctx->phase.as<double>() + 162 * 88,
+  launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.p,
                     ctx->chal.as<Challenge>(), COLUMNS, ctx->status.as<int>(), st);
   t.counter += COLUMNS;
   CKL("challenges");
@@ -1049,7 +1064,7 @@ int verify_device(lf_ctx* ctx, const uint8_t seed[32], const Shape& sh, const ui
   CK(ctx->eqt.ensure(sh.column_len * 24));
   CK(cudaMemcpyAsync(ctx->hasher.p, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(ctx->status.p, 0, 16, st));
-  launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.as<double>(), ctx->phase.as<double>() + 162 * 88,
+  launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.p,
                     ctx->chal.as<Challenge>(), COLUMNS, ctx->status.as<int>(), st);
   t.counter += COLUMNS;
   CK(cudaMemcpyAsync(ctx->p0.p, p0.data(), 24 * p0.size(), cudaMemcpyHostToDevice, st));
@@ -1168,7 +1183,7 @@ struct NoAllocScratch {
   bk::Hasher hasher;                      // Transcript::new(domain) after absorb_bytes(prefix)
   int status[4];                          // status[0] != 0: a challenge failed its norm bound
   Challenge chal[NOALLOC_MAX_CHALLENGES];
-  double phase[2 * 162 * 88];             // phase tables (re, im)
+  uint8_t phase[PHASE_TABLE_BYTES];       // phase tables (f64 re, im; f32 re, im)
 };
 
 static __device__ __align__(256) uint8_t g_noalloc_scratch[sizeof(NoAllocScratch)];
@@ -1186,11 +1201,7 @@ int noalloc_setup(NoAllocDevice& d) {
   void* p = nullptr;
   if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return LF_E_CUDA;
   NoAllocScratch* sc = static_cast<NoAllocScratch*>(p);
-  std::vector<double> re, im;
-  phase_tables(re, im);
-  if (cudaMemcpy(sc->phase, re.data(), 162 * 88 * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(sc->phase + 162 * 88, im.data(), 162 * 88 * 8, cudaMemcpyHostToDevice) != cudaSuccess)
-    return LF_E_CUDA;
+  if (upload_phase_tables(sc->phase) != cudaSuccess) return LF_E_CUDA;
   bk::Hasher h;
   const char* c = "labinius 2026 challenge signs v1";
   h.init_derive(c, (uint32_t)strlen(c));
@@ -1210,7 +1221,7 @@ int noalloc_sample(NoAllocDevice& d, const char* domain, const uint8_t* prefix, 
   if (cudaMemcpyAsync(&sc->hasher, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemsetAsync(sc->status, 0, sizeof(sc->status), st) != cudaSuccess)
     return LF_E_CUDA;
-  launch_challenges(&sc->hasher, t.counter, d.sign_key, sc->phase, sc->phase + 162 * 88, sc->chal, (int)n, sc->status,
+  launch_challenges(&sc->hasher, t.counter, d.sign_key, sc->phase, sc->chal, (int)n, sc->status,
                     st);
   if (cudaGetLastError() != cudaSuccess) return LF_E_CUDA;
   if (cudaMemcpyAsync(out, sc->chal, (size_t)n * sizeof(Challenge), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
@@ -1255,11 +1266,7 @@ int lf_ctx_create(const lf_config* cfg, lf_ctx** out) {
     h.init_derive(c, (uint32_t)strlen(c));
     memcpy(ctx->sign_key, h.key, 32);
   }
-  std::vector<double> re, im;
-  phase_tables(re, im);
-  if (ctx->phase.ensure(2 * 162 * 88 * 8) != cudaSuccess ||
-      cudaMemcpy(ctx->phase.p, re.data(), 162 * 88 * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(ctx->phase.as<double>() + 162 * 88, im.data(), 162 * 88 * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+  if (ctx->phase.ensure(PHASE_TABLE_BYTES) != cudaSuccess || upload_phase_tables(ctx->phase.p) != cudaSuccess) {
     lf_ctx_destroy(ctx);
     return LF_E_CUDA;
   }
@@ -1442,7 +1449,7 @@ int lf_sample_challenges_traced(lf_ctx* ctx, const char* domain, const uint8_t* 
   CK(cudaMemsetAsync(ctx->scratch_small.p, 0, 64 * 4, ctx->stream));
   CK(cudaMemcpyAsync(ctx->hasher.p, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemsetAsync(ctx->status.p, 0, 16, ctx->stream));
-  launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.as<double>(), ctx->phase.as<double>() + 162 * 88,
+  launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.p,
                     ctx->chal.as<Challenge>(), (int)n, ctx->status.as<int>(), ctx->stream,
                     trace64 ? ctx->scratch_small.as<uint32_t>() : nullptr);
   CKL("challenges");

@@ -261,8 +261,9 @@ struct Hasher {
     for (int i = 0; i < 8; ++i) b[i] = (uint8_t)(x >> (8 * i));
     absorb(b, 8);
   }
-  LF_HD Pending finish() const {
-    Pending out = chunk.pending();
+  LF_HD Pending finish() const { return merge_up(chunk.pending()); }
+  // The root node over the stack with `out` as the rightmost node (the pending chunk).
+  LF_HD Pending merge_up(Pending out) const {
     for (uint32_t i = depth; i-- > 0;) {
       uint32_t right[8];
       out.cv(right);
@@ -288,8 +289,16 @@ LF_HD Pending derive_root(const Hasher& state, uint64_t counter, const char* lab
   for (int i = 0; i < 8; ++i) suffix[i] = (uint8_t)(counter >> (8 * i));
   for (int i = 0; i < 8; ++i) suffix[8 + i] = (uint8_t)((uint64_t)label_len >> (8 * i));
   for (uint32_t i = 0; i < label_len && i < 64; ++i) suffix[16 + i] = (uint8_t)label[i];
+  const uint32_t n = 16 + (label_len < 64 ? label_len : 64);
+  if (state.chunk.size() + n <= 1024) {
+    // The suffix stays inside the pending chunk: copy only the chunk (not the whole stack) and
+    // merge up through the state's own stack.
+    Chunk c = state.chunk;
+    c.absorb(suffix, n);
+    return state.merge_up(c.pending());
+  }
   Hasher h = state;
-  h.absorb(suffix, 16 + (label_len < 64 ? label_len : 64));
+  h.absorb(suffix, n);
   return h.finish();
 }
 

@@ -677,6 +677,7 @@ struct FinishArgs {
   uint32_t primes[MAX_PRIMES];
   uint32_t half[MAX_PRIMES];     // floor(product / 2), mixed radix
   uint32_t ginv[MAX_PRIMES][MAX_PRIMES];
+  uint32_t bar[MAX_PRIMES];      // floor(2^32 / p): every reduction below is of a value under 2^32
 };
 
 __global__ void __launch_bounds__(256) k_commit_finish(FinishArgs a, const PrimeConst* __restrict__ pcs,
@@ -685,10 +686,10 @@ __global__ void __launch_bounds__(256) k_commit_finish(FinishArgs a, const Prime
   const int col = blockIdx.x;
   for (int e = threadIdx.x; e < a.nprimes * 4 * LEAVES; e += blockDim.x) {
     int pi = e / (4 * LEAVES), rem = e % (4 * LEAVES), s = rem / 4, l = rem % 4;
-    uint64_t p = a.primes[pi], sum = 0;
+    uint32_t sum = 0;  // at most 40 splits of residues below 2^15
     for (int sp = 0; sp < a.splits; ++sp)
       sum += partial[(((size_t)sp * a.nprimes + pi) * COLUMNS + col) * LEAVES * 4 + rem];
-    v[pi][l][s] = (uint32_t)(sum % p);
+    v[pi][l][s] = reduce32(sum, a.bar[pi], a.primes[pi]);
   }
   __syncthreads();
   // Inverse radix-3 levels 4..1: nodes of length 3, 9, 27, 81.
@@ -699,17 +700,17 @@ __global__ void __launch_bounds__(256) k_commit_finish(FinishArgs a, const Prime
       int pi = e / (4 * per_t), rem = e % (4 * per_t), l = rem / per_t, r2 = rem % per_t;
       int n = r2 / sub, q = r2 % sub;
       const PrimeConst& P = pcs[pi];
-      const uint64_t p = P.p;
+      const uint32_t p = P.p, bar = P.bar;  // residues below 2^15: sums of two products stay under 2^32
       uint32_t* x = v[pi][l];
       int o = n * len + q;
-      uint64_t y0 = x[o], y1 = x[o + sub], y2 = x[o + 2 * sub];
-      uint64_t a0 = (y0 + y1 + y2) % p;
-      uint64_t a1 = (y0 + y1 * P.iom + y2 * P.iom2) % p;
-      uint64_t a2 = (y0 + y1 * P.iom2 + y2 * P.iom) % p;
+      const uint32_t y0 = x[o], y1 = x[o + sub], y2 = x[o + 2 * sub];
+      const uint32_t a0 = reduce32(y0 + y1 + y2, bar, p);
+      const uint32_t a1 = reduce32(y0 + y1 * P.iom + y2 * P.iom2, bar, p);
+      const uint32_t a2 = reduce32(y0 + y1 * P.iom2 + y2 * P.iom, bar, p);
       const uint32_t* it = P.itw[node_off(lvl) + n];
-      x[o] = (uint32_t)(a0 * P.inv3 % p);
-      x[o + sub] = (uint32_t)(a1 * P.inv3 % p * it[0] % p);
-      x[o + 2 * sub] = (uint32_t)(a2 * P.inv3 % p * it[1] % p);
+      x[o] = reduce32(a0 * P.inv3, bar, p);
+      x[o + sub] = reduce32(reduce32(a1 * P.inv3, bar, p) * it[0], bar, p);
+      x[o + 2 * sub] = reduce32(reduce32(a2 * P.inv3, bar, p) * it[1], bar, p);
     }
     __syncthreads();
     len *= 3;
@@ -717,23 +718,23 @@ __global__ void __launch_bounds__(256) k_commit_finish(FinishArgs a, const Prime
   for (int e = threadIdx.x; e < a.nprimes * 4 * 81; e += blockDim.x) {
     int pi = e / (4 * 81), rem = e % (4 * 81), l = rem / 81, j = rem % 81;
     const PrimeConst& P = pcs[pi];
-    const uint64_t p = P.p;
+    const uint32_t p = P.p, bar = P.bar;
     uint32_t* x = v[pi][l];
-    uint64_t u = x[j], w = x[j + 81];
-    uint64_t b = (u + p - w) % p * P.inv_split % p;
-    x[j] = (uint32_t)((u + p * p - (uint64_t)P.w * b) % p);
-    x[j + 81] = (uint32_t)b;
+    const uint32_t u = x[j], w = x[j + 81];
+    const uint32_t b = reduce32(reduce32(u + p - w, bar, p) * P.inv_split, bar, p);
+    x[j] = reduce32(u + p * p - P.w * b, bar, p);
+    x[j + 81] = b;
   }
   __syncthreads();
   // Coefficient 4p + l of the column is coefficient p of C_l. Garner's CRT into [0, Q).
   for (int i = threadIdx.x; i < RING_N; i += blockDim.x) {
     int pp = i >> 2, l = i & 3;
-    uint64_t digit[MAX_PRIMES];
+    uint32_t digit[MAX_PRIMES];
     for (int k = 0; k < a.nprimes; ++k) {
-      uint64_t pk = a.primes[k];
-      uint64_t t = v[k][l][pp];
+      const uint32_t pk = a.primes[k], bk = a.bar[k];
+      uint32_t t = v[k][l][pp];
       // t <- (r_k - (d_0 + p_0 d_1 + ...)) / (p_0 ... p_{k-1}) mod p_k, digit by digit
-      for (int j = 0; j < k; ++j) t = (t + pk - digit[j] % pk) % pk * a.ginv[k][j] % pk;
+      for (int j = 0; j < k; ++j) t = reduce32(reduce32(t + pk - reduce32(digit[j], bk, pk), bk, pk) * a.ginv[k][j], bk, pk);
       digit[k] = t;
     }
     u128 val = 0;
@@ -774,6 +775,7 @@ void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t
   for (int i = 0; i < mp.nprimes; ++i) {
     a.primes[i] = mp.primes[i];
     a.half[i] = mp.half_digits[i];
+    a.bar[i] = (uint32_t)((1ull << 32) / mp.primes[i]);
     for (int j = 0; j < i; ++j) a.ginv[i][j] = mp.garner_inv[i][j];
   }
   k_commit_finish<<<ncols, 256, 0, s>>>(a, mp.dconsts, partial, out);

@@ -125,9 +125,10 @@ void launch_switch_fold(Soa a, Soa p, uint64_t half, f162 r, int sms, cudaStream
 // ---- launch wrappers (lf_open.cu) ----
 void launch_row_eval(const uint4* table, int rl, const f162* eqt, f162* row, cudaStream_t s);
 struct HasherImage;  // a bk::Hasher copied to the device
-void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint32_t sign_key[8], const double* phase_re,
-                       const double* phase_im, Challenge* out, int n, int* status, cudaStream_t s,
-                       uint32_t* dbg = nullptr);
+// PHASE[162][88] as f64 re, f64 im, f32 re, f32 im, one after the other.
+constexpr size_t PHASE_TABLE_BYTES = 162 * 88 * (8 + 8 + 4 + 4);
+void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint32_t sign_key[8], const void* phase,
+                       Challenge* out, int n, int* status, cudaStream_t s, uint32_t* dbg = nullptr);
 int fold_splits(uint64_t ring_elements, int sms);
 constexpr size_t FOLD_STRIP_BYTES = 53 * 128;  // per column
 void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Challenge* ch, uint8_t* strips,

@@ -78,7 +78,8 @@ __device__ __forceinline__ void xof_refill(ChWarp& s, const bk::Pending& root, u
 
 __global__ void __launch_bounds__(32 * CH_WARPS) k_challenges(const bk::Hasher* __restrict__ state, uint64_t base,
                                                               bk::Pending sign_key_node, const double* __restrict__ re,
-                                                              const double* __restrict__ im, double bound_sq,
+                                                              const double* __restrict__ im, const float* __restrict__ re32,
+                                                              const float* __restrict__ im32, double bound_sq,
                                                               Challenge* __restrict__ out, int n, int* status,
                                                               uint32_t* __restrict__ dbg) {
   __shared__ ChWarp sw[CH_WARPS];
@@ -166,8 +167,28 @@ __global__ void __launch_bounds__(32 * CH_WARPS) k_challenges(const bk::Hasher* 
       for (int i = 0; i < 28; ++i) reinterpret_cast<uint8_t*>(dbg + 35)[i] = sorted[wid][i];
       dbg[42] = signs;
     }
+    // The norm test first in f32: 28 terms of magnitude <= 1 put the f32 |c|^2 within 0.01 of the
+    // f64 value (the table's f32 rounding and 28 additions each contribute < 2^-24 per term, and
+    // |c| < 29), so outside [bound - 0.05, bound + 0.05] the f32 decision is the f64 decision.
+    // Inside that window (rare) the lane repeats the reference's f64 sequence exactly.
+    const float bound_f = (float)bound_sq;
     bool over = false;
     for (int k = lane; k < 81; k += 32) {
+      float fr = 0.0f, fi = 0.0f;
+      for (int t = 0; t < WEIGHT; ++t) {
+        const int b = sorted[wid][t] * PHASE_LANES + k;
+        const float pr = re32[b], pi = im32[b];
+        const bool neg = (signs >> t) & 1;
+        fr += neg ? -pr : pr;
+        fi += neg ? -pi : pi;
+      }
+      const float m2f = fr * fr + fi * fi;
+      const bool traced = trace && attempt == 0 && k == 0;  // the diagnostic records the f64 values
+      if (!traced && m2f > bound_f + 0.05f) {
+        over = true;
+        continue;
+      }
+      if (!traced && m2f < bound_f - 0.05f) continue;
       double vr = 0.0, vi = 0.0;
       for (int t = 0; t < WEIGHT; ++t) {
         int b = sorted[wid][t] * PHASE_LANES + k;
@@ -200,8 +221,13 @@ __global__ void __launch_bounds__(32 * CH_WARPS) k_challenges(const bk::Hasher* 
   if (lane == 0) atomicExch(status, 1);
 }
 
-void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint32_t sign_key[8], const double* phase_re,
-                       const double* phase_im, Challenge* out, int n, int* status, cudaStream_t s, uint32_t* dbg) {
+void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint32_t sign_key[8], const void* phase,
+                       Challenge* out, int n, int* status, cudaStream_t s, uint32_t* dbg) {
+  const size_t np = 162 * PHASE_LANES;
+  const double* phase_re = static_cast<const double*>(phase);
+  const double* phase_im = phase_re + np;
+  const float* re32 = reinterpret_cast<const float*>(phase_im + np);
+  const float* im32 = re32 + np;
   bk::Pending sk;
   for (int i = 0; i < 8; ++i) sk.h[i] = sign_key[i];
   for (int i = 0; i < 16; ++i) sk.m[i] = 0;
@@ -210,7 +236,8 @@ void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint
   sk.flags = bk::F_DERIVE_MAT | bk::F_CHUNK_START | bk::F_CHUNK_END;
   const double bound_sq = 12.0 * 12.0 + 1e-12;
   k_challenges<<<(n + CH_WARPS - 1) / CH_WARPS, 32 * CH_WARPS, 0, s>>>(
-      reinterpret_cast<const bk::Hasher*>(hasher_dev), base_counter, sk, phase_re, phase_im, bound_sq, out, n, status, dbg);
+      reinterpret_cast<const bk::Hasher*>(hasher_dev), base_counter, sk, phase_re, phase_im, re32, im32, bound_sq, out, n,
+      status, dbg);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -485,34 +512,53 @@ __global__ void k_chunk_cvs(const uint8_t* __restrict__ stream, uint64_t nchunks
   for (int i = 0; i < 8; ++i) cvs[c * 8 + i] = h[i];
 }
 
+// The chaining values of the complete subtrees of the stream's finished chunks (sizes = the set
+// bits of nchunks, largest first). All subtrees are reduced together, one tree level per pass:
+// level L halves every subtree still larger than 2^L, so the block runs max(log2 size) dependent
+// parent compressions instead of their sum. Subtree s keeps its chunk offset in the ping-pong
+// buffers A and B (level 0 reads the chunk values themselves).
 __global__ void __launch_bounds__(1024) k_subtrees(const uint32_t* __restrict__ cvs, uint32_t* scratch, uint64_t nchunks,
                                                    KeyArg key, uint32_t mode, uint32_t* __restrict__ out) {
-  uint32_t* bufA = scratch;
-  uint32_t* bufB = scratch + nchunks * 8;
-  uint64_t off = 0;
-  int d = 0;
-  for (int bit = 63; bit >= 0; --bit) {
-    uint64_t size = 1ull << bit;
-    if (!(nchunks & size)) continue;
-    const uint32_t* src = cvs + off * 8;
-    uint32_t* dst = bufA;
-    uint64_t cnt = size;
-    while (cnt > 1) {
-      for (uint64_t i = threadIdx.x; i < cnt / 2; i += blockDim.x) {
-        uint32_t l[8], r[8], o[8];
-        for (int k = 0; k < 8; ++k) l[k] = src[(2 * i) * 8 + k], r[k] = src[(2 * i + 1) * 8 + k];
-        bk::parent(l, r, key.k, mode, o);
-        for (int k = 0; k < 8; ++k) dst[i * 8 + k] = o[k];
+  uint32_t* buf[2] = {scratch, scratch + nchunks * 8};
+  int nsub = 0, top = 0;
+  uint64_t offs[64];
+  int bits[64];
+  {
+    uint64_t off = 0;
+    for (int bit = 63; bit >= 0; --bit)
+      if (nchunks >> bit & 1) {
+        offs[nsub] = off, bits[nsub] = bit, ++nsub;
+        off += 1ull << bit;
+        top = max(top, bit);
       }
-      __syncthreads();
-      cnt /= 2;
-      src = dst;
-      dst = (dst == bufA) ? bufB : bufA;
+  }
+  for (int L = 0; L < top; ++L) {
+    const uint32_t* src = L == 0 ? cvs : buf[(L - 1) & 1];
+    uint32_t* dst = buf[L & 1];
+    uint64_t total = 0;  // the level's pairs of all subtrees, spread over the block as one range
+    for (int sidx = 0; sidx < nsub; ++sidx)
+      if (bits[sidx] > L) total += 1ull << (bits[sidx] - L - 1);
+    for (uint64_t g = threadIdx.x; g < total; g += blockDim.x) {
+      uint64_t i = g;
+      int sidx = 0;
+      for (; sidx < nsub; ++sidx) {
+        if (bits[sidx] <= L) continue;
+        const uint64_t pairs = 1ull << (bits[sidx] - L - 1);
+        if (i < pairs) break;
+        i -= pairs;
+      }
+      const uint32_t* a = src + (offs[sidx] + 2 * i) * 8;
+      uint32_t l[8], r[8], o[8];
+      for (int k = 0; k < 8; ++k) l[k] = a[k], r[k] = a[8 + k];
+      bk::parent(l, r, key.k, mode, o);
+      for (int k = 0; k < 8; ++k) dst[(offs[sidx] + i) * 8 + k] = o[k];
     }
-    if (threadIdx.x < 8) out[d * 8 + threadIdx.x] = src[threadIdx.x];
     __syncthreads();
-    ++d;
-    off += size;
+  }
+  // subtree s's value: its single chunk value (size 1) or the last level that halved it
+  for (int sidx = 0; sidx < nsub; ++sidx) {
+    const uint32_t* src = bits[sidx] == 0 ? cvs : buf[(bits[sidx] - 1) & 1];
+    if (threadIdx.x < 8) out[sidx * 8 + threadIdx.x] = src[offs[sidx] * 8 + threadIdx.x];
   }
 }
 

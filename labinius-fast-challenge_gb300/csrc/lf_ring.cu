@@ -18,9 +18,10 @@
 //    product reduced mod X^648 - X^324 + 1 (at most 972 (Q-1)^2); the centred mixed-radix value
 //    is that integer, reduced mod Q by Horner with Barrett steps (a mask when Q is a power of 2).
 //
-// One CTA per product and one warp per prime: the operands are staged once in shared memory,
-// each warp reduces them modulo its prime, transforms both, multiplies pointwise (Montgomery),
-// transforms back; the CTA then recombines the residues of each coefficient.
+// One CTA per product and one warp per prime: each warp reads the operands (the block's other
+// warps hit L1), reduces them modulo its prime, transforms both in shared memory, multiplies
+// pointwise (Montgomery) and transforms back; the CTA then recombines the residues of each
+// coefficient.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -351,22 +352,24 @@ __global__ void __launch_bounds__(32 * MAX_RING_PRIMES)
     k_ring_mul(RingArgs A, const RingPrimeDev* __restrict__ rps, const uint4* __restrict__ a,
                const uint4* __restrict__ b, uint4* __restrict__ c, int* status) {
   extern __shared__ __align__(16) uint8_t rsm[];
-  uint4* ia = reinterpret_cast<uint4*>(rsm);
-  uint4* ib = ia + RING_N;
-  uint32_t* res = reinterpret_cast<uint32_t*>(ib + RING_N);  // [prime][2][648]
+  uint32_t* res = reinterpret_cast<uint32_t*>(rsm);  // [prime][2][648]
   const size_t prod = blockIdx.x;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nt = blockDim.x;
   const u128 q = ((u128)A.q_hi << 64) | A.q_lo;
-  bool bad = false;
-  for (int i = tid; i < RING_N; i += nt) {
-    const uint4 x = a[prod * RING_N + i], y = b[prod * RING_N + i];
-    ia[i] = x, ib[i] = y;
-    const u128 xv = ((u128)(((uint64_t)x.w << 32) | x.z) << 64) | (((uint64_t)x.y << 32) | x.x);
-    const u128 yv = ((u128)(((uint64_t)y.w << 32) | y.z) << 64) | (((uint64_t)y.y << 32) | y.x);
-    bad |= xv >= q || yv >= q;
+  // Every warp reads the operands itself (the other warps of the block find them in L1); warp 0
+  // also checks that they are below q.
+  const uint4* ia = a + prod * RING_N;
+  const uint4* ib = b + prod * RING_N;
+  if (warp == 0) {
+    bool bad = false;
+    for (int i = lane; i < RING_N; i += 32) {
+      const uint4 x = ia[i], y = ib[i];
+      const u128 xv = ((u128)(((uint64_t)x.w << 32) | x.z) << 64) | (((uint64_t)x.y << 32) | x.x);
+      const u128 yv = ((u128)(((uint64_t)y.w << 32) | y.z) << 64) | (((uint64_t)y.y << 32) | y.x);
+      bad |= xv >= q || yv >= q;
+    }
+    if (bad) atomicOr(status, 1);
   }
-  if (bad) atomicOr(status, 1);
-  __syncthreads();
   {
     const RingPrimeDev& P = rps[warp];
     const uint32_t p = P.p;
@@ -461,7 +464,7 @@ __global__ void __launch_bounds__(32 * MAX_RING_PRIMES)
   }
 }
 
-size_t ring_mul_smem(int nprimes) { return 2 * RING_N * 16 + (size_t)nprimes * 2 * RING_N * 4; }
+size_t ring_mul_smem(int nprimes) { return (size_t)nprimes * 2 * RING_N * 4; }
 
 void launch_ring_mul(const RingPlan& rp, const RingPrimeDev* rps_dev, const void* a, const void* b, void* c, size_t n,
                      int* status, cudaStream_t s) {

@@ -82,3 +82,12 @@ def test_device_challenges_match_oracle(prover, oracle, prefix):
     want = oracle.short_challenges("labinius/test/batch", prefix, 64)
     got = prover.sample_challenges("labinius/test/batch", prefix, 64)
     assert got == want
+
+
+@pytest.mark.parametrize("prefix", [b"many", bytes(range(200))], ids=["4-byte", "200B"])
+def test_many_device_challenges_match_oracle(prover, oracle, prefix):
+    # 4096 challenges: about half a million norm evaluations, a few of them inside the band
+    # around the bound where the sampler repeats the f64 arithmetic.
+    want = oracle.short_challenges("labinius/test/many", prefix, 4096)
+    got = prover.sample_challenges("labinius/test/many", prefix, 4096)
+    assert got == want
