@@ -13,6 +13,7 @@
 //
 // Results modulo each prime are recombined by Garner's CRT. For Q = 3889*9721*17497 (the three
 // primes of solution-arm/proof_generate/src/ntt.rs:37-40) the recombination is already modulo Q.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -417,7 +418,7 @@ static double commit_bit_value(int kappa) {
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_commit_tc(const uint4* __restrict__ table, const uint32_t* __restrict__ key, const uint4* __restrict__ btiles,
                 const PrimeConst* __restrict__ pcs, uint32_t* __restrict__ partial, int rl, int elements,
-                int per_split, int nprimes, int* status) {
+                int per_split, int nprimes, int split_base, int* status) {
   extern __shared__ __align__(1024) uint8_t tsm[];
   uint8_t* sA = tsm;
   uint8_t* sB = tsm + 4 * TC_A_BYTES;
@@ -428,7 +429,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
   const int pi = blockIdx.x / 3, third = blockIdx.x % 3;
   const int col0 = blockIdx.y * TC_COLS;
-  const int split = blockIdx.z;
+  const int split = split_base + (int)blockIdx.z;
   const int m_begin = split * per_split;
   const int nelem = max(0, min(elements, m_begin + per_split) - m_begin);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -652,17 +653,27 @@ int commit_splits(uint64_t elements, int nprimes, int sms) {
 }
 
 void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint32_t* key,
-                   const uint16_t* btiles, uint32_t* partial, int splits, int* status, cudaStream_t s) {
+                   const uint16_t* btiles, uint32_t* partial, int splits, int* status, cudaStream_t s, int split_begin,
+                   int split_end) {
   const int elements = (int)sh.ring_elements;
   const int per = (elements + splits - 1) / splits;
+  if (split_end < 0) split_end = splits;
+  if (split_end <= split_begin) return;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_commit_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     attr = true;
   }
-  dim3 grid(mp.nprimes * 3, COLUMNS / TC_COLS, splits);
+  dim3 grid(mp.nprimes * 3, COLUMNS / TC_COLS, split_end - split_begin);
   k_commit_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(table, key, reinterpret_cast<const uint4*>(btiles), mp.dconsts, partial,
-                                                 sh.rl, elements, per, mp.nprimes, status);
+                                                 sh.rl, elements, per, mp.nprimes, split_begin, status);
+}
+
+// Element range [m0, m1) of split range [s0, s1): the part of every column those splits read.
+void commit_split_elements(uint64_t elements, int splits, int s0, int s1, uint64_t& m0, uint64_t& m1) {
+  const uint64_t per = (elements + splits - 1) / splits;
+  m0 = std::min<uint64_t>(elements, (uint64_t)s0 * per);
+  m1 = std::min<uint64_t>(elements, (uint64_t)s1 * per);
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -140,6 +140,10 @@ void launch_chunk_cvs(const uint8_t* stream, uint64_t nchunks, const uint32_t ke
 void launch_subtrees(uint32_t* cvs, uint32_t* scratch, uint64_t nchunks, const uint32_t key[8], uint32_t mode,
                      uint32_t* out, cudaStream_t s);
 
+// One device write of zero per 4 KB of a host buffer the device reaches through the host's page
+// tables (and its last byte), so later copies into it find the pages already mapped for the device.
+void launch_touch_pages(uint8_t* host, size_t n, cudaStream_t s);
+
 // ---- launch wrappers (lf_commit.cu) ----
 // The public matrix reduced modulo each prime: ared[prime][m][648].
 void launch_matrix_expand(const ModulusPlan& mp, uint64_t elements, uint32_t* ared, cudaStream_t s);
@@ -149,8 +153,11 @@ void launch_matrix_raw(u128 q, uint64_t elements, void* out, cudaStream_t s);
 void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32_t* ared, uint32_t* leafvals,
                           uint32_t* key, cudaStream_t s);
 int commit_splits(uint64_t elements, int nprimes, int sms);
+// Splits [split_begin, split_end) of the `splits` element splits (split_end < 0: all of them).
 void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint32_t* key,
-                   const uint16_t* btiles, uint32_t* partial, int splits, int* status, cudaStream_t s);
+                   const uint16_t* btiles, uint32_t* partial, int splits, int* status, cudaStream_t s,
+                   int split_begin = 0, int split_end = -1);
+void commit_split_elements(uint64_t elements, int splits, int s0, int s1, uint64_t& m0, uint64_t& m1);
 void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t* partial, int splits, uint8_t* out,
                           cudaStream_t s, int ncols = COLUMNS);
 // Verifier pieces (lf_commit.cu): a_times_v into `out` (648 coefficients of `width` bytes) and

@@ -504,6 +504,18 @@ void launch_ghash_mul(const void* a, const void* b, void* c, size_t n, int sms, 
                                                reinterpret_cast<uint4*>(c), n);
 }
 
+__global__ void k_touch_pages(uint8_t* __restrict__ p, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t pages = (n + 4095) / 4096;
+  if (i < pages) p[i * 4096] = 0;
+  if (i == 0 && n) p[n - 1] = 0;
+}
+
+void launch_touch_pages(uint8_t* host, size_t n, cudaStream_t s) {
+  const size_t pages = (n + 4095) / 4096;
+  if (pages) k_touch_pages<<<(unsigned)((pages + 255) / 256), 256, 0, s>>>(host, n);
+}
+
 __global__ void k_widen_i16(const int16_t* __restrict__ v, int32_t* __restrict__ out, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     out[i] = v[i];
