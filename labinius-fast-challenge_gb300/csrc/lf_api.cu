@@ -219,7 +219,7 @@ struct lf_ctx {
   std::vector<std::unique_ptr<RingCache>> rings;  // lf_ring_mul plans, oldest evicted first
   KeyCache* key = nullptr;                      // the key of the proof in progress
   uint64_t key_clock = 0;
-  DevBuf table, stream_buf, partial, sblk, ehi, elo, lo_planes, rhi, vparts, psi, batch, soa, msg, p0, eqt, row,
+  DevBuf table, stream_buf, partial, sblk, ehi, elo, rhi, vparts, psi, batch, soa, msg, p0, eqt, row,
       hasher, chal, fold, cvs, cvs_scratch, subtrees, status, phase, scratch_small, wbuf, rbuf;
   uint32_t sign_key[8];
   std::vector<uint8_t> host_fold;
@@ -424,15 +424,13 @@ int device_partials(lf_ctx* ctx, const uint4* table, const Shape& sh, const std:
   CK(ctx->rhi.ensure(64 * 16));
   CK(ctx->elo.ensure(4096 * 16));
   CK(ctx->ehi.ensure(nblocks * 16));
-  CK(ctx->lo_planes.ensure(4096 * 256));  // E_lo expanded to bf16 rows (32 tiles of 128)
   CK(ctx->sblk.ensure(nblocks * 128 * 16));
   CK(ctx->vparts.ensure(256 * 8));
   CK(ctx->status.ensure(16));
   CK(cudaMemcpyAsync(ctx->rhi.p, hi.data(), 16 * hi.size(), cudaMemcpyHostToDevice, st));
   launch_eq_b128(ctx->rhi.as<b128>() + HB, LB, ctx->elo.as<b128>(), st);
   launch_eq_b128(ctx->rhi.as<b128>(), HB, ctx->ehi.as<b128>(), st);
-  launch_expand_rows(ctx->elo.as<b128>(), 4096, ctx->lo_planes.as<uint8_t>(), st);
-  launch_sblock(table, nblocks, ctx->lo_planes.as<uint8_t>(), ctx->sblk.as<uint8_t>(), ctx->status.as<int>(), st);
+  launch_sblock(table, nblocks, ctx->elo.as<b128>(), ctx->sblk.as<uint8_t>(), ctx->status.as<int>(), st);
   CK(cudaMemsetAsync(ctx->vparts.p, 0, 256 * 8, st));
   launch_partials_combine(ctx->ehi.as<b128>(), ctx->sblk.as<uint8_t>(), (int)nblocks,
                           ctx->vparts.as<unsigned long long>(), st);
@@ -1322,7 +1320,7 @@ void lf_ctx_destroy(lf_ctx* ctx) {
   for (lf_ctx* l : ctx->lanes) lf_ctx_destroy(l);
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  DevBuf* bufs[] = {&ctx->table, &ctx->stream_buf, &ctx->partial, &ctx->sblk, &ctx->ehi, &ctx->elo, &ctx->lo_planes,
+  DevBuf* bufs[] = {&ctx->table, &ctx->stream_buf, &ctx->partial, &ctx->sblk, &ctx->ehi, &ctx->elo,
                     &ctx->rhi, &ctx->vparts, &ctx->psi, &ctx->batch, &ctx->soa, &ctx->msg, &ctx->p0, &ctx->eqt,
                     &ctx->row, &ctx->hasher, &ctx->chal, &ctx->fold, &ctx->cvs, &ctx->cvs_scratch, &ctx->subtrees,
                     &ctx->status, &ctx->phase, &ctx->scratch_small, &ctx->wbuf, &ctx->rbuf};

@@ -107,8 +107,8 @@ struct Challenge {
 // ---- launch wrappers (lf_switch.cu) ----
 void launch_eq_b128(const b128* r, int n, b128* out, cudaStream_t s);
 void launch_eq_table_f162(const f162* ps, int n, f162* out, cudaStream_t s);
-void launch_expand_rows(const b128* x, int n, uint8_t* rows, cudaStream_t s);
-void launch_sblock(const uint4* table, uint64_t nblocks, const uint8_t* elo_rows, uint8_t* sblk, int* status,
+// S blocks: E_lo (4096 GHASH entries) as 16-byte words; each block expands the k-tile's rows itself.
+void launch_sblock(const uint4* table, uint64_t nblocks, const b128* elo, uint8_t* sblk, int* status,
                    cudaStream_t s);
 void launch_partials_combine(const b128* ehi, const uint8_t* sblk, int nblocks, unsigned long long* v, cudaStream_t s);
 void launch_psi_tables(const f162* batch, f162* tab, cudaStream_t s);

@@ -262,8 +262,8 @@ constexpr int FT_TILE = 128 * 128 * 2;          // A tile: 128 words x 128 bits,
 constexpr int FT_STAGES = 4;                    // A tiles (read by the MMAs)
 constexpr int FT_RING = 8;                      // strips and raw words, loaded FT_AHEAD columns early
 constexpr int FT_AHEAD = 3;
-constexpr int FT_THREADS = 128;
-constexpr int FT_SMEM = FT_RING * FT_STRIP + FT_STAGES * FT_TILE + FT_RING * 128 * 16 + 64;
+constexpr int FT_THREADS = 256;                  // two threads per table word (a half each)
+constexpr int FT_SMEM = FT_RING * FT_STRIP + FT_STAGES * FT_TILE + FT_RING * FT_THREADS * 16 + 64;
 constexpr long long FT_WAIT_CYCLES = 2000000000LL;
 
 // Strip of column j: core e holds element (r, i) = C_j[303 - (8 e + r + i)] / 2 as bf16.
@@ -290,10 +290,11 @@ __global__ void __launch_bounds__(128) k_fold_cores(const Challenge* __restrict_
 
 // Word -> row r of an A tile, bits in natural order: u32 s of chunk q holds bits 8q + 2s (low
 // bf16) and 8q + 2s + 1 (high bf16) as 2.0 or 0.
-__device__ __forceinline__ void fold_write_row(uint8_t* tile, int r, uint4 v) {
+__device__ __forceinline__ void fold_write_row(uint8_t* tile, int r, uint4 v, int half) {
   const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-  for (int q = 0; q < 16; ++q) {
+  for (int qq = 0; qq < 8; ++qq) {
+    const int q = 8 * half + qq;  // this thread's half of the word: bits 64 half .. 64 half + 63
     const uint32_t x = xs[q >> 2];
     uint32_t u[4];
 #pragma unroll
@@ -315,16 +316,17 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   extern __shared__ __align__(1024) uint8_t fsm[];
   uint8_t* sS = fsm;                                   // [FT_RING][FT_STRIP] (first: reads past a strip stay in smem)
   uint8_t* sA = fsm + FT_RING * FT_STRIP;              // [FT_STAGES][FT_TILE]
-  uint4* sW = reinterpret_cast<uint4*>(sA + FT_STAGES * FT_TILE);  // [FT_RING][128] raw words
-  uint64_t* done = reinterpret_cast<uint64_t*>(sW + FT_RING * 128);  // [FT_STAGES]
+  uint4* sW = reinterpret_cast<uint4*>(sA + FT_STAGES * FT_TILE);  // [FT_RING][FT_THREADS] raw words
+  uint64_t* done = reinterpret_cast<uint64_t*>(sW + FT_RING * FT_THREADS);  // [FT_STAGES]
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + FT_STAGES);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = tid & 127, half = tid >> 7;       // the word (A row) and which half of it
   const uint64_t words = 4 * ring_elements;
   const uint64_t w0 = (uint64_t)blockIdx.x * 128;  // first word (row) of the block
   const int split = blockIdx.y;
   const int c_begin = split * cols_per_split, c_end = min(COLUMNS, c_begin + cols_per_split);
-  const bool live = w0 + tid < words;
+  const bool live = w0 + row < words;
   if (tid == 0) {
     *abort_flag = 0;
     for (int i = 0; i < FT_STAGES; ++i) tc::mbar_init(&done[i], 1);
@@ -346,7 +348,7 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
       const int slot = (c - c_begin) % FT_RING;
       const uint4* src = strips + (size_t)c * (FT_STRIP / 16);
       for (int i = tid; i < FT_STRIP / 16; i += FT_THREADS) tc::cp_async16(sS + slot * FT_STRIP + 16 * i, src + i);
-      if (live) tc::cp_async16(sW + slot * 128 + tid, table + ((uint64_t)c << rl) + w0 + tid);
+      if (live) tc::cp_async16(sW + slot * FT_THREADS + tid, table + ((uint64_t)c << rl) + w0 + row);
     }
     tc::cp_async_commit();
   };
@@ -366,7 +368,7 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
     fetch(c + FT_AHEAD);
     tc::cp_async_wait<FT_AHEAD>();  // column c's group has landed
     const bool go = !*abort_flag;
-    if (go) fold_write_row(sA + s * FT_TILE, tid, live ? sW[slot * 128 + tid] : make_uint4(0, 0, 0, 0));
+    if (go) fold_write_row(sA + s * FT_TILE, row, live ? sW[slot * FT_THREADS + tid] : make_uint4(0, 0, 0, 0), half);
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
@@ -402,8 +404,9 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   // Ring reduction per row into shared memory (the stages are free now): fin[row][i], i < 162.
   int32_t* fin = reinterpret_cast<int32_t*>(fsm);
   const int FS = N162 + 1;
-  for (int i = 0; i < N162; ++i) fin[tid * FS + i] = 0;
-  if (ok && ncols > 0) {
+  if (tid < 128)
+    for (int i = 0; i < N162; ++i) fin[tid * FS + i] = 0;
+  if (ok && ncols > 0 && tid < 128) {  // warps 0-3: TMEM lanes 32 w .. 32 w + 31 = the block's rows
 #pragma unroll 1
     for (int n0 = 0; n0 < 304; n0 += 16) {
       uint32_t v[16];

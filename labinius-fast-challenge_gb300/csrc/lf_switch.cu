@@ -52,8 +52,9 @@ __global__ void k_eq_table_f162(const f162* __restrict__ ps, int n, f162* __rest
 // an exact integer in f32. Both operands are the words expanded to bf16 rows
 // (tc::write_row), read MN-major: row = entry j (K), 128 bit positions along M (table word) or
 // N (E_lo). A block takes two h; the 4096 entries run in 32 k-tiles of 128 through two shared
-// memory stages, so the expansion of tile t + 1 overlaps the MMAs of tile t. E_lo's rows are
-// expanded once per proof (k_expand_rows) and streamed with cp.async. D for both h sits in TMEM
+// memory stages, so the expansion of tile t + 1 overlaps the MMAs of tile t. Every block expands
+// the tile's E_lo rows itself from the 16-byte entries (2 KB per tile from L2, instead of 32 KB of
+// expanded rows); the words of both operands are loaded two tiles ahead. D for both h sits in TMEM
 // (2 x 128 columns). Set bits are bf16 2.0 in both operands, so D = 4 x count (<= 16384, exact);
 // the count's parity is bit 2 of the f32 mantissa after adding 2^23. Waits are bounded; a
 // timeout sets *status = 4.
@@ -63,13 +64,8 @@ constexpr int SBT_TILE = 128 * 128 * 2;                       // 128 entries x 1
 constexpr int SBT_SMEM = 2 * SBT_TILE + 2 * 2 * SBT_TILE + 64;  // [B0][B1][A0: 2 h][A1: 2 h][barriers]
 constexpr long long SBT_WAIT_CYCLES = 2000000000LL;
 
-__global__ void k_expand_rows(const uint4* __restrict__ x, int n, uint8_t* __restrict__ rows) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < n) tc::write_row(rows + (size_t)(j >> 7) * SBT_TILE, j & 127, x[j]);
-}
-
 __global__ void __launch_bounds__(SBT_THREADS, 1)
-    k_sblock_tc(const uint4* __restrict__ table, uint64_t nblocks, const uint4* __restrict__ elo_rows,
+    k_sblock_tc(const uint4* __restrict__ table, uint64_t nblocks, const uint4* __restrict__ elo,
                 uint8_t* __restrict__ sblk, int* status) {
   extern __shared__ __align__(1024) uint8_t sbs[];
   uint8_t* sB = sbs;                  // stage s at sB + s * SBT_TILE (E_lo rows of the k-tile)
@@ -99,7 +95,13 @@ __global__ void __launch_bounds__(SBT_THREADS, 1)
     return __all_sync(0xffffffffu, r);
   };
 
+  // The k-tile's operands are expanded here from 16-byte words (the block's table entries and the
+  // E_lo entries 128 t .. 128 t + 127, which every block shares from L2); the words are loaded two
+  // k-tiles ahead. Threads 0-127 also expand one E_lo row each.
   uint4 w = live ? src[0] : make_uint4(0, 0, 0, 0);
+  uint4 w1 = live ? src[128] : make_uint4(0, 0, 0, 0);
+  uint4 e = tid < 128 ? elo[tid] : make_uint4(0, 0, 0, 0);
+  uint4 e1 = tid < 128 ? elo[128 + tid] : make_uint4(0, 0, 0, 0);
   int last = -1;  // k-tile of the issuer's last commit
   for (int t = 0; t < 32; ++t) {
     const int s = t & 1;
@@ -109,12 +111,14 @@ __global__ void __launch_bounds__(SBT_THREADS, 1)
     }
     const bool go = !*abort_flag;
     if (go) {
-      const uint4* bsrc = elo_rows + (size_t)t * (SBT_TILE / 16);
-      for (int i = tid; i < SBT_TILE / 16; i += SBT_THREADS) tc::cp_async16(sB + s * SBT_TILE + 16 * i, bsrc + i);
       tc::write_row(sA + (2 * s + hb) * SBT_TILE, j, w);
+      if (tid < 128) tc::write_row(sB + s * SBT_TILE, tid, e);
     }
-    if (t + 1 < 32) w = live ? src[(t + 1) * 128] : make_uint4(0, 0, 0, 0);
-    tc::cp_async_wait_all();
+    w = w1, e = e1;
+    if (t + 2 < 32) {
+      w1 = live ? src[(t + 2) * 128] : make_uint4(0, 0, 0, 0);
+      if (tid < 128) e1 = elo[(t + 2) * 128 + tid];
+    }
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
@@ -439,10 +443,7 @@ void launch_eq_table_f162(const f162* ps, int n, f162* out, cudaStream_t s) {
   uint64_t N = 1ull << n;
   k_eq_table_f162<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(ps, n, out);
 }
-void launch_expand_rows(const b128* x, int n, uint8_t* rows, cudaStream_t s) {
-  k_expand_rows<<<(n + 127) / 128, 128, 0, s>>>(reinterpret_cast<const uint4*>(x), n, rows);
-}
-void launch_sblock(const uint4* table, uint64_t nblocks, const uint8_t* elo_rows, uint8_t* sblk, int* status,
+void launch_sblock(const uint4* table, uint64_t nblocks, const b128* elo, uint8_t* sblk, int* status,
                    cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
@@ -450,7 +451,7 @@ void launch_sblock(const uint4* table, uint64_t nblocks, const uint8_t* elo_rows
     attr = true;
   }
   k_sblock_tc<<<(unsigned)((nblocks + 1) / 2), SBT_THREADS, SBT_SMEM, s>>>(
-      table, nblocks, reinterpret_cast<const uint4*>(elo_rows), sblk, status);
+      table, nblocks, reinterpret_cast<const uint4*>(elo), sblk, status);
 }
 void launch_partials_combine(const b128* ehi, const uint8_t* sblk, int nblocks, unsigned long long* v, cudaStream_t s) {
   int run = 16;
