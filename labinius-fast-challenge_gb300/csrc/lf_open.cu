@@ -259,10 +259,10 @@ constexpr int RAW_Y = 128 + 161;                // 289 raw positions
 constexpr int FT_CORES = 53;                    // cores per column strip
 constexpr int FT_STRIP = FT_CORES * 128;        // 6784 bytes
 constexpr int FT_TILE = 128 * 128 * 2;          // A tile: 128 words x 128 bits, bf16
-constexpr int FT_STAGES = 4;                    // A tiles (read by the MMAs)
+constexpr int FT_STAGES = 3;                    // A tiles (read by the MMAs)
 constexpr int FT_RING = 8;                      // strips and raw words, loaded FT_AHEAD columns early
 constexpr int FT_AHEAD = 3;
-constexpr int FT_THREADS = 256;                  // two threads per table word (a half each)
+constexpr int FT_THREADS = 512;                  // four threads per table word (a quarter each)
 constexpr int FT_SMEM = FT_RING * FT_STRIP + FT_STAGES * FT_TILE + FT_RING * FT_THREADS * 16 + 64;
 constexpr long long FT_WAIT_CYCLES = 2000000000LL;
 
@@ -290,11 +290,11 @@ __global__ void __launch_bounds__(128) k_fold_cores(const Challenge* __restrict_
 
 // Word -> row r of an A tile, bits in natural order: u32 s of chunk q holds bits 8q + 2s (low
 // bf16) and 8q + 2s + 1 (high bf16) as 2.0 or 0.
-__device__ __forceinline__ void fold_write_row(uint8_t* tile, int r, uint4 v, int half) {
+__device__ __forceinline__ void fold_write_row(uint8_t* tile, int r, uint4 v, int part) {
   const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-  for (int qq = 0; qq < 8; ++qq) {
-    const int q = 8 * half + qq;  // this thread's half of the word: bits 64 half .. 64 half + 63
+  for (int qq = 0; qq < 16 * 128 / FT_THREADS; ++qq) {
+    const int q = 16 * 128 / FT_THREADS * part + qq;  // this thread's share of the word's 16 chunks
     const uint32_t x = xs[q >> 2];
     uint32_t u[4];
 #pragma unroll
@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + FT_STAGES);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int row = tid & 127, half = tid >> 7;       // the word (A row) and which half of it
+  const int row = tid & 127, half = tid >> 7;       // the word (A row) and which quarter of it
   const uint64_t words = 4 * ring_elements;
   const uint64_t w0 = (uint64_t)blockIdx.x * 128;  // first word (row) of the block
   const int split = blockIdx.y;
