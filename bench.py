@@ -277,7 +277,11 @@ def batched_leg(lfgpu, prover, n=32, seed=20260):
         hosts[i] = h
         jobs.append(prover.make_job(s, h.data_ptr(), lv, nbytes=h.numel()))
     torch.cuda.synchronize()
-    prover.prove_batch(jobs)  # buffers of every lane grown, pages touched
+    prover.prove_batch(jobs)  # pages touched, keys and buffers of the shapes each lane took
+    big = max(range(n), key=lambda i: shapes[i])
+    for _ in range(2):  # the largest shape once per lane, so no lane grows a buffer while timed
+        prover.prove_batch([prover.make_job(seeds(1, 200 + big)[0], hosts[big].data_ptr(), shapes[big],
+                                            nbytes=hosts[big].numel()) for _ in range(max(prover.lanes or 4, 1))])
     for lv in sorted(set(shapes)):
         prover.key_prepare(lv)  # every lane holds every shape's key
     runs = []

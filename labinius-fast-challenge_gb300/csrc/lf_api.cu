@@ -182,6 +182,25 @@ struct DevBuf {
   }
 };
 
+// Stream-ordered scratch: allocated and freed on one stream from the device's memory pool, so
+// freeing it does not wait for the whole device (a cudaFree would, stalling the other lanes and a
+// table upload running on the copy stream).
+struct StreamBuf {
+  void* p = nullptr;
+  cudaStream_t s;
+  explicit StreamBuf(cudaStream_t st) : s(st) {}
+  StreamBuf(const StreamBuf&) = delete;
+  StreamBuf& operator=(const StreamBuf&) = delete;
+  ~StreamBuf() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  cudaError_t alloc(size_t n) { return cudaMallocAsync(&p, n, s); }
+  template <class T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
 // The commitment key of one (Q, ring elements per column): built once on the device, kept.
 struct KeyCache {
   u128 q = 0;
@@ -226,6 +245,7 @@ struct lf_ctx {
   cudaEvent_t ev[16];
   // batches: a second table buffer and a copy stream, so the next table uploads during a proof
   DevBuf table2, fold_strips, fold_part;
+  DevBuf kb_ared, kb_leaf, kb_matrix;  // key-build scratch (matrix residues, leaf values, XOF blocks)
   int nlanes = 4;                // proofs in flight at once: this context and nlanes - 1 lanes
   std::vector<lf_ctx*> lanes;    // contexts on the same device (own stream, buffers, keys)
   std::mutex lanemu;             // guards lanes (created on first use, only added to)
@@ -324,7 +344,8 @@ cudaError_t upload_phase_tables(void* dst) {
 // a key build. Used for admission against the context's HBM budget.
 size_t proof_footprint(const Shape& sh, bool host_table, int sms, int nprimes) {
   const size_t key = (size_t)nprimes * sh.ring_elements * LEAVES * 64;
-  const size_t build = (size_t)nprimes * sh.ring_elements * (RING_N + 4 * LEAVES) * 4;
+  const size_t build = (size_t)nprimes * sh.ring_elements * (RING_N + 4 * LEAVES) * 4 +
+                       matrix_scratch_bytes(sh.ring_elements, ~(u128)0 >> 32);  // widest coefficients
   const size_t partial =
       (size_t)commit_splits(sh.ring_elements, nprimes, sms) * nprimes * COLUMNS * LEAVES * 16;
   const size_t blocks = (sh.words / 4096) * (128 * 16 + 16);
@@ -378,9 +399,14 @@ int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh, int extra_bits = 0) {
     }
     std::unique_ptr<KeyCache> kc(new KeyCache());
     const uint64_t E = sh.ring_elements;
-    DevBuf ared, leaf;
+    // key-build scratch stays with the context (grown, never freed mid-run: a cudaFree would wait
+    // for the whole device, including a table upload on the copy stream and the other lanes)
+    DevBuf& ared = ctx->kb_ared;
+    DevBuf& leaf = ctx->kb_leaf;
+    DevBuf& mscratch = ctx->kb_matrix;
     CK(ared.ensure((size_t)mp.nprimes * E * RING_N * 4));
     CK(leaf.ensure((size_t)mp.nprimes * E * 4 * LEAVES * 4));
+    CK(mscratch.ensure(matrix_scratch_bytes(E, q)));
     CK(kc->key.ensure((size_t)mp.nprimes * E * LEAVES * 16 * 4));
     CK(kc->btiles.ensure(mp.btiles.size() * 2));
     CK(cudaMemcpyAsync(kc->btiles.p, mp.btiles.data(), mp.btiles.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
@@ -388,12 +414,10 @@ int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh, int extra_bits = 0) {
     CK(cudaMemcpyAsync(kc->consts.p, mp.consts.data(), sizeof(PrimeConst) * mp.nprimes, cudaMemcpyHostToDevice,
                        ctx->stream));
     mp.dconsts = kc->consts.as<PrimeConst>();
-    launch_matrix_expand(mp, E, ared.as<uint32_t>(), ctx->stream);
+    launch_matrix_expand(mp, E, ared.as<uint32_t>(), mscratch.p, ctx->stream);
     launch_key_transform(mp, E, ared.as<uint32_t>(), leaf.as<uint32_t>(), kc->key.as<uint32_t>(), ctx->stream);
     CKL("key build");
     CK(cudaStreamSynchronize(ctx->stream));
-    ared.release();
-    leaf.release();
     kc->mp = mp;
     kc->q = q;
     kc->elements = E;
@@ -1094,9 +1118,9 @@ int verify_device(lf_ctx* ctx, const uint8_t seed[32], const Shape& sh, const ui
   t.counter += COLUMNS;
   CK(cudaMemcpyAsync(ctx->p0.p, p0.data(), 24 * p0.size(), cudaMemcpyHostToDevice, st));
   launch_eq_table_f162(ctx->p0.as<f162>(), sh.rl, ctx->eqt.as<f162>(), st);
-  DevBuf vdev, vred, vhat, part, atv, chpart, checks;
-  CK(vdev.ensure(4 * nv));
-  CK(checks.ensure(64));
+  StreamBuf vdev(st), vred(st), vhat(st), part(st), atv(st), chpart(st), checks(st);
+  CK(vdev.alloc(4 * nv));
+  CK(checks.alloc(64));
   CK(cudaMemcpyAsync(vdev.p, pr.folded, 4 * nv, cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(checks.p, 0, 64, st));
   launch_fold_checks(vdev.as<int32_t>(), E, ctx->eqt.as<f162>(), checks.as<unsigned long long>(), st);
@@ -1105,11 +1129,11 @@ int verify_device(lf_ctx* ctx, const uint8_t seed[32], const Shape& sh, const ui
     int rc2 = ensure_key(ctx, q, sh, 15);  // |v| <= 2^15
     if (rc2) return rc2;
     const ModulusPlan& mp = ctx->key->mp;
-    CK(vred.ensure((size_t)mp.nprimes * nv * 4));
-    CK(vhat.ensure((size_t)mp.nprimes * E * 4 * LEAVES * 4));
-    CK(part.ensure((size_t)mp.nprimes * COLUMNS * LEAVES * 16));
-    CK(atv.ensure(RING_N * w + 64));
-    CK(chpart.ensure((size_t)32 * (2 * RING_N - 1) * 16));
+    CK(vred.alloc((size_t)mp.nprimes * nv * 4));
+    CK(vhat.alloc((size_t)mp.nprimes * E * 4 * LEAVES * 4));
+    CK(part.alloc((size_t)mp.nprimes * COLUMNS * LEAVES * 16));
+    CK(atv.alloc(RING_N * w + 64));
+    CK(chpart.alloc((size_t)32 * (2 * RING_N - 1) * 16));
     launch_commit_range(commit_dev, (uint32_t)w, q, (uint64_t)COLUMNS * RING_N, checks.as<unsigned long long>() + 6, st);
     launch_a_times_v(mp, sh, vdev.as<int32_t>(), ctx->key->key.as<uint32_t>(), vred.as<uint32_t>(),
                      vhat.as<uint32_t>(), part.as<uint32_t>(), atv.as<uint8_t>(), st);
@@ -1327,6 +1351,9 @@ void lf_ctx_destroy(lf_ctx* ctx) {
   ctx->keys.clear();
   for (DevBuf* b : bufs) b->release();
   ctx->table2.release();
+  ctx->kb_ared.release();
+  ctx->kb_leaf.release();
+  ctx->kb_matrix.release();
   ctx->fold_strips.release();
   ctx->fold_part.release();
   for (auto& ev : ctx->ev) cudaEventDestroy(ev);
@@ -1718,7 +1745,9 @@ int lf_ajtai_matrix_device(lf_ctx* ctx, const uint8_t q_le[16], uint64_t element
   std::lock_guard<std::mutex> g(ctx->mu);
   cudaSetDevice(ctx->device);
   if (!elements) return LF_OK;
-  launch_matrix_raw(q, elements, out_dev, ctx->stream);
+  StreamBuf mscratch(ctx->stream);
+  CK(mscratch.alloc(matrix_scratch_bytes(elements, q)));
+  launch_matrix_raw(q, elements, out_dev, mscratch.p, ctx->stream);
   CKL("matrix expansion");
   CK(cudaStreamSynchronize(ctx->stream));
   return LF_OK;
@@ -1740,12 +1769,12 @@ int lf_a_times_v(lf_ctx* ctx, const uint8_t q_le[16], uint64_t elements, const i
   if (rc) return rc;
   const ModulusPlan& mp = ctx->key->mp;
   const size_t nv = (size_t)elements * RING_N, w = mp.width;
-  DevBuf v32, vred, vhat, part, atv;
-  CK(v32.ensure(4 * nv));
-  CK(vred.ensure((size_t)mp.nprimes * nv * 4));
-  CK(vhat.ensure((size_t)mp.nprimes * elements * 4 * LEAVES * 4));
-  CK(part.ensure((size_t)mp.nprimes * COLUMNS * LEAVES * 16));
-  CK(atv.ensure(RING_N * w + 64));
+  StreamBuf v32(ctx->stream), vred(ctx->stream), vhat(ctx->stream), part(ctx->stream), atv(ctx->stream);
+  CK(v32.alloc(4 * nv));
+  CK(vred.alloc((size_t)mp.nprimes * nv * 4));
+  CK(vhat.alloc((size_t)mp.nprimes * elements * 4 * LEAVES * 4));
+  CK(part.alloc((size_t)mp.nprimes * COLUMNS * LEAVES * 16));
+  CK(atv.alloc(RING_N * w + 64));
   launch_widen_i16(v_dev, v32.as<int32_t>(), nv, ctx->stream);
   launch_a_times_v(mp, sh, v32.as<int32_t>(), ctx->key->key.as<uint32_t>(), vred.as<uint32_t>(), vhat.as<uint32_t>(),
                    part.as<uint32_t>(), atv.as<uint8_t>(), ctx->stream);

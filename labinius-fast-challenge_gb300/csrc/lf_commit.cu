@@ -217,7 +217,10 @@ struct MatrixArgs {
 };
 
 // With `raw` set, the coefficients themselves are written (u128 little-endian), else their residues.
-__global__ void k_matrix_expand(MatrixArgs a, uint64_t elements, uint32_t* ared, uint4* raw) {
+// With `only_if` set, the kernel does nothing unless *only_if is nonzero (the fallback of the
+// parallel expansion below, launched behind it on the same stream).
+__global__ void k_matrix_expand(MatrixArgs a, uint64_t elements, uint32_t* ared, uint4* raw, const int* only_if) {
+  if (only_if && *only_if == 0) return;
   uint64_t m = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (m >= elements) return;
   bk::Hasher h;
@@ -266,7 +269,116 @@ __global__ void k_matrix_expand(MatrixArgs a, uint64_t elements, uint32_t* ared,
   }
 }
 
-void launch_matrix_expand(const ModulusPlan& mp, uint64_t elements, uint32_t* ared, cudaStream_t s) {
+// The same expansion in parallel. Draw i of an element always sits at bytes [i w, (i + 1) w) of its
+// XOF stream (a rejected draw still consumes its bytes), so: one thread per element derives the
+// stream's root node; one thread per (element, 64-byte block) produces the first MX_DRAWS draws'
+// blocks; one warp per element then tests 32 draws at a time and gives each accepted draw its
+// coefficient index by a ballot prefix count. Every modulus accepts a draw with probability
+// q / 2^bits > 1/2, so 1600 draws fall short of 648 acceptances with probability below 1e-13 per
+// element; if one does, a flag releases the sequential kernel for the whole matrix.
+constexpr int MX_DRAWS = 1600;
+
+__global__ void k_matrix_roots(MatrixArgs a, uint64_t elements, uint64_t m0, uint64_t count, bk::Pending* roots) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const uint64_t m = m0 + i;
+  bk::Hasher h;
+  uint8_t key[32];
+  for (int k = 0; k < 32; ++k) key[k] = 0x5a;
+  h.init_keyed(key);
+  const char dom[] = "labinius-fast/ajtai-matrix/v1";
+  h.absorb((const uint8_t*)dom, sizeof(dom) - 1);
+  uint8_t b[16];
+  for (int k = 0; k < 8; ++k) b[k] = (uint8_t)(a.q_lo >> (8 * k)), b[8 + k] = (uint8_t)(a.q_hi >> (8 * k));
+  h.absorb(b, 16);
+  h.absorb_u64(elements);
+  h.absorb_u64(m);
+  roots[i] = h.finish();
+}
+
+__global__ void k_matrix_xof(const bk::Pending* __restrict__ roots, uint64_t count, int nblk, uint4* __restrict__ buf) {
+  const uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (g >= count * (uint64_t)nblk) return;
+  const uint64_t i = g / nblk, blk = g % nblk;
+  uint32_t w[16];
+  roots[i].root_block(blk, w);
+  uint4* o = buf + g * 4;
+  o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+  o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+  o[2] = make_uint4(w[8], w[9], w[10], w[11]);
+  o[3] = make_uint4(w[12], w[13], w[14], w[15]);
+}
+
+__global__ void __launch_bounds__(256) k_matrix_draw(MatrixArgs a, uint64_t elements, uint64_t m0, uint64_t count,
+                                                     int nblk, const uint8_t* __restrict__ buf,
+                                                     uint32_t* __restrict__ ared, uint4* __restrict__ raw,
+                                                     int* short_flag) {
+  const uint64_t i = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= count) return;
+  const uint64_t m = m0 + i;
+  const uint8_t* src = buf + i * (uint64_t)nblk * 64;
+  const u128 q = ((u128)a.q_hi << 64) | a.q_lo;
+  const u128 mask = a.bits >= 128 ? ~(u128)0 : (((u128)1 << a.bits) - 1);
+  int accepted = 0;
+  for (int base = 0; base < MX_DRAWS && accepted < RING_N; base += 32) {
+    const int d = base + lane;
+    u128 v = 0;
+    bool ok = false;
+    if (d < MX_DRAWS) {
+      const uint8_t* p = src + (size_t)d * a.width;
+      for (int k = (int)a.width - 1; k >= 0; --k) v = (v << 8) | p[k];
+      v &= mask;
+      ok = v < q;
+    }
+    const uint32_t bal = __ballot_sync(0xffffffffu, ok);
+    const int t = accepted + __popc(bal & ((1u << lane) - 1u));
+    if (ok && t < RING_N) {
+      if (raw) {
+        const uint64_t lo = (uint64_t)v, hi = (uint64_t)(v >> 64);
+        raw[m * RING_N + t] = make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
+      } else {
+        const uint64_t lo = (uint64_t)v, hi = (uint64_t)(v >> 64);
+        for (int k = 0; k < a.nprimes; ++k) {
+          const uint64_t pk = a.primes[k];
+          ared[((size_t)k * elements + m) * RING_N + t] = (uint32_t)(((hi % pk) * a.two64[k] + lo % pk) % pk);
+        }
+      }
+    }
+    accepted += __popc(bal);
+  }
+  if (lane == 0 && accepted < RING_N) atomicExch(short_flag, 1);
+}
+
+// Scratch bytes of the parallel expansion per element (the XOF blocks of MX_DRAWS draws).
+static size_t matrix_blocks(uint32_t width) { return ((size_t)MX_DRAWS * width + 63) / 64; }
+size_t matrix_scratch_bytes(uint64_t elements, u128 q) {
+  const uint32_t bits = bits_of(q - 1), width = (bits + 7) / 8;
+  const uint64_t chunk = std::min<uint64_t>(elements, 8192);
+  return chunk * (matrix_blocks(width) * 64 + sizeof(bk::Pending)) + 64;
+}
+
+static void matrix_parallel(const MatrixArgs& a, uint64_t elements, uint32_t* ared, uint4* raw, void* scratch,
+                            cudaStream_t s) {
+  const int nblk = (int)matrix_blocks(a.width);
+  const uint64_t chunk = std::min<uint64_t>(elements, 8192);
+  int* flag = reinterpret_cast<int*>(scratch);
+  bk::Pending* roots = reinterpret_cast<bk::Pending*>(static_cast<uint8_t*>(scratch) + 64);
+  uint8_t* buf = reinterpret_cast<uint8_t*>(roots + chunk);
+  cudaMemsetAsync(flag, 0, 4, s);
+  for (uint64_t m0 = 0; m0 < elements; m0 += chunk) {
+    const uint64_t count = std::min(chunk, elements - m0);
+    k_matrix_roots<<<(unsigned)((count + 127) / 128), 128, 0, s>>>(a, elements, m0, count, roots);
+    const uint64_t nb = count * (uint64_t)nblk;
+    k_matrix_xof<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(roots, count, nblk, reinterpret_cast<uint4*>(buf));
+    k_matrix_draw<<<(unsigned)((count * 32 + 255) / 256), 256, 0, s>>>(a, elements, m0, count, nblk, buf, ared, raw,
+                                                                        flag);
+  }
+  // the sequential expansion, which returns at once unless an element fell short
+  k_matrix_expand<<<(unsigned)((elements + 63) / 64), 64, 0, s>>>(a, elements, ared, raw, flag);
+}
+
+void launch_matrix_expand(const ModulusPlan& mp, uint64_t elements, uint32_t* ared, void* scratch, cudaStream_t s) {
   MatrixArgs a;
   memset(&a, 0, sizeof a);
   a.q_lo = (uint64_t)mp.q;
@@ -278,20 +390,17 @@ void launch_matrix_expand(const ModulusPlan& mp, uint64_t elements, uint32_t* ar
     a.primes[i] = mp.primes[i];
     a.two64[i] = (uint32_t)powmod(powmod(2, 32, mp.primes[i]), 2, mp.primes[i]);
   }
-  int threads = 64;
-  k_matrix_expand<<<(unsigned)((elements + threads - 1) / threads), threads, 0, s>>>(a, elements, ared, nullptr);
+  matrix_parallel(a, elements, ared, nullptr, scratch, s);
 }
 
-void launch_matrix_raw(u128 q, uint64_t elements, void* out, cudaStream_t s) {
+void launch_matrix_raw(u128 q, uint64_t elements, void* out, void* scratch, cudaStream_t s) {
   MatrixArgs a;
   memset(&a, 0, sizeof a);
   a.q_lo = (uint64_t)q;
   a.q_hi = (uint64_t)(q >> 64);
   a.bits = bits_of(q - 1);
   a.width = (a.bits + 7) / 8;
-  int threads = 64;
-  k_matrix_expand<<<(unsigned)((elements + threads - 1) / threads), threads, 0, s>>>(a, elements, nullptr,
-                                                                                     reinterpret_cast<uint4*>(out));
+  matrix_parallel(a, elements, nullptr, reinterpret_cast<uint4*>(out), scratch, s);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -659,11 +768,8 @@ void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, c
   const int per = (elements + splits - 1) / splits;
   if (split_end < 0) split_end = splits;
   if (split_end <= split_begin) return;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_commit_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr{0};
+  smem_limit(k_commit_tc, TC_SMEM, attr);
   dim3 grid(mp.nprimes * 3, COLUMNS / TC_COLS, split_end - split_begin);
   k_commit_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(table, key, reinterpret_cast<const uint4*>(btiles), mp.dconsts, partial,
                                                  sh.rl, elements, per, mp.nprimes, split_begin, status);

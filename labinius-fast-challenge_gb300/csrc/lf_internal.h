@@ -4,6 +4,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -12,6 +13,19 @@
 namespace lf {
 
 typedef unsigned __int128 u128;
+
+// Raises a kernel's dynamic shared-memory limit once per device (idempotent; concurrent first
+// calls from several lanes may both set it, which is harmless).
+template <class K>
+inline void smem_limit(K kernel, int bytes, std::atomic<unsigned long long>& done) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(done.load(std::memory_order_acquire) & bit)) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    done.fetch_or(bit, std::memory_order_release);
+  }
+}
 
 constexpr int RING_N = 648;      // degree of R_Q = Z_Q[X]/(X^648 - X^324 + 1)
 constexpr int LEAVES = 162;      // slots of the transform over Y = X^4
@@ -146,9 +160,11 @@ void launch_touch_pages(uint8_t* host, size_t n, cudaStream_t s);
 
 // ---- launch wrappers (lf_commit.cu) ----
 // The public matrix reduced modulo each prime: ared[prime][m][648].
-void launch_matrix_expand(const ModulusPlan& mp, uint64_t elements, uint32_t* ared, cudaStream_t s);
+// scratch: matrix_scratch_bytes(elements, q) bytes of device memory.
+void launch_matrix_expand(const ModulusPlan& mp, uint64_t elements, uint32_t* ared, void* scratch, cudaStream_t s);
 // The public matrix itself: elements x 648 coefficients in [0, q) as u128 little-endian.
-void launch_matrix_raw(u128 q, uint64_t elements, void* out, cudaStream_t s);
+void launch_matrix_raw(u128 q, uint64_t elements, void* out, void* scratch, cudaStream_t s);
+size_t matrix_scratch_bytes(uint64_t elements, u128 q);
 // Leaf-form key: key[prime][m][162][16] u16.
 void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32_t* ared, uint32_t* leafvals,
                           uint32_t* key, cudaStream_t s);

@@ -473,11 +473,8 @@ int fold_splits(uint64_t ring_elements, int sms) {
 
 void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Challenge* ch, uint8_t* strips,
                  int32_t* part, int splits, int32_t* out, int* status, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_fold_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, FT_SMEM);
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr{0};
+  smem_limit(k_fold_tc, FT_SMEM, attr);
   k_fold_cores<<<COLUMNS, 128, 0, s>>>(ch, strips);
   const unsigned blocks = (unsigned)((4 * ring_elements + 127) / 128);
   const int per = (COLUMNS + splits - 1) / splits;

@@ -470,11 +470,8 @@ void launch_ring_mul(const RingPlan& rp, const RingPrimeDev* rps_dev, const void
                      int* status, cudaStream_t s) {
   const int k = (int)rp.primes.size();
   const size_t smem = ring_mul_smem(k);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_ring_mul, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ring_mul_smem(MAX_RING_PRIMES));
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr{0};
+  smem_limit(k_ring_mul, (int)ring_mul_smem(MAX_RING_PRIMES), attr);
   for (size_t done = 0; done < n;) {  // grids of at most 2^31 - 1 products
     const size_t m = std::min(n - done, (size_t)0x7fffffff);
     k_ring_mul<<<(unsigned)m, 32 * k, smem, s>>>(rp.args, rps_dev, reinterpret_cast<const uint4*>(a) + done * RING_N,

@@ -403,11 +403,8 @@ void launch_rblock_level(const b128* in, uint64_t nout, b128 rho, b128* out, cud
 void launch_switch_round_blocks(const b128* R, uint64_t X, b128 rho, const f162* phi, const f162* w,
                                 unsigned long long* msg, int sms, cudaStream_t s) {
   const int smem = 16 * 256 * 24;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_switch_round_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr{0};
+  smem_limit(k_switch_round_blocks, smem, attr);
   unsigned g = (unsigned)(X < (uint64_t)sms ? X : (uint64_t)sms);
   k_switch_round_blocks<<<g, 128, smem, s>>>(R, X, rho, phi, w, msg);
 }
@@ -417,11 +414,8 @@ void launch_w_update(const f162* w, uint64_t X, f162 rp, f162* wn, cudaStream_t 
 }
 void launch_phi_apply(const b128* e, uint64_t n, const f162* phi, Soa a, cudaStream_t s) {
   const int smem = 16 * 256 * 24;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_phi_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr{0};
+  smem_limit(k_phi_apply, smem, attr);
   k_phi_apply<<<16, 256, smem, s>>>(e, n, phi, a);
 }
 void launch_materialize(const uint4* table, const f162* w, uint64_t X, Soa p, cudaStream_t s) {
@@ -445,11 +439,8 @@ void launch_eq_table_f162(const f162* ps, int n, f162* out, cudaStream_t s) {
 }
 void launch_sblock(const uint4* table, uint64_t nblocks, const b128* elo, uint8_t* sblk, int* status,
                    cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_sblock_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SBT_SMEM);
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr{0};
+  smem_limit(k_sblock_tc, SBT_SMEM, attr);
   k_sblock_tc<<<(unsigned)((nblocks + 1) / 2), SBT_THREADS, SBT_SMEM, s>>>(
       table, nblocks, reinterpret_cast<const uint4*>(elo), sblk, status);
 }
