@@ -246,6 +246,10 @@ struct lf_ctx {
   // batches: a second table buffer and a copy stream, so the next table uploads during a proof
   DevBuf table2, fold_strips, fold_part;
   DevBuf kb_ared, kb_leaf, kb_matrix;  // key-build scratch (matrix residues, leaf values, XOF blocks)
+  // switch rounds: msg (device) accumulates a round's message, msg_out (page-locked, mapped) receives
+  // it from the last block of the round's kernel
+  unsigned long long* msg_out = nullptr;
+  unsigned long long* msg_out_dev = nullptr;
   int nlanes = 4;                // proofs in flight at once: this context and nlanes - 1 lanes
   std::vector<lf_ctx*> lanes;    // contexts on the same device (own stream, buffers, keys)
   std::mutex lanemu;             // guards lanes (created on first use, only added to)
@@ -618,7 +622,6 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   CK(ctx->batch.ensure(2 * 128 * 24));
   CK(ctx->psi.ensure(16 * 256 * 24));
   CK(ctx->soa.ensure(6 * nsmall * 8));
-  CK(ctx->msg.ensure(6 * 8));
   CK(ctx->wbuf.ensure(2 * xmax * 24 + 48));
   CK(ctx->rbuf.ensure((xmax > 2 ? xmax : 2) * 128 * 16));
   f162* G[2] = {ctx->batch.as<f162>(), ctx->batch.as<f162>() + 128};
@@ -645,12 +648,11 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   for (int r = 0; r < HB; ++r) {
     const uint64_t X = 1ull << r;
     launch_psi_tables(G[cur], ctx->psi.as<f162>(), st);
-    CK(cudaMemsetAsync(ctx->msg.p, 0, 48, st));
     launch_switch_round_blocks(R[HB - 1 - r], X, hi[r], ctx->psi.as<f162>(), W[cur],
-                               ctx->msg.as<unsigned long long>(), ctx->sms, st);
+                               ctx->msg.as<unsigned long long>(), ctx->msg_out_dev, ctx->sms, st);
     f162 m[2];
-    CK(cudaMemcpyAsync(m, ctx->msg.p, 48, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    memcpy(m, ctx->msg_out, 48);
     t.absorb_f162(m, 2);
     f162 rr = t.sample_f162("switch-round", 1)[0];
     rounds.push_back(m[0]);
@@ -673,11 +675,10 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   uint64_t half = nsmall;
   for (int r = HB; r < sh.lp; ++r) {
     half >>= 1;
-    CK(cudaMemsetAsync(ctx->msg.p, 0, 48, st));
-    launch_switch_msg(A, P, half, ctx->msg.as<unsigned long long>(), ctx->sms, st);
+    launch_switch_msg(A, P, half, ctx->msg.as<unsigned long long>(), ctx->msg_out_dev, ctx->sms, st);
     f162 m[2];
-    CK(cudaMemcpyAsync(m, ctx->msg.p, 48, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    memcpy(m, ctx->msg_out, 48);
     t.absorb_f162(m, 2);
     f162 rr = t.sample_f162("switch-round", 1)[0];
     rounds.push_back(m[0]);
@@ -1316,7 +1317,10 @@ int lf_ctx_create(const lf_config* cfg, lf_ctx** out) {
     h.init_derive(c, (uint32_t)strlen(c));
     memcpy(ctx->sign_key, h.key, 32);
   }
-  if (ctx->phase.ensure(PHASE_TABLE_BYTES) != cudaSuccess || upload_phase_tables(ctx->phase.p) != cudaSuccess) {
+  if (ctx->phase.ensure(PHASE_TABLE_BYTES) != cudaSuccess || upload_phase_tables(ctx->phase.p) != cudaSuccess ||
+      ctx->msg.ensure(64) != cudaSuccess || cudaMemset(ctx->msg.p, 0, 64) != cudaSuccess ||
+      cudaHostAlloc(reinterpret_cast<void**>(&ctx->msg_out), 64, cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->msg_out_dev), ctx->msg_out, 0) != cudaSuccess) {
     lf_ctx_destroy(ctx);
     return LF_E_CUDA;
   }
@@ -1351,6 +1355,7 @@ void lf_ctx_destroy(lf_ctx* ctx) {
   ctx->keys.clear();
   for (DevBuf* b : bufs) b->release();
   ctx->table2.release();
+  if (ctx->msg_out) cudaFreeHost(ctx->msg_out);
   ctx->kb_ared.release();
   ctx->kb_leaf.release();
   ctx->kb_matrix.release();

@@ -127,13 +127,17 @@ void launch_sblock(const uint4* table, uint64_t nblocks, const b128* elo, uint8_
 void launch_partials_combine(const b128* ehi, const uint8_t* sblk, int nblocks, unsigned long long* v, cudaStream_t s);
 void launch_psi_tables(const f162* batch, f162* tab, cudaStream_t s);
 void launch_rblock_level(const b128* in, uint64_t nout, b128 rho, b128* out, cudaStream_t s);
+// The round-message kernels: msg = 7 device words (6 accumulators + a block count, zero between
+// rounds; the last block clears them), out = 6 words the message is forwarded to (mapped host
+// memory).
 void launch_switch_round_blocks(const b128* R, uint64_t X, b128 rho, const f162* phi, const f162* w,
-                                unsigned long long* msg, int sms, cudaStream_t s);
+                                unsigned long long* msg, unsigned long long* out, int sms, cudaStream_t s);
 void launch_g_update(const f162* G, b128 rho, f162 rp, f162* Gn, cudaStream_t s);
 void launch_w_update(const f162* w, uint64_t X, f162 rp, f162* wn, cudaStream_t s);
 void launch_phi_apply(const b128* e, uint64_t n, const f162* phi, Soa a, cudaStream_t s);
 void launch_materialize(const uint4* table, const f162* w, uint64_t X, Soa p, cudaStream_t s);
-void launch_switch_msg(Soa a, Soa p, uint64_t half, unsigned long long* msg, int sms, cudaStream_t s);
+void launch_switch_msg(Soa a, Soa p, uint64_t half, unsigned long long* msg, unsigned long long* out, int sms,
+                       cudaStream_t s);
 void launch_switch_fold(Soa a, Soa p, uint64_t half, f162 r, int sms, cudaStream_t s);
 
 // ---- launch wrappers (lf_open.cu) ----

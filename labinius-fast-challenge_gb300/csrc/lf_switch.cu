@@ -212,8 +212,26 @@ __device__ __forceinline__ f162 shfl_xor_f162(f162 v, int m) {
   return v;
 }
 
+// A round message's blocks XOR their shares into msg[0..5] (device) and count themselves in
+// msg[6]; the last block to arrive forwards the message to `out` (host memory the device writes
+// through) and clears msg for the next round, so a round needs no separate clear or copy. Called
+// by every thread of the block after its shares were added; no block waits for another.
+__device__ __forceinline__ void msg_forward(unsigned long long* msg, unsigned long long* out) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(msg + 6, 1ull) == (unsigned long long)gridDim.x - 1;
+  __syncthreads();
+  if (last && threadIdx.x < 6) {
+    __threadfence();
+    out[threadIdx.x] = atomicExch(msg + threadIdx.x, 0ull);
+  }
+  if (last && threadIdx.x == 0) msg[6] = 0;
+}
+
 // msg = [sum_{j<half} a_j p_j, sum (a_j + a_{j+half})(p_j + p_{j+half})] (sumcheck.rs:128-189)
-__global__ void __launch_bounds__(256) k_switch_msg(Soa a, Soa p, uint64_t half, unsigned long long* __restrict__ msg) {
+__global__ void __launch_bounds__(256) k_switch_msg(Soa a, Soa p, uint64_t half, unsigned long long* __restrict__ msg,
+                                                    unsigned long long* __restrict__ out) {
   f162 e0 = {0, 0, 0}, ei = {0, 0, 0};
   for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < half; j += (uint64_t)gridDim.x * blockDim.x) {
     f162 a0 = a.get(j), a1 = a.get(j + half), p0 = p.get(j), p1 = p.get(j + half);
@@ -233,6 +251,7 @@ __global__ void __launch_bounds__(256) k_switch_msg(Soa a, Soa p, uint64_t half,
     atomicXor(o + 1, (unsigned long long)s.w1);
     atomicXor(o + 2, (unsigned long long)s.w2);
   }
+  msg_forward(msg, out);
 }
 
 // x[j] <- x[j] + r (x[j] + x[j + half]) for j < half, both polynomials (sumcheck.rs:191-245)
@@ -298,7 +317,8 @@ __device__ __forceinline__ f162 phi_apply(const f162* tab, b128 e) {
 // One round's message from R (2X entries of 128 columns). Block of 128 threads: thread = column.
 __global__ void __launch_bounds__(128) k_switch_round_blocks(const b128* __restrict__ R, uint64_t X, b128 rho,
                                                             const f162* __restrict__ phi, const f162* __restrict__ w,
-                                                            unsigned long long* __restrict__ msg) {
+                                                            unsigned long long* __restrict__ msg,
+                                                            unsigned long long* __restrict__ out) {
   extern __shared__ __align__(16) uint64_t sm64[];
   f162* tab = reinterpret_cast<f162*>(sm64);
   for (int i = threadIdx.x; i < 16 * 256; i += blockDim.x) tab[i] = phi[i];
@@ -338,23 +358,26 @@ __global__ void __launch_bounds__(128) k_switch_round_blocks(const b128* __restr
     atomicXor(&msg[4], (unsigned long long)ei.w1);
     atomicXor(&msg[5], (unsigned long long)ei.w2);
   }
+  msg_forward(msg, out);
 }
 
 // G_{r+1}[b] = Phi_r(y1) + r' (Phi_r(y1) + Phi_r(y2)), y1 = (1 + rho) X^b, y2 = rho X^b.
-__global__ void k_g_update(const f162* __restrict__ G, b128 rho, f162 rp, f162* __restrict__ Gn) {
+// Four threads per output b, each over 32 of the 128 input bits, combined by shuffles.
+__global__ void __launch_bounds__(512) k_g_update(const f162* __restrict__ G, b128 rho, f162 rp, f162* __restrict__ Gn) {
   __shared__ f162 g[128];
-  const int b = threadIdx.x;
-  g[b] = G[b];
+  const int b = threadIdx.x >> 2, part = threadIdx.x & 3;
+  if (threadIdx.x < 128) g[threadIdx.x] = G[threadIdx.x];
   __syncthreads();
   b128 xb = {b < 64 ? 1ull << b : 0, b >= 64 ? 1ull << (b - 64) : 0};
   b128 y2 = b128_mul(rho, xb);
   b128 y1 = b128_add(xb, y2);
   f162 p1 = {0, 0, 0}, p2 = {0, 0, 0};
-  for (int k = 0; k < 128; ++k) {
+  for (int k = 32 * part; k < 32 * part + 32; ++k) {
     if (b128_bit(y1, k)) p1 = f162_add(p1, g[k]);
     if (b128_bit(y2, k)) p2 = f162_add(p2, g[k]);
   }
-  Gn[b] = f162_add(p1, f162_mul(rp, f162_add(p1, p2)));
+  for (int m = 1; m < 4; m <<= 1) p1 = shfl_xor_f162(p1, m), p2 = shfl_xor_f162(p2, m);
+  if (part == 0) Gn[b] = f162_add(p1, f162_mul(rp, f162_add(p1, p2)));
 }
 
 // w_{r+1}[2x] = (1 + r') w_r[x], w_{r+1}[2x + 1] = r' w_r[x]
@@ -401,14 +424,14 @@ void launch_rblock_level(const b128* in, uint64_t nout, b128 rho, b128* out, cud
   k_rblock_level<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, nout, rho, out);
 }
 void launch_switch_round_blocks(const b128* R, uint64_t X, b128 rho, const f162* phi, const f162* w,
-                                unsigned long long* msg, int sms, cudaStream_t s) {
+                                unsigned long long* msg, unsigned long long* out, int sms, cudaStream_t s) {
   const int smem = 16 * 256 * 24;
   static std::atomic<unsigned long long> attr{0};
   smem_limit(k_switch_round_blocks, smem, attr);
   unsigned g = (unsigned)(X < (uint64_t)sms ? X : (uint64_t)sms);
-  k_switch_round_blocks<<<g, 128, smem, s>>>(R, X, rho, phi, w, msg);
+  k_switch_round_blocks<<<g, 128, smem, s>>>(R, X, rho, phi, w, msg, out);
 }
-void launch_g_update(const f162* G, b128 rho, f162 rp, f162* Gn, cudaStream_t s) { k_g_update<<<1, 128, 0, s>>>(G, rho, rp, Gn); }
+void launch_g_update(const f162* G, b128 rho, f162 rp, f162* Gn, cudaStream_t s) { k_g_update<<<1, 512, 0, s>>>(G, rho, rp, Gn); }
 void launch_w_update(const f162* w, uint64_t X, f162 rp, f162* wn, cudaStream_t s) {
   k_w_update<<<(unsigned)((X + 127) / 128), 128, 0, s>>>(w, X, rp, wn);
 }
@@ -449,8 +472,9 @@ void launch_partials_combine(const b128* ehi, const uint8_t* sblk, int nblocks, 
   k_partials_combine<<<(nblocks + run - 1) / run, 128, 0, s>>>(ehi, sblk, nblocks, run, v);
 }
 void launch_psi_tables(const f162* batch, f162* tab, cudaStream_t s) { k_psi_tables<<<16, 256, 0, s>>>(batch, tab); }
-void launch_switch_msg(Soa a, Soa p, uint64_t half, unsigned long long* msg, int sms, cudaStream_t s) {
-  k_switch_msg<<<grid_for(half, 256, sms * 8), 256, 0, s>>>(a, p, half, msg);
+void launch_switch_msg(Soa a, Soa p, uint64_t half, unsigned long long* msg, unsigned long long* out, int sms,
+                       cudaStream_t s) {
+  k_switch_msg<<<grid_for(half, 256, sms * 8), 256, 0, s>>>(a, p, half, msg, out);
 }
 void launch_switch_fold(Soa a, Soa p, uint64_t half, f162 r, int sms, cudaStream_t s) {
   k_switch_fold<<<grid_for(half, 256, sms * 8), 256, 0, s>>>(a, p, half, r);
