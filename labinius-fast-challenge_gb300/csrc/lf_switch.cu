@@ -362,22 +362,20 @@ __global__ void __launch_bounds__(128) k_switch_round_blocks(const b128* __restr
 }
 
 // G_{r+1}[b] = Phi_r(y1) + r' (Phi_r(y1) + Phi_r(y2)), y1 = (1 + rho) X^b, y2 = rho X^b.
-// Four threads per output b, each over 32 of the 128 input bits, combined by shuffles.
-__global__ void __launch_bounds__(512) k_g_update(const f162* __restrict__ G, b128 rho, f162 rp, f162* __restrict__ Gn) {
+__global__ void k_g_update(const f162* __restrict__ G, b128 rho, f162 rp, f162* __restrict__ Gn) {
   __shared__ f162 g[128];
-  const int b = threadIdx.x >> 2, part = threadIdx.x & 3;
-  if (threadIdx.x < 128) g[threadIdx.x] = G[threadIdx.x];
+  const int b = threadIdx.x;
+  g[b] = G[b];
   __syncthreads();
   b128 xb = {b < 64 ? 1ull << b : 0, b >= 64 ? 1ull << (b - 64) : 0};
   b128 y2 = b128_mul(rho, xb);
   b128 y1 = b128_add(xb, y2);
   f162 p1 = {0, 0, 0}, p2 = {0, 0, 0};
-  for (int k = 32 * part; k < 32 * part + 32; ++k) {
+  for (int k = 0; k < 128; ++k) {
     if (b128_bit(y1, k)) p1 = f162_add(p1, g[k]);
     if (b128_bit(y2, k)) p2 = f162_add(p2, g[k]);
   }
-  for (int m = 1; m < 4; m <<= 1) p1 = shfl_xor_f162(p1, m), p2 = shfl_xor_f162(p2, m);
-  if (part == 0) Gn[b] = f162_add(p1, f162_mul(rp, f162_add(p1, p2)));
+  Gn[b] = f162_add(p1, f162_mul(rp, f162_add(p1, p2)));
 }
 
 // w_{r+1}[2x] = (1 + r') w_r[x], w_{r+1}[2x + 1] = r' w_r[x]
@@ -431,7 +429,7 @@ void launch_switch_round_blocks(const b128* R, uint64_t X, b128 rho, const f162*
   unsigned g = (unsigned)(X < (uint64_t)sms ? X : (uint64_t)sms);
   k_switch_round_blocks<<<g, 128, smem, s>>>(R, X, rho, phi, w, msg, out);
 }
-void launch_g_update(const f162* G, b128 rho, f162 rp, f162* Gn, cudaStream_t s) { k_g_update<<<1, 512, 0, s>>>(G, rho, rp, Gn); }
+void launch_g_update(const f162* G, b128 rho, f162 rp, f162* Gn, cudaStream_t s) { k_g_update<<<1, 128, 0, s>>>(G, rho, rp, Gn); }
 void launch_w_update(const f162* w, uint64_t X, f162 rp, f162* wn, cudaStream_t s) {
   k_w_update<<<(unsigned)((X + 127) / 128), 128, 0, s>>>(w, X, rp, wn);
 }

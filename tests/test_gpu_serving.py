@@ -122,3 +122,18 @@ def test_admission_against_the_hbm_budget(gpu_lib, oracle):
         with pytest.raises(gpu_lib.LfError) as e:
             small.submit(big)
         assert e.value.code == -9  # LF_E_ADMISSION
+
+
+def test_lane_count_is_checked_and_one_lane_batches_match(gpu_lib, oracle):
+    with pytest.raises(gpu_lib.LfError) as e:
+        gpu_lib.Prover(0, lanes=9)
+    assert e.value.code == gpu_lib.LF_E_ARGS
+    cases = _cases(oracle, [19, 20, 19])
+    with gpu_lib.Prover(0) as many, gpu_lib.Prover(0, lanes=1) as one:
+        want = [many.prove(s, t, lv) for s, lv, t in cases]
+        for p in (many, one):
+            jobs = [p.make_job(s, t, lv) for s, lv, t in cases]
+            res = p.prove_batch(jobs)
+            assert [p.job_proof(j, r) for j, r in zip(jobs, res)] == want
+        assert many.footprint(20) > many.footprint(19) > many.footprint(19, host_table=False) > 0
+        assert many.footprint(18) == 0  # unsupported shape
