@@ -268,13 +268,13 @@ def batched_leg(lfgpu, prover, n=32, seed=20260):
 
     rng = random.Random(seed)
     shapes = [20 + int(9 * rng.random()) for _ in range(n)]
-    hosts, jobs = {}, []
+    hosts, devs, jobs = {}, {}, []
     for i, lv in enumerate(shapes):
         s = seeds(1, 200 + i)[0]
         dev = device_table(prover, s, lv)
         h = torch.empty(dev.numel(), dtype=torch.uint8, pin_memory=True)
         h.copy_(dev)
-        hosts[i] = h
+        hosts[i], devs[i] = h, dev
         jobs.append(prover.make_job(s, h.data_ptr(), lv, nbytes=h.numel()))
     torch.cuda.synchronize()
     prover.prove_batch(jobs)  # pages touched, keys and buffers of the shapes each lane took
@@ -293,6 +293,9 @@ def batched_leg(lfgpu, prover, n=32, seed=20260):
         if bad:
             raise RuntimeError(f"batched proofs failed: {bad}")
     dt = statistics.median(runs)
+    # every proof of the last timed batch through the GPU checker (device tables)
+    accepted = sum(prover.verify_device(seeds(1, 200 + i)[0], prover.job_proof(jobs[i], res[i]), shapes[i],
+                                        devs[i].data_ptr())[0] for i in range(n))
     # the plain path on the same jobs: one lf_prove_batch call per job runs it alone on the
     # context's own stream (host table uploaded, proven, proof downloaded), one after another
     t1 = time.perf_counter()
@@ -304,7 +307,7 @@ def batched_leg(lfgpu, prover, n=32, seed=20260):
     return {"proofs_per_s": round(n / dt, 1), "jobs": n, "total_ms": round(dt * 1e3, 2),
             "runs_ms": [round(x * 1e3, 2) for x in runs],
             "plain_proofs_per_s": round(n / dt_plain, 1), "vs_plain": round(dt_plain / dt, 2),
-            "lanes": prover.lanes or 4, "log_vars": shapes,
+            "lanes": prover.lanes or 4, "log_vars": shapes, "verified": f"{accepted}/{n} accepted by the GPU checker",
             "tables": "page-locked host memory, H2D inside the timed batch"}
 
 
@@ -364,12 +367,12 @@ def serving_leg(lfgpu, prover, requests=100, rate=8.0, seed=20261):
     import torch
 
     rng = random.Random(seed)
-    pool = {}
+    pool, dev_pool = {}, {}
     for lv in range(22, 32):
         dev = device_table(prover, seeds(1, 300 + lv)[0], lv)
         h = torch.empty(dev.numel(), dtype=torch.uint8, pin_memory=True)
         h.copy_(dev)
-        pool[lv] = h
+        pool[lv], dev_pool[lv] = h, dev
     torch.cuda.synchronize()
     arrivals, t = [], 0.0
     for _ in range(requests):
@@ -392,22 +395,27 @@ def serving_leg(lfgpu, prover, requests=100, rate=8.0, seed=20261):
             j = p.make_job(seeds(1, 1000 + i)[0], pool[lv].data_ptr(), lv, nbytes=pool[lv].numel())
             jobs.append(j)
             tickets.append(p.submit(j))
-        lat = []
+        lat, done = [], []
         for t_ in tickets:
             rc, r = p.poll(t_, 120000)
             if rc != 0 or r.status != 0:
                 raise RuntimeError(f"served request failed: {rc} {r.status}")
             lat.append(r.queue_ms + r.run_ms)
+            done.append(r)
         wall = time.perf_counter() - t0
+        # every served proof through the GPU checker (the shape's device table)
+        ok = sum(p.verify_device(seeds(1, 1000 + i)[0], p.job_proof(j, r), shapes[i], dev_pool[shapes[i]].data_ptr())[0]
+                 for i, (j, r) in enumerate(zip(jobs, done)))
         lat.sort()
         pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))]
-        return round(pct(0.50), 3), round(pct(0.99), 3), round(requests / wall, 2), round(wall, 2)
+        return round(pct(0.50), 3), round(pct(0.99), 3), round(requests / wall, 2), round(wall, 2), ok
 
-    p50, p99, pps, wall = run(prover)
+    p50, p99, pps, wall, ok = run(prover)
     with lfgpu.Prover(prover.device, lanes=1) as one:
-        p50_1, p99_1, _, _ = run(one)
+        p50_1, p99_1, _, _, _ = run(one)
     return {"p50_ms": p50, "p99_ms": p99, "proofs_per_s": pps, "requests": requests, "rate_per_s": rate,
             "lanes": prover.lanes or 4, "plain": {"p50_ms": p50_1, "p99_ms": p99_1, "lanes": 1},
+            "verified": f"{ok}/{requests} accepted by the GPU checker",
             "log_vars": "uniform 22..31", "wall_s": wall, "latency": "queue + prove, host tables (H2D included)"}
 
 
