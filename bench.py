@@ -436,6 +436,7 @@ def main():
     ap.add_argument("--lanes", type=int, default=0, help="proofs in flight per context (0 = the library default)")
     ap.add_argument("--no-micro", action="store_true", help="skip the ring / GHASH / a_times_v microbenchmark")
     ap.add_argument("--only-batch", action="store_true", help="run only the batched leg and exit")
+    ap.add_argument("--no-tune", action="store_true", help="keep the heuristic commitment split count")
     ap.add_argument("--only-micro", action="store_true",
                     help="run only a small microbenchmark (baseline ring products, 2^25 GHASH products) and exit")
     args = ap.parse_args()
@@ -468,6 +469,10 @@ def main():
     cap = lfgpu.proof_size(Q, log_vars)
     out = (ctypes.c_uint8 * cap)()
     prover.key_prepare(log_vars)
+    tuned = None
+    if not args.no_tune:  # lf_tune: the commitment's split count measured on this GPU (proofs unchanged)
+        sp, tms, cand = prover.tune(log_vars, tables[0].data_ptr())
+        tuned = {"commit_splits": sp, "commit_ms": round(tms, 3), "candidates": cand}
     nt = len(ss)
     warm = max(3, args.warmup)
     for i in range(warm):
@@ -563,7 +568,7 @@ def main():
                                "Q=661473542593, 1024 columns", "log_vars": log_vars, "seeds": nt,
                    "l2": f"inputs larger than L2 ({nt} tables of {tbytes >> 20} MiB cycled), no flush",
                    "parallelism": f"replicas x{world}",
-                   "timing": "CUDA events on the prover's stream around the timed steps"},
+                   "timing": "CUDA events on the prover's stream around the timed steps", "tuned": tuned},
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms/proof", "h2d_bytes_per_step": tbytes,
                 "d2h_bytes_per_step": cap},
         "process_e2e_ms": proc_ms,

@@ -140,6 +140,19 @@ int lf_prove_batch(lf_ctx* ctx, size_t n, const lf_job* jobs, lf_result* results
  * queued or running, LF_E_TICKET for an unknown ticket. lf_ctx_destroy completes the job in
  * progress and reports LF_E_INTERNAL for jobs still queued. No counterpart in the reference. */
 int lf_submit(lf_ctx* ctx, const lf_job* job, uint64_t* ticket);
+/* Tuning: the commitment kernel's element-split count (its grid depth, the analogue of the
+ * reference's commit column-group choice, solution/labinius/crates/pcs/src/simd/commit.rs:98-107)
+ * is measured on this device for the shape, using table_dev (a device table of the shape: the
+ * result does not depend on its content), over the candidates whose last wave is at least 3/4
+ * full; the fastest is kept for this shape and modulus on every lane of the context (the proof
+ * bytes do not depend on it). Without tuning a wave-balance heuristic chooses. */
+typedef struct lf_tune_result {
+  int commit_splits;  /* the count kept */
+  float commit_ms;    /* its measured commitment time */
+  int candidates;     /* counts measured */
+} lf_tune_result;
+int lf_tune(lf_ctx* ctx, const uint8_t q_le[16], uint32_t log_vars, const void* table_dev, lf_tune_result* out);
+
 /* Device bytes one request of this shape and modulus holds while it is proven on this context's
  * GPU (table copy when host_table, key, work buffers, transient key-build buffers): the figure
  * admission compares with the budget. 0 for an unsupported shape or modulus. */

@@ -246,6 +246,13 @@ struct lf_ctx {
   // batches: a second table buffer and a copy stream, so the next table uploads during a proof
   DevBuf table2, fold_strips, fold_part;
   DevBuf kb_ared, kb_leaf, kb_matrix;  // key-build scratch (matrix residues, leaf values, XOF blocks)
+  // element splits of the commitment per (log_vars, primes) chosen by lf_tune; the wave-balance
+  // heuristic otherwise
+  std::map<std::pair<int, int>, int> tuned_splits;
+  int split_for(const Shape& sh, int nprimes) const {
+    auto it = tuned_splits.find({sh.log_vars, nprimes});
+    return it != tuned_splits.end() ? it->second : commit_splits(sh.ring_elements, nprimes, sms);
+  }
   // switch rounds: msg (device) accumulates a round's message, msg_out (page-locked, mapped) receives
   // it from the last block of the round's kernel
   unsigned long long* msg_out = nullptr;
@@ -573,7 +580,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   cudaEventRecord(ctx->ev[2], st);
 
   // ---- commitment (K1 + K2), written after the 112 transcript prefix bytes of the stream ----
-  const int splits = commit_splits(sh.ring_elements, ctx->key->mp.nprimes, ctx->sms);
+  const int splits = ctx->split_for(sh, ctx->key->mp.nprimes);
   const ModulusPlan& mp = ctx->key->mp;
   CK(ctx->partial.ensure((size_t)splits * mp.nprimes * COLUMNS * LEAVES * 4 * 4));
   CK(ctx->stream_buf.ensure(STREAM_PREFIX + commit_bytes + 1024));
@@ -1655,6 +1662,60 @@ int lf_submit(lf_ctx* ctx, const lf_job* job, uint64_t* ticket) {
     for (lf_ctx* l : lanes) ctx->workers.emplace_back(serve_loop, ctx, l);
   }
   ctx->qcv.notify_all();
+  return LF_OK;
+}
+
+int lf_tune(lf_ctx* ctx, const uint8_t q_le[16], uint32_t log_vars, const void* table_dev, lf_tune_result* out) {
+  if (!ctx || !q_le || !table_dev) return fail(ctx, LF_E_ARGS, "null argument");
+  Shape sh;
+  if (!sh.set(log_vars) || sh.lp < 12) return fail(ctx, LF_E_SHAPE, "unsupported LOG_VARS");
+  const u128 q = q_from_le(q_le);
+  if (!accept_modulus(q, sh)) return fail(ctx, LF_E_MODULUS, "invalid commitment modulus");
+  std::vector<lf_ctx*> lanes = lanes_of(ctx);
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaSetDevice(ctx->device);
+  int rc = ensure_key(ctx, q, sh);
+  if (rc) return rc;
+  const ModulusPlan& mp = ctx->key->mp;
+  const uint4* table = static_cast<const uint4*>(table_dev);
+  cudaStream_t st = ctx->stream;
+  const long blocks1 = (long)(COLUMNS / 128) * mp.nprimes * 3;  // blocks per split
+  int best = commit_splits(sh.ring_elements, mp.nprimes, ctx->sms), tried = 0;
+  float best_ms = 1e30f;
+  CK(ctx->status.ensure(16));
+  for (int sp = 1; sp <= 48; ++sp) {
+    if ((uint64_t)sp > sh.ring_elements) break;
+    const long blocks = blocks1 * sp, waves = (blocks + ctx->sms - 1) / ctx->sms;
+    if (blocks < ctx->sms / 2 && sp != 1) continue;
+    if ((double)blocks / (double)(waves * ctx->sms) < 0.75 && sp != best) continue;  // poor last wave
+    CK(ctx->partial.ensure((size_t)sp * mp.nprimes * COLUMNS * LEAVES * 4 * 4));
+    CK(cudaMemsetAsync(ctx->status.p, 0, 16, st));
+    float ms = 0;
+    for (int rep = 0; rep < 2; ++rep) {  // the second run is timed
+      cudaEventRecord(ctx->ev[12], st);
+      launch_commit(mp, sh, table, ctx->key->key.as<uint32_t>(), ctx->key->btiles.as<uint16_t>(),
+                    ctx->partial.as<uint32_t>(), sp, ctx->status.as<int>(), st);
+      cudaEventRecord(ctx->ev[13], st);
+      CKL("tuning the commitment");
+      CK(cudaEventSynchronize(ctx->ev[13]));
+      cudaEventElapsedTime(&ms, ctx->ev[12], ctx->ev[13]);
+    }
+    ++tried;
+    if (ms < best_ms) best_ms = ms, best = sp;
+  }
+  int status = 0;
+  CK(cudaMemcpy(&status, ctx->status.p, 4, cudaMemcpyDeviceToHost));
+  if (status) return fail(ctx, LF_E_INTERNAL, "the commitment kernel failed while tuning");
+  ctx->tuned_splits[{sh.log_vars, mp.nprimes}] = best;
+  for (lf_ctx* l : lanes) {
+    std::lock_guard<std::mutex> gl(l->mu);
+    l->tuned_splits[{sh.log_vars, mp.nprimes}] = best;
+  }
+  if (out) {
+    out->commit_splits = best;
+    out->commit_ms = best_ms;
+    out->candidates = tried;
+  }
   return LF_OK;
 }
 

@@ -30,7 +30,7 @@ EXPORTS = [
     "lf_last_profile", "lf_strerror", "lf_last_error", "lf_last_challenges",
     "lf_sample_challenges", "lf_sample_challenges_noalloc", "lf_prove_batch", "lf_submit", "lf_poll",
     "lf_verify", "lf_verify_device", "lf_request_footprint", "lf_ring_mul", "lf_ghash_mul", "lf_ajtai_matrix_device",
-    "lf_a_times_v",
+    "lf_a_times_v", "lf_tune",
 ]
 
 
@@ -38,6 +38,10 @@ class LfError(RuntimeError):
     def __init__(self, code, msg=""):
         super().__init__(f"{ERRORS.get(code, code)}: {msg}")
         self.code = code
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("commit_splits", ctypes.c_int), ("commit_ms", ctypes.c_float), ("candidates", ctypes.c_int)]
 
 
 class Config(ctypes.Structure):
@@ -107,6 +111,7 @@ def load(path=LIB_PATH):
     lib.lf_poll.argtypes = [p, ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(Result)]
     lib.lf_request_footprint.argtypes = [p, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_int]
     lib.lf_request_footprint.restype = sz
+    lib.lf_tune.argtypes = [p, ctypes.c_char_p, ctypes.c_uint32, p, ctypes.POINTER(TuneResult)]
     lib.lf_ring_mul.argtypes = [p, ctypes.c_char_p, sz, p, p, p]
     lib.lf_ghash_mul.argtypes = [p, sz, p, p, p]
     lib.lf_ajtai_matrix_device.argtypes = [p, ctypes.c_char_p, ctypes.c_uint64, p]
@@ -267,6 +272,12 @@ class Prover:
     def footprint(self, log_vars, q=BASELINE_Q, host_table=True):
         """Device bytes one request holds while proven (what admission compares with the budget)."""
         return self.lib.lf_request_footprint(self.ctx, q_bytes(q), log_vars, 1 if host_table else 0)
+
+    def tune(self, log_vars, table_dev, q=BASELINE_Q):
+        """lf_tune: the commitment's split count measured for this shape; (splits, ms, candidates)."""
+        r = TuneResult()
+        self._check(self.lib.lf_tune(self.ctx, q_bytes(q), log_vars, ctypes.c_void_p(table_dev), ctypes.byref(r)))
+        return r.commit_splits, r.commit_ms, r.candidates
 
     def ring_mul(self, q, n, a_dev, b_dev, c_dev):
         """c = a * b in R_q for n pairs of device elements (648 u128 LE coefficients each)."""

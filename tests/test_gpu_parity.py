@@ -91,3 +91,20 @@ def test_many_device_challenges_match_oracle(prover, oracle, prefix):
     want = oracle.short_challenges("labinius/test/many", prefix, 4096)
     got = prover.sample_challenges("labinius/test/many", prefix, 4096)
     assert got == want
+
+
+def test_tuned_split_count_keeps_the_proof(gpu_lib, oracle):
+    # lf_tune changes only the commitment's grid depth; the proof must stay the oracle's
+    seed = SEEDS[0]
+    log_vars = 21
+    table = oracle.write_table(seed, log_vars)
+    with gpu_lib.Prover(0, lanes=2) as p:
+        dev = p.alloc(len(table))
+        try:
+            p.h2d(dev, table)
+            splits, ms, tried = p.tune(log_vars, dev)
+            assert splits >= 1 and ms > 0 and tried >= 1
+            got = p.prove(seed, table, log_vars)
+        finally:
+            p.free(dev)
+    assert got == oracle.prove(seed, table, log_vars)
