@@ -5,6 +5,7 @@
 #include "lf_blake3.cuh"
 #include "lf_internal.h"
 #include "lf_tc.cuh"
+#include "lf_window.cuh"
 
 namespace lf {
 
@@ -19,30 +20,41 @@ __device__ __forceinline__ f162 shfl_xor_f162(f162 v, int m) {
   return v;
 }
 
+// One block per run of RW_SHARE rows i, all columns (RW_COLS per thread): the window table of
+// eq[i] serves the 1024 products of row i; each thread reads its columns' words in order of i.
+// row (1024 F162) is zeroed by the caller and receives the blocks' shares by XOR.
+constexpr int RW_COLS = COLUMNS / 256;
+constexpr uint64_t RW_SHARE = 32;
 __global__ void __launch_bounds__(256) k_row_eval(const uint4* __restrict__ table, int rl, const f162* __restrict__ eqt,
                                                   f162* __restrict__ row) {
-  const int col = blockIdx.x;
+  __shared__ WinTable T;
   const uint64_t n = 1ull << rl;
-  const uint4* w = table + ((uint64_t)col << rl);
-  f162 acc = {0, 0, 0};
-  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
-    uint4 x = w[i];
-    b128 b = {(uint64_t)x.x | ((uint64_t)x.y << 32), (uint64_t)x.z | ((uint64_t)x.w << 32)};
-    acc = f162_add(acc, f162_mul_lifted(eqt[i], b));
+  const uint64_t i0 = blockIdx.x * RW_SHARE, i1 = min(n, i0 + RW_SHARE);
+  f162 acc[RW_COLS];
+#pragma unroll
+  for (int k = 0; k < RW_COLS; ++k) acc[k] = {0, 0, 0};
+  for (uint64_t i = i0; i < i1; ++i) {
+    uint4 v[RW_COLS];
+#pragma unroll
+    for (int k = 0; k < RW_COLS; ++k) v[k] = table[((uint64_t)(threadIdx.x + 256 * k) << rl) + i];
+    win_build(T, eqt[i], threadIdx.x, 256);
+#pragma unroll
+    for (int k = 0; k < RW_COLS; ++k) win_mul_add(T, v[k], acc[k]);
+    __syncthreads();
   }
-  for (int m = 16; m; m >>= 1) acc = shfl_xor_f162(acc, m);
-  __shared__ f162 part[8];
-  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    f162 s = {0, 0, 0};
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s = f162_add(s, part[i]);
-    row[col] = s;
+#pragma unroll
+  for (int k = 0; k < RW_COLS; ++k) {
+    unsigned long long* o = reinterpret_cast<unsigned long long*>(row + threadIdx.x + 256 * k);
+    atomicXor(o, (unsigned long long)acc[k].w0);
+    atomicXor(o + 1, (unsigned long long)acc[k].w1);
+    atomicXor(o + 2, (unsigned long long)acc[k].w2);
   }
 }
 
 void launch_row_eval(const uint4* table, int rl, const f162* eqt, f162* row, cudaStream_t s) {
-  k_row_eval<<<COLUMNS, 256, 0, s>>>(table, rl, eqt, row);
+  const uint64_t n = 1ull << rl;
+  cudaMemsetAsync(row, 0, COLUMNS * sizeof(f162), s);
+  k_row_eval<<<(unsigned)((n + RW_SHARE - 1) / RW_SHARE), 256, 0, s>>>(table, rl, eqt, row);
 }
 
 // ---------------------------------------------------------------------------------------------

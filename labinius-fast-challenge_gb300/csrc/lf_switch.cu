@@ -14,6 +14,7 @@
 
 #include "lf_internal.h"
 #include "lf_tc.cuh"
+#include "lf_window.cuh"
 
 namespace lf {
 
@@ -399,19 +400,33 @@ __global__ void __launch_bounds__(256) k_phi_apply(const b128* __restrict__ e, u
 }
 
 // p[j] = sum_x w[x] lift(pi0[x 2^12 + j]) for j < 4096: block (j tile of 256, x share).
+// p[j] += sum over the block's x of w[x] * lift(table[4096 x + j]): one window table per x (w[x] is
+// the block's common multiplier), MW_J entries j per thread.
+constexpr int MW_J = 2;
 __global__ void __launch_bounds__(256) k_materialize(const uint4* __restrict__ table, const f162* __restrict__ w,
                                                      uint64_t X, uint64_t x_share, Soa p) {
-  const uint64_t j = blockIdx.x * 256ull + threadIdx.x;
+  __shared__ WinTable T;
+  const uint64_t j0 = blockIdx.x * (256ull * MW_J) + threadIdx.x;
   const uint64_t x0 = blockIdx.y * x_share, x1 = min(X, x0 + x_share);
-  f162 acc = {0, 0, 0};
+  f162 acc[MW_J];
+#pragma unroll
+  for (int k = 0; k < MW_J; ++k) acc[k] = {0, 0, 0};
   for (uint64_t x = x0; x < x1; ++x) {
-    const uint4 v = table[(x << 12) + j];
-    const b128 b = {(uint64_t)v.x | ((uint64_t)v.y << 32), (uint64_t)v.z | ((uint64_t)v.w << 32)};
-    acc = f162_add(acc, f162_mul_lifted(w[x], b));
+    uint4 v[MW_J];
+#pragma unroll
+    for (int k = 0; k < MW_J; ++k) v[k] = table[(x << 12) + j0 + 256 * k];
+    win_build(T, w[x], threadIdx.x, 256);
+#pragma unroll
+    for (int k = 0; k < MW_J; ++k) win_mul_add(T, v[k], acc[k]);
+    __syncthreads();  // the next x rebuilds the table
   }
-  atomicXor(reinterpret_cast<unsigned long long*>(p.w0 + j), (unsigned long long)acc.w0);
-  atomicXor(reinterpret_cast<unsigned long long*>(p.w1 + j), (unsigned long long)acc.w1);
-  atomicXor(reinterpret_cast<unsigned long long*>(p.w2 + j), (unsigned long long)acc.w2);
+#pragma unroll
+  for (int k = 0; k < MW_J; ++k) {
+    const uint64_t j = j0 + 256 * k;
+    atomicXor(reinterpret_cast<unsigned long long*>(p.w0 + j), (unsigned long long)acc[k].w0);
+    atomicXor(reinterpret_cast<unsigned long long*>(p.w1 + j), (unsigned long long)acc[k].w1);
+    atomicXor(reinterpret_cast<unsigned long long*>(p.w2 + j), (unsigned long long)acc[k].w2);
+  }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -442,7 +457,7 @@ void launch_phi_apply(const b128* e, uint64_t n, const f162* phi, Soa a, cudaStr
 void launch_materialize(const uint4* table, const f162* w, uint64_t X, Soa p, cudaStream_t s) {
   uint64_t shares = X >= 64 ? 64 : X;
   uint64_t x_share = (X + shares - 1) / shares;
-  k_materialize<<<dim3(16, (unsigned)shares), 256, 0, s>>>(table, w, X, x_share, p);
+  k_materialize<<<dim3(4096 / (256 * MW_J), (unsigned)shares), 256, 0, s>>>(table, w, X, x_share, p);
 }
 static unsigned grid_for(uint64_t n, int threads, unsigned cap) {
   uint64_t g = (n + threads - 1) / threads;
