@@ -67,6 +67,13 @@ LF_HD b128 b128_reduce(uint64_t p0, uint64_t p1, uint64_t p2, uint64_t p3) {
   return {p0 ^ l0, p1 ^ l1};
 }
 
+// a X^b for b < 128, reduced (a shift, then the GHASH reduction).
+LF_HD b128 b128_shl(b128 a, int b) {
+  const int r = b & 63;
+  const uint64_t s0 = a.lo << r, s1 = (a.hi << r) | (r ? a.lo >> (64 - r) : 0), s2 = r ? a.hi >> (64 - r) : 0;
+  return b < 64 ? b128_reduce(s0, s1, s2, 0) : b128_reduce(0, s0, s1, s2);
+}
+
 LF_HD b128 b128_mul(b128 a, b128 b) {
   uint64_t l0, h0, l1, h1, lm, hm;
   clmul64(a.lo, b.lo, l0, h0);

@@ -29,6 +29,16 @@ int main() {
     if (memcmp(ob, &c, 16)) {
       if (fails++ < 5) printf("b128 mismatch %d\n", i);
     }
+    // shifts by X^k (the window-table bases) against the product with the monomial
+    {
+      const int k = (int)(r64() % 128);
+      const b128 xk = {k < 64 ? 1ull << k : 0, k >= 64 ? 1ull << (k - 64) : 0};
+      const b128 s = b128_shl(a, k), m = b128_mul(a, xk);
+      ++cases;
+      if (s.lo != m.lo || s.hi != m.hi) {
+        if (fails++ < 5) printf("b128 shift mismatch %d k=%d\n", i, k);
+      }
+    }
     f162 x = {r64(), r64(), r64() & F162_TOP_MASK}, y = {r64(), r64(), r64() & F162_TOP_MASK};
     if (i % 97 == 0) x.w2 = F162_TOP_MASK, y.w2 = F162_TOP_MASK;
     f162 z = f162_mul(x, y);
