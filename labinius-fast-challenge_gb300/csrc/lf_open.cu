@@ -274,8 +274,9 @@ constexpr int FT_TILE = 128 * 128 * 2;          // A tile: 128 words x 128 bits,
 constexpr int FT_STAGES = 3;                    // A tiles (read by the MMAs)
 constexpr int FT_RING = 8;                      // strips and raw words, loaded FT_AHEAD columns early
 constexpr int FT_AHEAD = 3;
-constexpr int FT_THREADS = 512;                  // four threads per table word (a quarter each)
-constexpr int FT_SMEM = FT_RING * FT_STRIP + FT_STAGES * FT_TILE + FT_RING * FT_THREADS * 16 + 64;
+constexpr int FT_PRODUCERS = 512;                // four per table word (a quarter each): warps 1-16
+constexpr int FT_THREADS = FT_PRODUCERS + 32;   // warp 0 issues the MMAs
+constexpr int FT_SMEM = FT_RING * FT_STRIP + FT_STAGES * FT_TILE + FT_RING * FT_PRODUCERS * 16 + 128;
 constexpr long long FT_WAIT_CYCLES = 2000000000LL;
 
 // Strip of column j: core e holds element (r, i) = C_j[303 - (8 e + r + i)] / 2 as bf16.
@@ -305,8 +306,8 @@ __global__ void __launch_bounds__(128) k_fold_cores(const Challenge* __restrict_
 __device__ __forceinline__ void fold_write_row(uint8_t* tile, int r, uint4 v, int part) {
   const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-  for (int qq = 0; qq < 16 * 128 / FT_THREADS; ++qq) {
-    const int q = 16 * 128 / FT_THREADS * part + qq;  // this thread's share of the word's 16 chunks
+  for (int qq = 0; qq < 16 * 128 / FT_PRODUCERS; ++qq) {
+    const int q = 16 * 128 / FT_PRODUCERS * part + qq;  // this thread's share of the word's 16 chunks
     const uint32_t x = xs[q >> 2];
     uint32_t u[4];
 #pragma unroll
@@ -328,20 +329,26 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   extern __shared__ __align__(1024) uint8_t fsm[];
   uint8_t* sS = fsm;                                   // [FT_RING][FT_STRIP] (first: reads past a strip stay in smem)
   uint8_t* sA = fsm + FT_RING * FT_STRIP;              // [FT_STAGES][FT_TILE]
-  uint4* sW = reinterpret_cast<uint4*>(sA + FT_STAGES * FT_TILE);  // [FT_RING][FT_THREADS] raw words
-  uint64_t* done = reinterpret_cast<uint64_t*>(sW + FT_RING * FT_THREADS);  // [FT_STAGES]
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + FT_STAGES);
+  uint4* sW = reinterpret_cast<uint4*>(sA + FT_STAGES * FT_TILE);  // [FT_RING][FT_PRODUCERS] raw words
+  uint64_t* done = reinterpret_cast<uint64_t*>(sW + FT_RING * FT_PRODUCERS);  // [FT_STAGES] MMAs of a stage done
+  uint64_t* full = done + FT_STAGES;                                            // [FT_STAGES] a stage written
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(full + FT_STAGES);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int row = tid & 127, half = tid >> 7;       // the word (A row) and which quarter of it
+  const bool producer = warp >= 1;
+  const int ptid = tid - 32;                          // producer index
+  const int row = ptid & 127, quarter = ptid >> 7;    // the word (A row) and which quarter of it
   const uint64_t words = 4 * ring_elements;
   const uint64_t w0 = (uint64_t)blockIdx.x * 128;  // first word (row) of the block
   const int split = blockIdx.y;
   const int c_begin = split * cols_per_split, c_end = min(COLUMNS, c_begin + cols_per_split);
-  const bool live = w0 + row < words;
+  const bool live = producer && w0 + row < words;
   if (tid == 0) {
     *abort_flag = 0;
-    for (int i = 0; i < FT_STAGES; ++i) tc::mbar_init(&done[i], 1);
+    for (int i = 0; i < FT_STAGES; ++i) {
+      tc::mbar_init(&done[i], 1);
+      tc::mbar_init(&full[i], FT_PRODUCERS);
+    }
     tc::mbar_init_fence();
   }
   if (warp == 0) tc::tmem_alloc(tslot, 512);
@@ -352,40 +359,54 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   const uint32_t id160 = tc::idesc_bf16_f32(128, 160) | (1u << 16);  // B MN-major
   const uint32_t id144 = tc::idesc_bf16_f32(128, 144) | (1u << 16);
 
-  // Column c's strip and this thread's word go to ring slot c % FT_RING, one commit group per
-  // column (empty past the run), FT_AHEAD columns before they are used.
-  if (!live) sW[tid] = make_uint4(0, 0, 0, 0);  // never copied: zero rows (only slot 0 is read then)
-  auto fetch = [&](int c) {
-    if (c < c_end) {
-      const int slot = (c - c_begin) % FT_RING;
-      const uint4* src = strips + (size_t)c * (FT_STRIP / 16);
-      for (int i = tid; i < FT_STRIP / 16; i += FT_THREADS) tc::cp_async16(sS + slot * FT_STRIP + 16 * i, src + i);
-      if (live) tc::cp_async16(sW + slot * FT_THREADS + tid, table + ((uint64_t)c << rl) + w0 + row);
-    }
-    tc::cp_async_commit();
-  };
-  for (int a = 0; a < FT_AHEAD; ++a) fetch(c_begin + a);
+  // Producers (warps 1-16) and the issuer (lane 0 of warp 0) meet only at the stage barriers: a
+  // producer waits for done[s] (the MMAs that read stage s three columns ago), fills it and arrives
+  // on full[s]; the issuer waits for full[s] and issues the column's MMAs, committing to done[s].
+  // So the expansion runs up to FT_STAGES columns ahead of the tensor core. Every wait is bounded
+  // and gives up at once after an abort; producers keep arriving so no phase is skipped.
   int last = -1;
-  for (int c = c_begin; c < c_end; ++c) {
-    const int it = c - c_begin, s = it % FT_STAGES, slot = it % FT_RING;
-    // A stage s was read by the MMAs of column it - FT_STAGES; the strip slot that fetch() is
-    // about to fill was read by those of it + FT_AHEAD - FT_RING, which are older.
-    if (it >= FT_STAGES) {
-      const bool r = tc::mbar_wait(&done[s], ((it / FT_STAGES) - 1) & 1, abort_flag, FT_WAIT_CYCLES);
-      if (!__all_sync(0xffffffffu, r)) {
+  if (producer) {
+    // Column c's strip and this thread's word go to ring slot c % FT_RING, one commit group per
+    // column (empty past the run), FT_AHEAD columns before they are used.
+    auto fetch = [&](int c) {
+      if (c < c_end) {
+        const int slot = (c - c_begin) % FT_RING;
+        const uint4* src = strips + (size_t)c * (FT_STRIP / 16);
+        for (int i = ptid; i < FT_STRIP / 16; i += FT_PRODUCERS) tc::cp_async16(sS + slot * FT_STRIP + 16 * i, src + i);
+        if (live) tc::cp_async16(sW + slot * FT_PRODUCERS + ptid, table + ((uint64_t)c << rl) + w0 + row);
+      }
+      tc::cp_async_commit();
+    };
+    for (int a = 0; a < FT_AHEAD; ++a) fetch(c_begin + a);
+    for (int c = c_begin; c < c_end; ++c) {
+      const int it = c - c_begin, s = it % FT_STAGES, slot = it % FT_RING;
+      // A stage s was read by the MMAs of column it - FT_STAGES; the strip slot that fetch() is
+      // about to fill was read by those of it + FT_AHEAD - FT_RING, which are older.
+      if (it >= FT_STAGES) {
+        const bool r = tc::mbar_wait(&done[s], ((it / FT_STAGES) - 1) & 1, abort_flag, FT_WAIT_CYCLES);
+        if (!__all_sync(0xffffffffu, r) && !*abort_flag) {
+          *abort_flag = 1;
+          atomicExch(status, 5);
+        }
+      }
+      fetch(c + FT_AHEAD);
+      tc::cp_async_wait<FT_AHEAD>();  // column c's group has landed
+      if (!*abort_flag)
+        fold_write_row(sA + s * FT_TILE, row, live ? sW[slot * FT_PRODUCERS + ptid] : make_uint4(0, 0, 0, 0),
+                       quarter);
+      tc::fence_proxy_async();
+      tc::mbar_arrive(&full[s]);
+    }
+    tc::cp_async_wait<0>();
+  } else if (tid == 0) {
+    for (int c = c_begin; c < c_end; ++c) {
+      const int it = c - c_begin, s = it % FT_STAGES, slot = it % FT_RING;
+      if (!tc::mbar_wait(&full[s], (it / FT_STAGES) & 1, abort_flag, FT_WAIT_CYCLES) && !*abort_flag) {
         *abort_flag = 1;
         atomicExch(status, 5);
       }
-    }
-    fetch(c + FT_AHEAD);
-    tc::cp_async_wait<FT_AHEAD>();  // column c's group has landed
-    const bool go = !*abort_flag;
-    if (go) fold_write_row(sA + s * FT_TILE, row, live ? sW[slot * FT_THREADS + tid] : make_uint4(0, 0, 0, 0), half);
-    tc::fence_proxy_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (tid == 0 && go && !*abort_flag) {
+      if (*abort_flag) continue;
+      tc::fence_after_sync();
       const uint32_t a0 = tc::smem_u32(sA + s * FT_TILE), b0 = tc::smem_u32(sS + slot * FT_STRIP);
 #pragma unroll
       for (int kk = 0; kk < 8; ++kk) {
@@ -397,11 +418,10 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
       tc::mma_commit(&done[s]);
       last = it;
     }
-  }
-  tc::cp_async_wait<0>();
-  if (tid == 0 && last >= 0) {  // drain: the last commit covers every MMA
-    const long long t0 = clock64();
-    while (!tc::mbar_try_wait(&done[last % FT_STAGES], (last / FT_STAGES) & 1) && clock64() - t0 < FT_WAIT_CYCLES) {
+    if (last >= 0) {  // drain: the last commit covers every MMA
+      const long long t0 = clock64();
+      while (!tc::mbar_try_wait(&done[last % FT_STAGES], (last / FT_STAGES) & 1) && clock64() - t0 < FT_WAIT_CYCLES) {
+      }
     }
   }
   const int ncols = c_end - c_begin;
