@@ -60,7 +60,8 @@ __global__ void k_eq_table_f162(const f162* __restrict__ ps, int n, f162* __rest
 // the count's parity is bit 2 of the f32 mantissa after adding 2^23. Waits are bounded; a
 // timeout sets *status = 4.
 // ---------------------------------------------------------------------------------------------
-constexpr int SBT_THREADS = 256;
+constexpr int SBT_PRODUCERS = 256;                           // warps 0-7 expand; warp 8 issues
+constexpr int SBT_THREADS = SBT_PRODUCERS + 32;
 constexpr int SBT_TILE = 128 * 128 * 2;                       // 128 entries x 128 bits, bf16
 constexpr int SBT_SMEM = 2 * SBT_TILE + 2 * 2 * SBT_TILE + 64;  // [B0][B1][A0: 2 h][A1: 2 h][barriers]
 constexpr long long SBT_WAIT_CYCLES = 2000000000LL;
@@ -72,17 +73,21 @@ __global__ void __launch_bounds__(SBT_THREADS, 1)
   uint8_t* sB = sbs;                  // stage s at sB + s * SBT_TILE (E_lo rows of the k-tile)
   uint8_t* sA = sbs + 2 * SBT_TILE;   // stage s, block hb at sA + (2 s + hb) * SBT_TILE
   uint64_t* done = reinterpret_cast<uint64_t*>(sbs + 6 * SBT_TILE);  // [2] MMAs of a stage done
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 2);
+  uint64_t* full = done + 2;                                          // [2] a stage written
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(full + 2);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint64_t h0 = 2 * (uint64_t)blockIdx.x;
   const int hb = tid >> 7, j = tid & 127;
-  const bool live = h0 + hb < nblocks;
+  const bool producer = tid < SBT_PRODUCERS;
+  const bool live = producer && h0 + hb < nblocks;
   const uint4* src = table + (h0 + hb) * 4096 + j;  // entry 128 t + j of block h0 + hb
   if (tid == 0) {
     *abort_flag = 0;
     tc::mbar_init(&done[0], 1);
     tc::mbar_init(&done[1], 1);
+    tc::mbar_init(&full[0], SBT_PRODUCERS);
+    tc::mbar_init(&full[1], SBT_PRODUCERS);
     tc::mbar_init_fence();
   }
   if (warp == 0) tc::tmem_alloc(tslot, 256);
@@ -98,33 +103,42 @@ __global__ void __launch_bounds__(SBT_THREADS, 1)
 
   // The k-tile's operands are expanded here from 16-byte words (the block's table entries and the
   // E_lo entries 128 t .. 128 t + 127, which every block shares from L2); the words are loaded two
-  // k-tiles ahead. Threads 0-127 also expand one E_lo row each.
-  uint4 w = live ? src[0] : make_uint4(0, 0, 0, 0);
-  uint4 w1 = live ? src[128] : make_uint4(0, 0, 0, 0);
-  uint4 e = tid < 128 ? elo[tid] : make_uint4(0, 0, 0, 0);
-  uint4 e1 = tid < 128 ? elo[128 + tid] : make_uint4(0, 0, 0, 0);
+  // k-tiles ahead. Threads 0-127 also expand one E_lo row each. The producers (warps 0-7) and the
+  // issuer (lane 0 of warp 8) meet only at the stage barriers: full[s] once a stage is written,
+  // done[s] once its MMAs have read it; every wait is bounded and gives up at once after an abort.
   int last = -1;  // k-tile of the issuer's last commit
-  for (int t = 0; t < 32; ++t) {
-    const int s = t & 1;
-    if (t >= 2 && !wait_all(&done[s], ((t >> 1) - 1) & 1)) {
-      *abort_flag = 1;
-      atomicExch(status, 4);
+  if (producer) {
+    uint4 w = live ? src[0] : make_uint4(0, 0, 0, 0);
+    uint4 w1 = live ? src[128] : make_uint4(0, 0, 0, 0);
+    uint4 e = tid < 128 ? elo[tid] : make_uint4(0, 0, 0, 0);
+    uint4 e1 = tid < 128 ? elo[128 + tid] : make_uint4(0, 0, 0, 0);
+    for (int t = 0; t < 32; ++t) {
+      const int s = t & 1;
+      if (t >= 2 && !wait_all(&done[s], ((t >> 1) - 1) & 1) && !*abort_flag) {
+        *abort_flag = 1;
+        atomicExch(status, 4);
+      }
+      if (!*abort_flag) {
+        tc::write_row(sA + (2 * s + hb) * SBT_TILE, j, w);
+        if (tid < 128) tc::write_row(sB + s * SBT_TILE, tid, e);
+      }
+      w = w1, e = e1;
+      if (t + 2 < 32) {
+        w1 = live ? src[(t + 2) * 128] : make_uint4(0, 0, 0, 0);
+        if (tid < 128) e1 = elo[(t + 2) * 128 + tid];
+      }
+      tc::fence_proxy_async();
+      tc::mbar_arrive(&full[s]);
     }
-    const bool go = !*abort_flag;
-    if (go) {
-      tc::write_row(sA + (2 * s + hb) * SBT_TILE, j, w);
-      if (tid < 128) tc::write_row(sB + s * SBT_TILE, tid, e);
-    }
-    w = w1, e = e1;
-    if (t + 2 < 32) {
-      w1 = live ? src[(t + 2) * 128] : make_uint4(0, 0, 0, 0);
-      if (tid < 128) e1 = elo[(t + 2) * 128 + tid];
-    }
-    tc::fence_proxy_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (tid == 0 && go && !*abort_flag) {
+  } else if (tid == SBT_PRODUCERS) {
+    for (int t = 0; t < 32; ++t) {
+      const int s = t & 1;
+      if (!tc::mbar_wait(&full[s], (t >> 1) & 1, abort_flag, SBT_WAIT_CYCLES) && !*abort_flag) {
+        *abort_flag = 1;
+        atomicExch(status, 4);
+      }
+      if (*abort_flag) continue;
+      tc::fence_after_sync();
       const uint32_t b0 = tc::smem_u32(sB + s * SBT_TILE);
 #pragma unroll
       for (int h2 = 0; h2 < 2; ++h2) {
@@ -137,18 +151,18 @@ __global__ void __launch_bounds__(SBT_THREADS, 1)
       tc::mma_commit(&done[s]);
       last = t;
     }
-  }
-  // Drain: the issuer's last commit covers every MMA it issued (also after an abort).
-  if (tid == 0 && last >= 0) {
-    const long long t0 = clock64();
-    while (!tc::mbar_try_wait(&done[last & 1], (last >> 1) & 1) && clock64() - t0 < SBT_WAIT_CYCLES) {
+    // Drain: the issuer's last commit covers every MMA it issued (also after an abort).
+    if (last >= 0) {
+      const long long t0 = clock64();
+      while (!tc::mbar_try_wait(&done[last & 1], (last >> 1) & 1) && clock64() - t0 < SBT_WAIT_CYCLES) {
+      }
     }
   }
   // The last commit (k-tile 31, stage 1, its 16th) covers every MMA of the block.
   bool ok = !*abort_flag && wait_all(&done[1], 1);
   ok = __syncthreads_and(ok);
   tc::fence_after_sync();
-  if (ok) {
+  if (ok && producer) {  // warps 0-7: TMEM lanes 32 (w % 4) .. + 31 of block h0 + w / 4
     const int h2 = warp >> 2, qd = warp & 3;
     if (h0 + h2 < nblocks) {
       const int m = 32 * qd + lane, c = tc::row_bit(m);
