@@ -48,6 +48,9 @@ typedef struct lf_profile {
   double upload_ms, key_ms, commit_ms, finish_ms, transcript_ms, partials_ms, switch_ms, row_ms, challenges_ms,
       fold_ms, download_ms, total_ms;
   int launches; /* kernels this library launched for the proof (key preparation excluded when cached) */
+  /* switch_ms in three parts: the rounds on the partials' blocks, the materialisation pass, the last
+   * 12 rounds (each round's host Fiat-Shamir step included) */
+  double switch_blocks_ms, switch_materialize_ms, switch_tail_ms;
 } lf_profile;
 
 /* Context lifetime. Replaces the process-wide pool and allocator of the reference prover

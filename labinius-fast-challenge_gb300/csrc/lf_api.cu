@@ -665,12 +665,13 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
     rounds.push_back(m[0]);
     rounds.push_back(m[1]);
     coords.push_back(rr);
-    launch_g_update(G[cur], hi[r], rr, G[cur ^ 1], st);
+    launch_g_update(ctx->psi.as<f162>(), hi[r], rr, G[cur ^ 1], st);
     launch_w_update(W[cur], X, rr, W[cur ^ 1], st);
     cur ^= 1;
     launches += 4;
   }
   CKL("switch rounds on blocks");
+  cudaEventRecord(ctx->ev[14], st);
   uint64_t* sb = ctx->soa.as<uint64_t>();
   Soa A = {sb, sb + nsmall, sb + 2 * nsmall}, P = {sb + 3 * nsmall, sb + 4 * nsmall, sb + 5 * nsmall};
   launch_psi_tables(G[cur], ctx->psi.as<f162>(), st);
@@ -679,6 +680,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   launch_materialize(table, W[cur], xmax, P, st);
   launches += 3;
   CKL("switch materialisation");
+  cudaEventRecord(ctx->ev[15], st);
   uint64_t half = nsmall;
   for (int r = HB; r < sh.lp; ++r) {
     half >>= 1;
@@ -780,6 +782,9 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   ctx->prof.transcript_ms = ev_ms(ctx, 3, 4);
   ctx->prof.partials_ms = ev_ms(ctx, 4, 5);
   ctx->prof.switch_ms = ev_ms(ctx, 5, 6);
+  ctx->prof.switch_blocks_ms = ev_ms(ctx, 5, 14);
+  ctx->prof.switch_materialize_ms = ev_ms(ctx, 14, 15);
+  ctx->prof.switch_tail_ms = ev_ms(ctx, 15, 6);
   ctx->prof.row_ms = ev_ms(ctx, 6, 7);
   ctx->prof.challenges_ms = ev_ms(ctx, 7, 8);
   ctx->prof.fold_ms = ev_ms(ctx, 8, 9);

@@ -330,6 +330,7 @@ __device__ __forceinline__ f162 phi_apply(const f162* tab, b128 e) {
 }
 
 // One round's message from R (2X entries of 128 columns). Block of 128 threads: thread = column.
+constexpr int RB_DEFER = 64;  // x per block whose weighting is deferred to one parallel pass
 __global__ void __launch_bounds__(128) k_switch_round_blocks(const b128* __restrict__ R, uint64_t X, b128 rho,
                                                             const f162* __restrict__ phi, const f162* __restrict__ w,
                                                             unsigned long long* __restrict__ msg,
@@ -339,10 +340,12 @@ __global__ void __launch_bounds__(128) k_switch_round_blocks(const b128* __restr
   for (int i = threadIdx.x; i < 16 * 256; i += blockDim.x) tab[i] = phi[i];
   __syncthreads();
   __shared__ f162 part[2][4];
+  __shared__ f162 sums[2][RB_DEFER];  // the block's column sums per x, weighted after the loop
   const int c = threadIdx.x, lane = c & 31, warp = c >> 5;
   const b128 one_rho = {rho.lo ^ 1, rho.hi};
   f162 e0 = {0, 0, 0}, ei = {0, 0, 0};
-  for (uint64_t x = blockIdx.x; x < X; x += gridDim.x) {
+  int nx = 0;
+  for (uint64_t x = blockIdx.x; x < X; x += gridDim.x, ++nx) {
     const b128 v0 = R[(2 * x) * 128 + c], v1 = R[(2 * x + 1) * 128 + c];
     f162 s0 = f162_shift(phi_apply(tab, b128_mul(one_rho, v0)), c);
     f162 si = f162_shift(phi_apply(tab, b128_add(v0, v1)), c);
@@ -357,13 +360,32 @@ __global__ void __launch_bounds__(128) k_switch_round_blocks(const b128* __restr
     if (lane == 0) part[0][warp] = s0, part[1][warp] = si;
     __syncthreads();
     if (c == 0) {
-      f162 a0 = f162_add(f162_add(part[0][0], part[0][1]), f162_add(part[0][2], part[0][3]));
-      f162 ai = f162_add(f162_add(part[1][0], part[1][1]), f162_add(part[1][2], part[1][3]));
-      const f162 wx = w[x];
-      e0 = f162_add(e0, f162_mul(wx, a0));
-      ei = f162_add(ei, f162_mul(wx, ai));
+      const f162 a0 = f162_add(f162_add(part[0][0], part[0][1]), f162_add(part[0][2], part[0][3]));
+      const f162 ai = f162_add(f162_add(part[1][0], part[1][1]), f162_add(part[1][2], part[1][3]));
+      if (nx < RB_DEFER) {
+        sums[0][nx] = a0, sums[1][nx] = ai;
+      } else {  // more x than the deferral buffer holds (only at very large shapes): weight now
+        const f162 wx = w[x];
+        e0 = f162_add(e0, f162_mul(wx, a0));
+        ei = f162_add(ei, f162_mul(wx, ai));
+      }
     }
     __syncthreads();
+  }
+  // the weights w_x times the deferred sums, one product per thread, then one reduction
+  {
+    f162 d0 = {0, 0, 0}, di = {0, 0, 0};
+    const int nd = min(nx, RB_DEFER);
+    for (int k = c; k < 2 * nd; k += blockDim.x) {
+      const int which = k / nd, i = k % nd;
+      const f162 prod = f162_mul(w[blockIdx.x + (uint64_t)i * gridDim.x], sums[which][i]);
+      if (which == 0) d0 = f162_add(d0, prod); else di = f162_add(di, prod);
+    }
+    for (int m = 16; m; m >>= 1) d0 = shfl_xor_f162(d0, m), di = shfl_xor_f162(di, m);
+    if (lane == 0) part[0][warp] = d0, part[1][warp] = di;
+    __syncthreads();
+    if (c == 0)
+      for (int q = 0; q < 4; ++q) e0 = f162_add(e0, part[0][q]), ei = f162_add(ei, part[1][q]);
   }
   if (c == 0) {
     atomicXor(&msg[0], (unsigned long long)e0.w0);
@@ -377,19 +399,14 @@ __global__ void __launch_bounds__(128) k_switch_round_blocks(const b128* __restr
 }
 
 // G_{r+1}[b] = Phi_r(y1) + r' (Phi_r(y1) + Phi_r(y2)), y1 = (1 + rho) X^b, y2 = rho X^b.
-__global__ void k_g_update(const f162* __restrict__ G, b128 rho, f162 rp, f162* __restrict__ Gn) {
-  __shared__ f162 g[128];
+// Phi_r is applied through the round's byte tables (psi, already built for the round's message),
+// and rho X^b is a shift: no GHASH product and no 128-term loop per output.
+__global__ void k_g_update(const f162* __restrict__ psi, b128 rho, f162 rp, f162* __restrict__ Gn) {
   const int b = threadIdx.x;
-  g[b] = G[b];
-  __syncthreads();
-  b128 xb = {b < 64 ? 1ull << b : 0, b >= 64 ? 1ull << (b - 64) : 0};
-  b128 y2 = b128_mul(rho, xb);
-  b128 y1 = b128_add(xb, y2);
-  f162 p1 = {0, 0, 0}, p2 = {0, 0, 0};
-  for (int k = 0; k < 128; ++k) {
-    if (b128_bit(y1, k)) p1 = f162_add(p1, g[k]);
-    if (b128_bit(y2, k)) p2 = f162_add(p2, g[k]);
-  }
+  const b128 xb = {b < 64 ? 1ull << b : 0, b >= 64 ? 1ull << (b - 64) : 0};
+  const b128 y2 = b128_shl(rho, b);
+  const b128 y1 = b128_add(xb, y2);
+  const f162 p1 = phi_apply(psi, y1), p2 = phi_apply(psi, y2);
   Gn[b] = f162_add(p1, f162_mul(rp, f162_add(p1, p2)));
 }
 
@@ -458,7 +475,9 @@ void launch_switch_round_blocks(const b128* R, uint64_t X, b128 rho, const f162*
   unsigned g = (unsigned)(X < (uint64_t)sms ? X : (uint64_t)sms);
   k_switch_round_blocks<<<g, 128, smem, s>>>(R, X, rho, phi, w, msg, out);
 }
-void launch_g_update(const f162* G, b128 rho, f162 rp, f162* Gn, cudaStream_t s) { k_g_update<<<1, 128, 0, s>>>(G, rho, rp, Gn); }
+void launch_g_update(const f162* psi, b128 rho, f162 rp, f162* Gn, cudaStream_t s) {
+  k_g_update<<<1, 128, 0, s>>>(psi, rho, rp, Gn);
+}
 void launch_w_update(const f162* w, uint64_t X, f162 rp, f162* wn, cudaStream_t s) {
   k_w_update<<<(unsigned)((X + 127) / 128), 128, 0, s>>>(w, X, rp, wn);
 }

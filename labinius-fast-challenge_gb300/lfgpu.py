@@ -62,7 +62,8 @@ class Result(ctypes.Structure):
 class Profile(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in (
         "upload_ms", "key_ms", "commit_ms", "finish_ms", "transcript_ms", "partials_ms", "switch_ms", "row_ms",
-        "challenges_ms", "fold_ms", "download_ms", "total_ms")] + [("launches", ctypes.c_int)]
+        "challenges_ms", "fold_ms", "download_ms", "total_ms")] + [("launches", ctypes.c_int)] + [
+        (n, ctypes.c_double) for n in ("switch_blocks_ms", "switch_materialize_ms", "switch_tail_ms")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
