@@ -30,11 +30,10 @@ constexpr int TC_COLS = 128;                         // table columns per block 
 constexpr int TC_LEAVES = 54;                        // leaves per block (a third of a prime)
 constexpr int TC_N = 64;                             // MMA N: 6 groups of 10 rows (9 leaves + 1 zero), padded
 constexpr int TC_K = 256;                            // MMA K: 128 bits x 2 limbs (A read twice)
-constexpr int TC_THREADS = 32 * 24;                  // 24 warps; lane 0 of the last also issues the MMAs
-constexpr int TC_A_BYTES = TC_COLS * 128 * 2;        // 32 KB per A slot (one table word per column)
+constexpr int TC_THREADS = 32 * 32;                  // 24 epilogue, 4 producer and 4 issuer warps
 constexpr int TC_B_BYTES = TC_N * TC_K * 2;          // 32 KB
 constexpr int TC_KEY_INTS = TC_LEAVES * 16;          // one element's key rows for the block's leaves
-constexpr int TC_SMEM = 4 * TC_A_BYTES + TC_B_BYTES + 4 * TC_KEY_INTS * 4 + 2 * 8 + 16;
+constexpr int TC_SMEM = TC_B_BYTES + 4 * TC_KEY_INTS * 4 + 3 * TC_COLS * 64 + 3 * TC_KEY_INTS * 4 + 16 * 8 + 16;
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;   // ~1 s at 2 GHz
 
 static void fill_btiles(const PrimePlan& pl, const PrimeConst& c, uint16_t* out);
@@ -483,7 +482,7 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
 // mod 4) at leaf s is the evaluation sum_j bit_j zeta_s^j (mod p), zeta_s the leaf's root: a
 // product with the Vandermonde matrix V[s][j] = zeta_s^j. On the tensor core it is exact:
 //   A (M = 128 table columns x 128 bits) holds each set bit as a power of two a_kappa (bf16 with
-//   one exponent bit, see commit_write_row) and is read twice;
+//   one exponent bit, see commit_expand_word) and is read twice;
 //   B (N = 64 x K = 256) holds per leaf (V mod 256) / a against the first reading and
 //   (V >> 8) * 256 / a against the second (both exact in bf16), so the f32 accumulator is
 //   sum_j bit_j V[s][j] < 2^22, an exact integer.
@@ -491,34 +490,47 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
 // does the 4x4 base multiplication with the key on the integer pipe.
 //
 // Block = one prime x one third of its 162 leaves (54) x 128 table columns x an element range.
-// Warps 0-23 do everything but the MMAs, in one loop over elements e:
-//   wait until the MMAs of e are done (their A slots are then free and TMEM buffer e % 2 full);
-//   expand element e + 1 into the four A slots (threads 0-511: column t % 128, word t / 128;
-//   its words were loaded one element earlier) and copy its key rows (threads 512-727) into a
-//   4-element ring; block barrier;
-//   epilogue of e: warp w reads TMEM lanes 32 (w % 4) .. +31 (its 32 columns), columns
-//   256 (e % 2) + 64 k + 10 (w / 4) + i, for leaves 9 (w / 4) + i, and accumulates 9 x 4 values.
-// After the barrier, lane 0 of warp 23 issues the MMAs of e + 1 (64 instructions), so the tensor
-// core works on e + 1 while the CUDA cores finish e. The waits on the tensor core are bounded
-// (about a second); a timeout sets *status = 3 and the block skips its remaining work but keeps
-// the barrier count, so every thread drains.
+// Tensor memory (512 columns) holds four word stages k = 0..3 (the four words of an element):
+// stage k = A (the expanded bits of word k of the current element, columns 128 k .. +63) and D
+// (its 64 leaf sums, columns 128 k + 64 .. +63). Roles, all meeting on per-stage mbarriers:
+//   warps 24-27 (producers; thread t = table column t = TMEM lane t): fetch words and key rows by
+//     cp.async two elements ahead; per element centre the key rows into a 4-element ring
+//     (arrive kfull), then per word k wait until the MMAs of the previous element's word k are
+//     done (done[k]), expand the word into stage k's A columns with tcgen05.st and arrive full[k];
+//   warp 28 + k (stage k's issuer): per element waits full[k] and dfree[k] (the epilogue has read
+//     the previous D of stage k), issues the word's 16 MMAs (A from TMEM, B = the leaf tile in
+//     shared memory) from lane 0 and commits them to done[k]. A thread issues a small MMA only
+//     every 50-70 cycles, so each stage has its own issuer and no issuer does other work;
+//   warps 0-23 (epilogue; warp w reads TMEM lanes 32 (w % 4) .. +31, leaves 9 (w / 4) + i):
+//     per word wait done[k], load the 9 sums, arrive dfree[k], reduce and accumulate 9 x 4 values.
+// So the expansion, the MMAs and the epilogue of different words run at the same time, and no
+// table bits pass through shared memory. Every wait is bounded (about a second); a timeout sets
+// *status = 3 and the abort flag, on which every role leaves its loop; TMEM is released after the
+// issuers' last commits drained.
 // ------------------------------------------------------------------------------------------------
-// Word -> row c of an A slot, K order as tc::write_row (u32 o holds bits o % 16 and o % 16 + 16
-// of word o / 16), but a set bit is the bf16 with the single exponent bit 11 + (o & 3): 2^-111,
-// 2^-95, 2^-63 or 2. One shift of the source serves four outputs through four masks; the B tiles
-// carry the inverse powers of two, so every product is the same integer as before.
-__device__ __forceinline__ void commit_write_row(uint8_t* tile, int c, uint4 v) {
+// One table word -> the 64 TMEM columns of its A row (K positions 2o and 2o + 1 in column o): u32 o
+// holds bits o % 16 and o % 16 + 16 of word o / 16, and a set bit at K position kappa is the bf16
+// with the single exponent bit 11 + (kappa / 2 & 3): 2^-111, 2^-95, 2^-63 or 2. One shift of the
+// source serves four columns through four masks; the B tiles carry the inverse powers of two, so
+// every product is the integer bit * V.
+__device__ __forceinline__ void commit_expand_word(uint32_t tA, uint4 v) {
   const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    const uint32_t x = xs[q >> 2];
-    const int t0 = (q & 3) * 4;
-    const uint32_t y = t0 < 12 ? x << (11 - t0) : x >> 1;
-    *reinterpret_cast<uint4*>(tile + (c >> 3) * 2048 + q * 128 + (c & 7) * 16) =
-        make_uint4(y & 0x08000800u, y & 0x10001000u, y & 0x20002000u, y & 0x40004000u);
+  for (int m = 0; m < 4; ++m) {
+    const uint32_t x = xs[m];
+    uint32_t u[16];
+#pragma unroll
+    for (int qq = 0; qq < 4; ++qq) {
+      const uint32_t y = qq < 3 ? x << (11 - 4 * qq) : x >> 1;
+      u[4 * qq + 0] = y & 0x08000800u;
+      u[4 * qq + 1] = y & 0x10001000u;
+      u[4 * qq + 2] = y & 0x20002000u;
+      u[4 * qq + 3] = y & 0x40004000u;
+    }
+    tc::tmem_st_x16(tA + 16 * m, u);
   }
 }
-// Value of a set bit at K position kappa (0..127) of a commit_write_row row.
+// Value of a set bit at K position kappa (0..127) of an expanded word.
 static double commit_bit_value(int kappa) {
   const int b = (kappa >> 1) & 3;
   return b == 3 ? 2.0 : b == 2 ? ldexp(1.0, -63) : b == 1 ? ldexp(1.0, -95) : ldexp(1.0, -111);
@@ -529,11 +541,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const PrimeConst* __restrict__ pcs, uint32_t* __restrict__ partial, int rl, int elements,
                 int per_split, int nprimes, int split_base, int* status) {
   extern __shared__ __align__(1024) uint8_t tsm[];
-  uint8_t* sA = tsm;
-  uint8_t* sB = tsm + 4 * TC_A_BYTES;
-  int* sKey = reinterpret_cast<int*>(sB + TC_B_BYTES);
-  uint64_t* t_full = reinterpret_cast<uint64_t*>(sKey + 4 * TC_KEY_INTS);  // [2] MMAs of an element done
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(t_full + 2);
+  uint8_t* sB = tsm;
+  int* sKey = reinterpret_cast<int*>(tsm + TC_B_BYTES);                            // [4][TC_KEY_INTS]
+  uint4* wring = reinterpret_cast<uint4*>(sKey + 4 * TC_KEY_INTS);                  // [3][128 columns][4 words]
+  uint4* kraw = wring + 3 * TC_COLS * 4;                                            // [3][TC_KEY_INTS / 4]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(kraw + 3 * (TC_KEY_INTS / 4));
+  uint64_t* full = bars;        // [4] producers wrote stage k's A (128 arrivals)
+  uint64_t* done = bars + 4;    // [4] the MMAs of stage k completed (tensor-core commit)
+  uint64_t* dfree = bars + 8;   // [4] the epilogue loaded stage k's D (24 arrivals)
+  uint64_t* kfull = bars + 12;  // [4] key ring slot ready (128 arrivals)
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 16);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
 
   const int pi = blockIdx.x / 3, third = blockIdx.x % 3;
@@ -542,13 +559,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int m_begin = split * per_split;
   const int nelem = max(0, min(elements, m_begin + per_split) - m_begin);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t p = pcs[pi].p, bar = pcs[pi].bar;
-  const int reduce_every = (int)pcs[pi].reduce_every;
 
   if (tid == 0) {
     *abort_flag = 0;
-    tc::mbar_init(&t_full[0], 1);
-    tc::mbar_init(&t_full[1], 1);
+    for (int k = 0; k < 4; ++k) {
+      tc::mbar_init(&full[k], 4 * 32);
+      tc::mbar_init(&done[k], 1);
+      tc::mbar_init(&dfree[k], 24);
+      tc::mbar_init(&kfull[k], 4 * 32);
+    }
     tc::mbar_init_fence();
   }
   if (warp == 0) tc::tmem_alloc(tslot, 512);
@@ -561,52 +580,97 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
+  const uint32_t p = pcs[pi].p;
+  int last_e = -1;  // an issuer's last commit
 
-  // MMA issue (lane 0 of warp 23): element e into TMEM buffer e % 2, one commit per element.
-  const bool issuer = tid == TC_THREADS - 32;
-  int last = -1;
-  auto issue = [&](int e) {
-    if (!issuer || *abort_flag) return;
+  if (warp >= 28) {
+    // ---------------- issuer of stage k ----------------
+    const int k = warp - 28;
     const uint32_t idesc = tc::idesc_bf16_f32(TC_COLS, TC_N);
-    const uint64_t adesc0 = tc::sdesc(tc::smem_u32(sA), 128, 2048);
     const uint64_t bdesc0 = tc::sdesc(tc::smem_u32(sB), 128, 4096);
-    const uint32_t d0 = tbase + 256 * (e & 1);
+    const uint32_t st = tbase + 128 * k;
+    for (int e = 0; e < nelem; ++e) {
+      int iok = 1;
+      if (lane == 0) {
+        iok = tc::mbar_wait(&full[k], e & 1, abort_flag, TC_WAIT_CYCLES) &&
+              (e == 0 || tc::mbar_wait(&dfree[k], (e - 1) & 1, abort_flag, TC_WAIT_CYCLES));
+        if (iok) {
+          tc::fence_after_sync();
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
-#pragma unroll
-      for (int kk = 0; kk < TC_K / 16; ++kk)
-        tc::mma_bf16(d0 + TC_N * k, adesc0 + (uint64_t)(k * (TC_A_BYTES >> 4) + (kk & 7) * 16),
-                     bdesc0 + (uint64_t)(kk * 16), idesc, kk > 0 ? 1u : 0u);
-    tc::mma_commit(&t_full[e & 1]);
-    last = e;
-  };
-  {
-    // ---------------- expansion + epilogue ----------------
-    const bool expander = tid < 4 * TC_COLS;                      // column tid % 128, word tid / 128
-    const bool keyer = tid >= 4 * TC_COLS && tid < 4 * TC_COLS + TC_KEY_INTS / 4;
-    const uint4* wsrc = table + ((size_t)(col0 + (tid & (TC_COLS - 1))) << rl) + (tid >> 7);
-    const uint4* ksrc = reinterpret_cast<const uint4*>(key) +
-                        ((size_t)pi * elements * LEAVES + TC_LEAVES * third) * 4 + (tid - 4 * TC_COLS);
-    const int half = (int)(p - 1) / 2;
-    auto load_pre = [&](int e) -> uint4 {  // this thread's input for element e
-      const size_t m = (size_t)(m_begin + e);
-      if (expander) return wsrc[4 * m];
-      if (keyer) return ksrc[m * LEAVES * 4];
-      return make_uint4(0, 0, 0, 0);
-    };
-    auto store_pre = [&](int e, uint4 u) {  // ... into the A slots / the key ring
-      if (expander) {
-        commit_write_row(sA + (tid >> 7) * TC_A_BYTES, tid & (TC_COLS - 1), u);
-      } else if (keyer) {
-        int4 v;  // centred into (-p/2, p/2]
-        v.x = (int)u.x > half ? (int)u.x - (int)p : (int)u.x;
-        v.y = (int)u.y > half ? (int)u.y - (int)p : (int)u.y;
-        v.z = (int)u.z > half ? (int)u.z - (int)p : (int)u.z;
-        v.w = (int)u.w > half ? (int)u.w - (int)p : (int)u.w;
-        reinterpret_cast<int4*>(sKey + (e & 3) * TC_KEY_INTS)[tid - 4 * TC_COLS] = v;
+          for (int kk = 0; kk < TC_K / 16; ++kk)
+            tc::mma_bf16_ta(st + 64, st + 8 * (kk & 7), bdesc0 + (uint64_t)(kk * 16), idesc, kk > 0 ? 1u : 0u);
+          tc::mma_commit(&done[k]);
+          last_e = e;
+        } else if (!*abort_flag) {
+          *abort_flag = 1;
+          atomicExch(status, 3);
+        }
       }
+      if (!__shfl_sync(0xffffffffu, iok, 0)) break;
+    }
+  } else if (warp >= 24) {
+    // ---------------- producers ----------------
+    const int t = tid - 24 * 32;  // table column, TMEM lane
+    const uint4* wsrc = table + ((size_t)(col0 + t) << rl);
+    const uint4* ksrc = reinterpret_cast<const uint4*>(key) +
+                        ((size_t)pi * elements * LEAVES + TC_LEAVES * third) * 4;
+    const int half = (int)(p - 1) / 2;
+    const uint32_t tl = tbase + ((uint32_t)(32 * (warp - 24)) << 16);
+    auto fetch = [&](int e) {  // element e's words (this column) and key rows t, t + 128 into ring slot e % 3
+      if (e < nelem) {
+        const size_t m = (size_t)(m_begin + e);
+        uint4* w = wring + ((e % 3) * TC_COLS + t) * 4;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) tc::cp_async16(w + k, wsrc + 4 * m + k);
+        uint4* kr = kraw + (e % 3) * (TC_KEY_INTS / 4);
+        tc::cp_async16(kr + t, ksrc + m * LEAVES * 4 + t);
+        if (t + 128 < TC_KEY_INTS / 4) tc::cp_async16(kr + t + 128, ksrc + m * LEAVES * 4 + t + 128);
+      }
+      tc::cp_async_commit();
     };
-
+    fetch(0);
+    fetch(1);
+    for (int e = 0; e < nelem; ++e) {
+      if (__any_sync(0xffffffffu, *abort_flag)) break;
+      fetch(e + 2);
+      tc::cp_async_wait<2>();
+      {
+        const uint4* kr = kraw + (e % 3) * (TC_KEY_INTS / 4);
+        int4* kd = reinterpret_cast<int4*>(sKey + (e & 3) * TC_KEY_INTS);
+        for (int i = t; i < TC_KEY_INTS / 4; i += 128) {
+          const uint4 u = kr[i];
+          int4 v;  // centred into (-p/2, p/2]
+          v.x = (int)u.x > half ? (int)u.x - (int)p : (int)u.x;
+          v.y = (int)u.y > half ? (int)u.y - (int)p : (int)u.y;
+          v.z = (int)u.z > half ? (int)u.z - (int)p : (int)u.z;
+          v.w = (int)u.w > half ? (int)u.w - (int)p : (int)u.w;
+          kd[i] = v;
+        }
+        tc::mbar_arrive(&kfull[e & 3]);
+      }
+      bool ok = true;
+      for (int k = 0; k < 4 && ok; ++k) {
+        if (e > 0) ok = __all_sync(0xffffffffu, tc::mbar_wait(&done[k], (e - 1) & 1, abort_flag, TC_WAIT_CYCLES));
+        if (!ok) break;
+        tc::fence_after_sync();
+        commit_expand_word(tl + 128 * k, wring[((e % 3) * TC_COLS + t) * 4 + k]);
+        tc::tmem_wait_st();
+        tc::fence_before_sync();
+        tc::mbar_arrive(&full[k]);
+      }
+      if (!ok) {
+        if (lane == 0 && !*abort_flag) {
+          *abort_flag = 1;
+          atomicExch(status, 3);
+        }
+        break;
+      }
+    }
+    tc::cp_async_wait<0>();
+  } else {
+    // ---------------- epilogue ----------------
+    const uint32_t bar = pcs[pi].bar;
+    const int reduce_every = (int)pcs[pi].reduce_every;
     const int g = warp >> 2, qd = warp & 3;
     const int c = 32 * qd + lane;
     const float pf = (float)p, invp = 1.0f / (float)p;
@@ -617,73 +681,52 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     for (int i = 0; i < 9; ++i)
 #pragma unroll
       for (int l = 0; l < 4; ++l) acc[i][l] = 0;
-
-    uint4 pre = make_uint4(0, 0, 0, 0);
-    if (nelem > 0) {
-      store_pre(0, load_pre(0));
-      if (nelem > 1) pre = load_pre(1);
-      tc::fence_proxy_async();
-      tc::fence_before_sync();
-      __syncthreads();
-      tc::fence_after_sync();
-      issue(0);
-    }
+    const uint32_t tb = tbase + ((uint32_t)(32 * qd) << 16) + 64 + 10 * g;
     int since = 0;
-    for (int e = 0; e < nelem; ++e) {
-      bool ok = !*abort_flag;
-      if (ok) {
-        ok = __all_sync(0xffffffffu, tc::mbar_wait(&t_full[e & 1], (e >> 1) & 1, abort_flag, TC_WAIT_CYCLES));
-        if (!ok) {
-          *abort_flag = 1;
-          atomicExch(status, 3);
-        }
-      }
-      ok = __all_sync(0xffffffffu, ok);
-      tc::fence_after_sync();
-      if (e + 1 < nelem) {
-        if (ok) store_pre(e + 1, pre);
-        if (e + 2 < nelem) pre = load_pre(e + 2);
-        tc::fence_proxy_async();
-        tc::fence_before_sync();
-        __syncthreads();
+    bool ok = true;
+    for (int e = 0; e < nelem && ok; ++e) {
+      ok = __all_sync(0xffffffffu, tc::mbar_wait(&kfull[e & 3], (e >> 2) & 1, abort_flag, TC_WAIT_CYCLES));
+      const int4* kp = reinterpret_cast<const int4*>(sKey + (e & 3) * TC_KEY_INTS) + 9 * g * 4;
+      for (int k = 0; k < 4 && ok; ++k) {
+        ok = __all_sync(0xffffffffu, tc::mbar_wait(&done[k], e & 1, abort_flag, TC_WAIT_CYCLES));
+        if (!ok) break;
         tc::fence_after_sync();
-        issue(e + 1);
+        const uint32_t ta = tb + 128 * k;
+        uint32_t v[9];
+        tc::tmem_ld_x2(ta + 0, v[0], v[1]);
+        tc::tmem_ld_x2(ta + 2, v[2], v[3]);
+        tc::tmem_ld_x2(ta + 4, v[4], v[5]);
+        tc::tmem_ld_x2(ta + 6, v[6], v[7]);
+        tc::tmem_ld_x1(ta + 8, v[8]);
+        tc::tmem_wait_ld(v);
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&dfree[k]);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+          const float L = __uint_as_float(v[i]);
+          const float q = fmaf(L, invp, MAGIC) - MAGIC;
+          const float r = fmaf(-q, pf, L);
+          const int ri = __float_as_int(r + MAGIC) - 0x4B400000;
+          const int4 kv = kp[i * 4 + k];
+          acc[i][0] += kv.x * ri;
+          acc[i][1] += kv.y * ri;
+          acc[i][2] += kv.z * ri;
+          acc[i][3] += kv.w * ri;
+        }
       }
-      if (ok) {
-        const int4* kp = reinterpret_cast<const int4*>(sKey + (e & 3) * TC_KEY_INTS) + 9 * g * 4;
-        const uint32_t tb = tbase + ((uint32_t)(32 * qd) << 16) + 256 * (e & 1) + 10 * g;
-        for (int k = 0; k < 4; ++k) {
-          const uint32_t ta = tb + TC_N * k;
-          uint32_t v[9];
-          tc::tmem_ld_x2(ta + 0, v[0], v[1]);
-          tc::tmem_ld_x2(ta + 2, v[2], v[3]);
-          tc::tmem_ld_x2(ta + 4, v[4], v[5]);
-          tc::tmem_ld_x2(ta + 6, v[6], v[7]);
-          tc::tmem_ld_x1(ta + 8, v[8]);
-          tc::tmem_wait_ld(v);
+      if (ok && ++since == reduce_every) {
+        since = 0;
 #pragma unroll
-          for (int i = 0; i < 9; ++i) {
-            const float L = __uint_as_float(v[i]);
-            const float q = fmaf(L, invp, MAGIC) - MAGIC;
-            const float r = fmaf(-q, pf, L);
-            const int ri = __float_as_int(r + MAGIC) - 0x4B400000;
-            const int4 kv = kp[i * 4 + k];
-            acc[i][0] += kv.x * ri;
-            acc[i][1] += kv.y * ri;
-            acc[i][2] += kv.z * ri;
-            acc[i][3] += kv.w * ri;
-          }
-        }
-        if (++since == reduce_every) {
-          since = 0;
+        for (int i = 0; i < 9; ++i)
 #pragma unroll
-          for (int i = 0; i < 9; ++i)
-#pragma unroll
-            for (int l = 0; l < 4; ++l) acc[i][l] = (int)reduce32((uint32_t)acc[i][l] + bias, bar, p);
-        }
+          for (int l = 0; l < 4; ++l) acc[i][l] = (int)reduce32((uint32_t)acc[i][l] + bias, bar, p);
       }
     }
-    tc::fence_before_sync();
+    if (!ok && lane == 0 && !*abort_flag) {
+      *abort_flag = 1;
+      atomicExch(status, 3);
+    }
     if (!*abort_flag) {
       uint32_t* out = partial + ((((size_t)split * nprimes + pi) * COLUMNS + col0 + c) * LEAVES + TC_LEAVES * third +
                                  9 * g) * 4;
@@ -698,10 +741,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
     }
   }
-  // Drain: the last commit covers every MMA issued; TMEM is released only after it.
-  if (issuer && last >= 0) {
+  // Drain: an issuer's last commit covers every MMA it issued; TMEM is released only after them.
+  if (warp >= 28 && lane == 0 && last_e >= 0) {
     const long long t0 = clock64();
-    while (!tc::mbar_try_wait(&t_full[last & 1], (last >> 1) & 1) && clock64() - t0 < TC_WAIT_CYCLES) {
+    while (!tc::mbar_try_wait(&done[warp - 28], last_e & 1) && clock64() - t0 < TC_WAIT_CYCLES) {
     }
   }
   tc::fence_before_sync();

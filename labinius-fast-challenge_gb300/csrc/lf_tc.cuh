@@ -1,6 +1,6 @@
 // Blackwell (sm_103a) tensor-core and barrier primitives in inline PTX: mbarriers, tensor memory
 // (tcgen05.alloc / ld / dealloc), the single-thread tcgen05.mma with shared-memory operand
-// descriptors, and the proxy fences between them. Only what the commitment kernel uses.
+// descriptors or a tensor-memory A operand, and the proxy fences between them.
 #pragma once
 #include <cstdint>
 
@@ -83,6 +83,17 @@ __device__ __forceinline__ void tmem_ld_x16(uint32_t taddr, uint32_t (&v)[16]) {
         "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
       : "r"(taddr));
 }
+// Warp-collective store of 16 consecutive 32-bit columns of the warp's 32 lanes (lane i of the
+// warp writes TMEM lane (taddr >> 16) + i). Complete after tmem_wait_st.
+__device__ __forceinline__ void tmem_st_x16(uint32_t taddr, const uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16};" ::"r"(taddr),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
+      "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 // Completes the warp's outstanding tensor-memory loads; the registers passed through tie their
 // later uses to this point.
 template <int N>
@@ -116,6 +127,19 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
       "}" ::"r"(d_tmem),
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// D[tmem] (+)= A[tmem] * B[smem]^T, K = 16: A's row i in TMEM lane i, its K elements packed two
+// per 32-bit column (even K index in the low half), 8 columns per instruction.
+__device__ __forceinline__ void mma_bf16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n"
+      "}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
 // The barrier receives one arrival when every MMA this thread issued before has completed.
