@@ -650,7 +650,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       bool ok = true;
       for (int k = 0; k < 4 && ok; ++k) {
-        if (e > 0) ok = __all_sync(0xffffffffu, tc::mbar_wait(&done[k], (e - 1) & 1, abort_flag, TC_WAIT_CYCLES));
+        if (e > 0) ok = __all_sync(0xffffffffu, tc::mbar_wait_fast(&done[k], (e - 1) & 1, abort_flag, TC_WAIT_CYCLES));
         if (!ok) break;
         tc::fence_after_sync();
         commit_expand_word(tl + 128 * k, wring[((e % 3) * TC_COLS + t) * 4 + k]);
@@ -685,10 +685,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     int since = 0;
     bool ok = true;
     for (int e = 0; e < nelem && ok; ++e) {
-      ok = __all_sync(0xffffffffu, tc::mbar_wait(&kfull[e & 3], (e >> 2) & 1, abort_flag, TC_WAIT_CYCLES));
+      ok = __all_sync(0xffffffffu, tc::mbar_wait_fast(&kfull[e & 3], (e >> 2) & 1, abort_flag, TC_WAIT_CYCLES));
       const int4* kp = reinterpret_cast<const int4*>(sKey + (e & 3) * TC_KEY_INTS) + 9 * g * 4;
       for (int k = 0; k < 4 && ok; ++k) {
-        ok = __all_sync(0xffffffffu, tc::mbar_wait(&done[k], e & 1, abort_flag, TC_WAIT_CYCLES));
+        ok = __all_sync(0xffffffffu, tc::mbar_wait_fast(&done[k], e & 1, abort_flag, TC_WAIT_CYCLES));
         if (!ok) break;
         tc::fence_after_sync();
         const uint32_t ta = tb + 128 * k;

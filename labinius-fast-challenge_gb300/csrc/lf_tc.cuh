@@ -50,6 +50,27 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const 
   return true;
 }
 
+// Non-blocking test of a phase; then the bounded suspending wait when it has not completed yet.
+// For a waiter that usually finds the phase complete (a suspending try_wait costs hundreds of
+// cycles even then).
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n"
+      "}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_fast(uint64_t* bar, uint32_t parity, const volatile int* abort,
+                                               long long limit_cycles) {
+  return mbar_test_wait(bar, parity) || mbar_wait(bar, parity, abort, limit_cycles);
+}
+
 // ---- proxy fences ----
 // Generic-proxy shared-memory writes become visible to the tensor core (async proxy).
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
