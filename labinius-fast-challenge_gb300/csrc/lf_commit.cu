@@ -33,7 +33,8 @@ constexpr int TC_K = 256;                            // MMA K: 128 bits x 2 limb
 constexpr int TC_THREADS = 32 * 32;                  // 24 epilogue, 4 producer and 4 issuer warps
 constexpr int TC_B_BYTES = TC_N * TC_K * 2;          // 32 KB
 constexpr int TC_KEY_INTS = TC_LEAVES * 16;          // one element's key rows for the block's leaves
-constexpr int TC_SMEM = TC_B_BYTES + 4 * TC_KEY_INTS * 4 + 3 * TC_COLS * 64 + 3 * TC_KEY_INTS * 4 + 16 * 8 + 16;
+constexpr int TC_SMEM =
+    TC_B_BYTES + 4 * TC_KEY_INTS * 4 + 3 * TC_COLS * 64 + 3 * TC_KEY_INTS * 4 + 4 * TC_LEAVES * 16 + 16 * 8 + 16;
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;   // ~1 s at 2 GHz
 
 static void fill_btiles(const PrimePlan& pl, const PrimeConst& c, uint16_t* out);
@@ -545,7 +546,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   int* sKey = reinterpret_cast<int*>(tsm + TC_B_BYTES);                            // [4][TC_KEY_INTS]
   uint4* wring = reinterpret_cast<uint4*>(sKey + 4 * TC_KEY_INTS);                  // [3][128 columns][4 words]
   uint4* kraw = wring + 3 * TC_COLS * 4;                                            // [3][TC_KEY_INTS / 4]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(kraw + 3 * (TC_KEY_INTS / 4));
+  uint4* csum = kraw + 3 * (TC_KEY_INTS / 4);                                       // [4][TC_LEAVES]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(csum + 4 * TC_LEAVES);
   uint64_t* full = bars;        // [4] producers wrote stage k's A (128 arrivals)
   uint64_t* done = bars + 4;    // [4] the MMAs of stage k completed (tensor-core commit)
   uint64_t* dfree = bars + 8;   // [4] the epilogue loaded stage k's D (24 arrivals)
@@ -615,6 +617,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const uint4* ksrc = reinterpret_cast<const uint4*>(key) +
                         ((size_t)pi * elements * LEAVES + TC_LEAVES * third) * 4;
     const int half = (int)(p - 1) / 2;
+    const int reduce_every = (int)pcs[pi].reduce_every;
+    uint4 cum[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
     const uint32_t tl = tbase + ((uint32_t)(32 * (warp - 24)) << 16);
     auto fetch = [&](int e) {  // element e's words (this column) and key rows t, t + 128 into ring slot e % 3
       if (e < nelem) {
@@ -637,14 +641,31 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       {
         const uint4* kr = kraw + (e % 3) * (TC_KEY_INTS / 4);
         int4* kd = reinterpret_cast<int4*>(sKey + (e & 3) * TC_KEY_INTS);
-        for (int i = t; i < TC_KEY_INTS / 4; i += 128) {
-          const uint4 u = kr[i];
-          int4 v;  // centred into (-p/2, p/2]
-          v.x = (int)u.x > half ? (int)u.x - (int)p : (int)u.x;
-          v.y = (int)u.y > half ? (int)u.y - (int)p : (int)u.y;
-          v.z = (int)u.z > half ? (int)u.z - (int)p : (int)u.z;
-          v.w = (int)u.w > half ? (int)u.w - (int)p : (int)u.w;
-          kd[i] = v;
+        const bool restart = e % reduce_every == 0;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const int i = t + 128 * j;  // key row: leaf i / 4, word i % 4
+          uint4 v = make_uint4(0, 0, 0, 0);
+          if (i < TC_KEY_INTS / 4) {
+            const uint4 u = kr[i];  // centred into (-p/2, p/2]
+            v.x = (int)u.x > half ? u.x - p : u.x;
+            v.y = (int)u.y > half ? u.y - p : u.y;
+            v.z = (int)u.z > half ? u.z - p : u.z;
+            v.w = (int)u.w > half ? u.w - p : u.w;
+            reinterpret_cast<uint4*>(kd)[i] = v;
+          }
+          // the leaf's four rows sit in lanes 4 (i / 4) .. + 3: their sum, and its running total
+          // over the epilogue's reduction window, kept by the first of them (mod 2^32)
+#pragma unroll
+          for (int o = 1; o <= 2; o <<= 1) {
+            v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+            v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+            v.z += __shfl_xor_sync(0xffffffffu, v.z, o);
+            v.w += __shfl_xor_sync(0xffffffffu, v.w, o);
+          }
+          if (restart) cum[j] = make_uint4(0, 0, 0, 0);
+          cum[j].x += v.x, cum[j].y += v.y, cum[j].z += v.z, cum[j].w += v.w;
+          if ((t & 3) == 0 && i < TC_KEY_INTS / 4) csum[(e & 3) * TC_LEAVES + (i >> 2)] = cum[j];
         }
         tc::mbar_arrive(&kfull[e & 3]);
       }
@@ -676,11 +697,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const float pf = (float)p, invp = 1.0f / (float)p;
     const float MAGIC = 12582912.0f;  // 1.5 * 2^23: adding it rounds to an integer
     const uint32_t bias = (0x80000000u / p) * p;
-    int acc[9][4];
+    // acc accumulates key * (0x4B400000 + r) mod 2^32; settling a reduction window subtracts
+    // 0x4B400000 times the window's key sums (kept by the producers), which leaves the exact
+    // sum of key * r (it fits in 32 bits over reduce_every elements), and reduces it mod p.
+    uint32_t acc[9][4];
 #pragma unroll
     for (int i = 0; i < 9; ++i)
 #pragma unroll
       for (int l = 0; l < 4; ++l) acc[i][l] = 0;
+    auto settle = [&](int e) {
+      const uint4* cs = csum + (e & 3) * TC_LEAVES + 9 * g;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        const uint4 w = cs[i];
+        acc[i][0] = reduce32(acc[i][0] - 0x4B400000u * w.x + bias, bar, p);
+        acc[i][1] = reduce32(acc[i][1] - 0x4B400000u * w.y + bias, bar, p);
+        acc[i][2] = reduce32(acc[i][2] - 0x4B400000u * w.z + bias, bar, p);
+        acc[i][3] = reduce32(acc[i][3] - 0x4B400000u * w.w + bias, bar, p);
+      }
+    };
     const uint32_t tb = tbase + ((uint32_t)(32 * qd) << 16) + 64 + 10 * g;
     int since = 0;
     bool ok = true;
@@ -707,8 +742,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           const float L = __uint_as_float(v[i]);
           const float q = fmaf(L, invp, MAGIC) - MAGIC;
           const float r = fmaf(-q, pf, L);
-          const int ri = __float_as_int(r + MAGIC) - 0x4B400000;
-          const int4 kv = kp[i * 4 + k];
+          const uint32_t ri = __float_as_uint(r + MAGIC);  // 0x4B400000 + r
+          const uint4 kv = reinterpret_cast<const uint4*>(kp)[i * 4 + k];
           acc[i][0] += kv.x * ri;
           acc[i][1] += kv.y * ri;
           acc[i][2] += kv.z * ri;
@@ -717,10 +752,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       if (ok && ++since == reduce_every) {
         since = 0;
-#pragma unroll
-        for (int i = 0; i < 9; ++i)
-#pragma unroll
-          for (int l = 0; l < 4; ++l) acc[i][l] = (int)reduce32((uint32_t)acc[i][l] + bias, bar, p);
+        settle(e);
       }
     }
     if (!ok && lane == 0 && !*abort_flag) {
@@ -728,17 +760,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       atomicExch(status, 3);
     }
     if (!*abort_flag) {
+      if (since > 0) settle(nelem - 1);
       uint32_t* out = partial + ((((size_t)split * nprimes + pi) * COLUMNS + col0 + c) * LEAVES + TC_LEAVES * third +
                                  9 * g) * 4;
 #pragma unroll
-      for (int i = 0; i < 9; ++i) {
-        uint4 o;
-        o.x = reduce32((uint32_t)acc[i][0] + bias, bar, p);
-        o.y = reduce32((uint32_t)acc[i][1] + bias, bar, p);
-        o.z = reduce32((uint32_t)acc[i][2] + bias, bar, p);
-        o.w = reduce32((uint32_t)acc[i][3] + bias, bar, p);
-        reinterpret_cast<uint4*>(out)[i] = o;
-      }
+      for (int i = 0; i < 9; ++i)
+        reinterpret_cast<uint4*>(out)[i] = make_uint4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
     }
   }
   // Drain: an issuer's last commit covers every MMA it issued; TMEM is released only after them.
