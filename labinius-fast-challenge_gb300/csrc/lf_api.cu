@@ -1,6 +1,7 @@
 // Host side of the prover: the C ABI, device buffers, the Fiat-Shamir transcript and the phase
 // pipeline of one proof (solution/proof_generate/src/main.rs:1692-2009; the checker's
 // reference prover verifier/proof_verify/src/reference.rs:137-177 fixes every byte).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -269,6 +270,13 @@ struct lf_ctx {
   cudaStream_t touch_stream = nullptr;
   cudaEvent_t touched = nullptr, up_t0 = nullptr, up_t1 = nullptr;
   int pageable_access = 0;
+  // lf_prove from page-locked memory: the table goes up in parts (element ranges of every column)
+  // and the copy stream writes the proof's epoch into ready[i] after part i (a stream memory
+  // operation: no kernel, so it cannot wait behind the commitment's blocks); the commitment starts
+  // at once and each block waits for the part it reads.
+  uint32_t* ready = nullptr;  // device, TABLE_PARTS flags
+  uint32_t epoch = 0;
+  CUresult (*write_value)(CUstream, CUdeviceptr, cuuint32_t, unsigned int) = nullptr;
   // serving: FIFO of submitted jobs, drained by one worker thread per lane
   struct Queued {
     uint64_t ticket;
@@ -292,6 +300,8 @@ struct lf_ctx {
 };
 
 namespace {
+
+constexpr int TABLE_PARTS = 16;  // parts of a page-locked host table (lf_prove)
 
 int fail(lf_ctx* c, int code, const std::string& msg) {
   if (c) {
@@ -552,14 +562,33 @@ int side_streams(lf_ctx* ctx) {
   CK(cudaEventCreateWithFlags(&ctx->touched, cudaEventDisableTiming));
   CK(cudaEventCreate(&ctx->up_t0));
   CK(cudaEventCreate(&ctx->up_t1));
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult qr{};
+  if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &fn, 12000, cudaEnableDefault, &qr) == cudaSuccess &&
+      qr == cudaDriverEntryPointSuccess && fn && cudaMalloc(&ctx->ready, TABLE_PARTS * 4) == cudaSuccess &&
+      cudaMemset(ctx->ready, 0, TABLE_PARTS * 4) == cudaSuccess) {
+    ctx->write_value = reinterpret_cast<CUresult (*)(CUstream, CUdeviceptr, cuuint32_t, unsigned int)>(fn);
+  }
+  cudaGetLastError();
   return LF_OK;
 }
 
 
+// A table still being copied in parts (lf_prove from page-locked memory): the commitment reads part
+// i once ready[i] holds epoch; every later reader waits for `done`.
+struct TableStream {
+  const uint32_t* ready;
+  uint32_t epoch;
+  int part_elems;
+  cudaEvent_t done;
+};
+
 // table_ready / proof_ready (may be null): events the prover's stream waits for before the first
-// kernel that reads the table and before the first device write into `proof`.
+// kernel that reads the table and before the first device write into `proof`. With ts, the
+// commitment starts before the table is complete (table_ready is then unused).
 int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, const uint4* table, uint8_t* proof,
-                 size_t* proof_len, cudaEvent_t table_ready = nullptr, cudaEvent_t proof_ready = nullptr) {
+                 size_t* proof_len, cudaEvent_t table_ready = nullptr, cudaEvent_t proof_ready = nullptr,
+                 const TableStream* ts = nullptr) {
   cudaStream_t st = ctx->stream;
   const size_t width = coefficient_bytes(q);
   const size_t commit_bytes = width * COLUMNS * RING_N;
@@ -589,9 +618,16 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   // (One commitment launch: splitting it by element ranges, so that each starts as its part of a
   // host table arrives, cost it its wave balance: 4 launches of about 5 splits each ran 1.4 ms
   // longer than one launch at 2^31 bits.)
-  if (table_ready) CK(cudaStreamWaitEvent(st, table_ready, 0));
-  launch_commit(mp, sh, table, ctx->key->key.as<uint32_t>(), ctx->key->btiles.as<uint16_t>(),
-                ctx->partial.as<uint32_t>(), splits, ctx->status.as<int>(), st);
+  if (ts) {
+    launch_commit(mp, sh, table, ctx->key->key.as<uint32_t>(), ctx->key->btiles.as<uint16_t>(),
+                  ctx->partial.as<uint32_t>(), splits, ctx->status.as<int>(), st, 0, -1, ts->ready, ts->epoch,
+                  ts->part_elems);
+    CK(cudaStreamWaitEvent(st, ts->done, 0));  // every later kernel reads the whole table
+  } else {
+    if (table_ready) CK(cudaStreamWaitEvent(st, table_ready, 0));
+    launch_commit(mp, sh, table, ctx->key->key.as<uint32_t>(), ctx->key->btiles.as<uint16_t>(),
+                  ctx->partial.as<uint32_t>(), splits, ctx->status.as<int>(), st);
+  }
   cudaEventRecord(ctx->ev[11], st);
   launch_commit_finish(mp, sh, ctx->partial.as<uint32_t>(), splits, ctx->stream_buf.as<uint8_t>() + STREAM_PREFIX, st);
   CKL("commitment");
@@ -1378,6 +1414,7 @@ void lf_ctx_destroy(lf_ctx* ctx) {
     if (ev) cudaEventDestroy(ev);
   if (ctx->upload_stream) cudaStreamDestroy(ctx->upload_stream);
   if (ctx->touch_stream) cudaStreamDestroy(ctx->touch_stream);
+  if (ctx->ready) cudaFree(ctx->ready);
   for (cudaEvent_t e : {ctx->touched, ctx->up_t0, ctx->up_t1})
     if (e) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1455,7 +1492,31 @@ int lf_prove(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32
   // first-access cost of its pages is not paid by the proof's own copies.
   cudaEventRecord(ctx->ev[0], ctx->stream);
   CK(cudaEventRecord(ctx->up_t0, ctx->upload_stream));
-  CK(cudaMemcpyAsync(ctx->table.p, table, table_bytes, cudaMemcpyHostToDevice, ctx->upload_stream));
+  // Page-locked tables go up in TABLE_PARTS element ranges of every column (one 2-D copy each),
+  // each followed by its ready flag; the commitment reads a part as soon as it has arrived.
+  cudaPointerAttributes ta{};
+  const bool locked = cudaPointerGetAttributes(&ta, table) == cudaSuccess && ta.type == cudaMemoryTypeHost;
+  cudaGetLastError();
+  TableStream tstream{};
+  const bool streamed = locked && ctx->write_value && sh.ring_elements >= (uint64_t)TABLE_PARTS;
+  if (streamed) {
+    const uint32_t epoch = ++ctx->epoch == 0 ? ++ctx->epoch : ctx->epoch;  // never 0, the flags' initial value
+    const int part_elems = (int)((sh.ring_elements + TABLE_PARTS - 1) / TABLE_PARTS);
+    const size_t pitch = (size_t)16 << sh.rl;  // one column
+    for (int i = 0; i < TABLE_PARTS; ++i) {
+      const uint64_t m0 = (uint64_t)i * part_elems, m1 = std::min<uint64_t>(sh.ring_elements, m0 + part_elems);
+      if (m0 >= m1) break;
+      CK(cudaMemcpy2DAsync(ctx->table.as<uint8_t>() + 64 * m0, pitch, static_cast<const uint8_t*>(table) + 64 * m0,
+                           pitch, 64 * (m1 - m0), COLUMNS, cudaMemcpyHostToDevice, ctx->upload_stream));
+      if (ctx->write_value(reinterpret_cast<CUstream>(ctx->upload_stream),
+                           reinterpret_cast<CUdeviceptr>(ctx->ready + i), epoch, CU_STREAM_WRITE_VALUE_DEFAULT) !=
+          CUDA_SUCCESS)
+        return fail(ctx, LF_E_CUDA, "stream write of a table part's ready flag failed");
+    }
+    tstream = TableStream{ctx->ready, epoch, part_elems, ctx->uploaded[0]};
+  } else {
+    CK(cudaMemcpyAsync(ctx->table.p, table, table_bytes, cudaMemcpyHostToDevice, ctx->upload_stream));
+  }
   CK(cudaEventRecord(ctx->uploaded[0], ctx->upload_stream));
   CK(cudaEventRecord(ctx->up_t1, ctx->upload_stream));
   cudaEvent_t proof_ready = nullptr;
@@ -1468,7 +1529,8 @@ int lf_prove(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32
     proof_ready = ctx->touched;
   }
   cudaGetLastError();  // cudaPointerGetAttributes on plain host memory leaves no error behind
-  rc = prove_device(ctx, seed, q, sh, ctx->table.as<uint4>(), proof, proof_len, ctx->uploaded[0], proof_ready);
+  rc = prove_device(ctx, seed, q, sh, ctx->table.as<uint4>(), proof, proof_len, ctx->uploaded[0], proof_ready,
+                    streamed ? &tstream : nullptr);
   // (a proof that failed early may not have waited for the side streams)
   cudaStreamSynchronize(ctx->upload_stream);
   cudaStreamSynchronize(ctx->touch_stream);

@@ -509,6 +509,11 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
 // *status = 3 and the abort flag, on which every role leaves its loop; TMEM is released after the
 // issuers' last commits drained.
 // ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
 // One table word -> the 64 TMEM columns of its A row (K positions 2o and 2o + 1 in column o): u32 o
 // holds bits o % 16 and o % 16 + 16 of word o / 16, and a set bit at K position kappa is the bf16
 // with the single exponent bit 11 + (kappa / 2 & 3): 2^-111, 2^-95, 2^-63 or 2. One shift of the
@@ -540,7 +545,8 @@ static double commit_bit_value(int kappa) {
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_commit_tc(const uint4* __restrict__ table, const uint32_t* __restrict__ key, const uint4* __restrict__ btiles,
                 const PrimeConst* __restrict__ pcs, uint32_t* __restrict__ partial, int rl, int elements,
-                int per_split, int nprimes, int split_base, int* status) {
+                int per_split, int nprimes, int split_base, int* status, const uint32_t* ready, uint32_t epoch,
+                int part_elems) {
   extern __shared__ __align__(1024) uint8_t tsm[];
   uint8_t* sB = tsm;
   int* sKey = reinterpret_cast<int*>(tsm + TC_B_BYTES);                            // [4][TC_KEY_INTS]
@@ -620,8 +626,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int reduce_every = (int)pcs[pi].reduce_every;
     uint4 cum[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
     const uint32_t tl = tbase + ((uint32_t)(32 * (warp - 24)) << 16);
+    int ready_part = -1;  // the table is known to be in device memory up to this part
     auto fetch = [&](int e) {  // element e's words (this column) and key rows t, t + 128 into ring slot e % 3
-      if (e < nelem) {
+      if (e < nelem && ready && (m_begin + e) / part_elems > ready_part) {
+        // The table is still arriving: part (m_begin + e) / part_elems is there once the copy
+        // stream has written the proof's epoch into its flag (after the part's copy).
+        const int part = (m_begin + e) / part_elems;
+        const long long t0 = clock64();
+        while ((int)(ld_acquire_u32(ready + part) - epoch) < 0) {
+          if (*abort_flag || *reinterpret_cast<volatile int*>(status) || clock64() - t0 > TC_WAIT_CYCLES) {
+            if (!*abort_flag) {
+              *abort_flag = 1;
+              atomicExch(status, 3);
+            }
+            break;
+          }
+          __nanosleep(256);
+        }
+        ready_part = part;
+      }
+      if (e < nelem && !*abort_flag) {
         const size_t m = (size_t)(m_begin + e);
         uint4* w = wring + ((e % 3) * TC_COLS + t) * 4;
 #pragma unroll
@@ -833,7 +857,7 @@ int commit_splits(uint64_t elements, int nprimes, int sms) {
 
 void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint32_t* key,
                    const uint16_t* btiles, uint32_t* partial, int splits, int* status, cudaStream_t s, int split_begin,
-                   int split_end) {
+                   int split_end, const uint32_t* ready, uint32_t epoch, int part_elems) {
   const int elements = (int)sh.ring_elements;
   const int per = (elements + splits - 1) / splits;
   if (split_end < 0) split_end = splits;
@@ -842,7 +866,8 @@ void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, c
   smem_limit(k_commit_tc, TC_SMEM, attr);
   dim3 grid(mp.nprimes * 3, COLUMNS / TC_COLS, split_end - split_begin);
   k_commit_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(table, key, reinterpret_cast<const uint4*>(btiles), mp.dconsts, partial,
-                                                 sh.rl, elements, per, mp.nprimes, split_begin, status);
+                                                 sh.rl, elements, per, mp.nprimes, split_begin, status, ready, epoch,
+                                                 part_elems > 0 ? part_elems : elements);
 }
 
 // Element range [m0, m1) of split range [s0, s1): the part of every column those splits read.

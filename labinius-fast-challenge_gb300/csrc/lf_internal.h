@@ -175,9 +175,12 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
                           uint32_t* key, cudaStream_t s);
 int commit_splits(uint64_t elements, int nprimes, int sms);
 // Splits [split_begin, split_end) of the `splits` element splits (split_end < 0: all of them).
+// ready (device, may be null): the table is still being copied in parts of part_elems ring
+// elements (of every column); part i may be read once ready[i] - epoch >= 0 (as int32).
 void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint32_t* key,
                    const uint16_t* btiles, uint32_t* partial, int splits, int* status, cudaStream_t s,
-                   int split_begin = 0, int split_end = -1);
+                   int split_begin = 0, int split_end = -1, const uint32_t* ready = nullptr, uint32_t epoch = 0,
+                   int part_elems = 0);
 void commit_split_elements(uint64_t elements, int splits, int s0, int s1, uint64_t& m0, uint64_t& m1);
 void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t* partial, int splits, uint8_t* out,
                           cudaStream_t s, int ncols = COLUMNS);

@@ -70,6 +70,29 @@ def test_device_table_writer_matches_oracle(prover, oracle):
         prover.free(dev)
 
 
+@pytest.mark.parametrize("log_vars", [22, 27, 31])
+def test_page_locked_table_streams_into_the_commitment(prover, oracle, log_vars):
+    # lf_prove from page-locked host memory copies the table in 16 element ranges while the
+    # commitment already runs, each block waiting for its range: the proof is the one of the same
+    # table proven from device memory (and, at 2^22 bits, the oracle's).
+    torch = pytest.importorskip("torch")
+    seed = SEEDS[0]
+    n = (1 << log_vars) // 8
+    dev = torch.empty(n, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    prover.write_table_device(seed, log_vars, dev.data_ptr())
+    proof_dev, n_dev = prover.prove_device(seed, dev.data_ptr(), log_vars)
+    torch.cuda.synchronize()
+    host = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    host.copy_(dev)
+    torch.cuda.synchronize()
+    for _ in range(2):  # the second run finds the ready flags set by the first, under a new epoch
+        got = prover.prove(seed, host.numpy(), log_vars)
+        assert got == bytes(proof_dev[:n_dev])
+    if log_vars == 22:
+        assert got == oracle.prove(seed, oracle.write_table(seed, log_vars), log_vars)
+
+
 def test_repeatable(prover, oracle):
     log_vars = 20
     seed = SEEDS[1]
