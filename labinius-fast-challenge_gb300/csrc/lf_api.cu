@@ -854,7 +854,46 @@ using clk = std::chrono::steady_clock;
 double ms_between(clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); }
 
 // One job with the context lock held; table_dev is the job's table already on the device.
-int run_job(lf_ctx* ctx, const lf_job& j, const uint4* table_dev, size_t* proof_len) {
+// Starts the copy of a host table into ctx->table on ctx's copy stream. A page-locked table goes up
+// in TABLE_PARTS element ranges of every column (one 2-D copy each), each followed by a stream
+// write of the proof's epoch into its ready flag, and *ts describes them (streamed = true): the
+// commitment reads a range as soon as it has arrived. Any other table goes up in one copy whose
+// completion is ctx->uploaded[0].
+int start_table_upload(lf_ctx* ctx, const void* table, size_t table_bytes, const Shape& sh, TableStream* ts,
+                       bool* streamed) {
+  int rc = side_streams(ctx);
+  if (rc) return rc;
+  CK(ctx->table.ensure(table_bytes));
+  CK(cudaEventRecord(ctx->up_t0, ctx->upload_stream));
+  cudaPointerAttributes ta{};
+  const bool locked = cudaPointerGetAttributes(&ta, table) == cudaSuccess && ta.type == cudaMemoryTypeHost;
+  cudaGetLastError();  // plain host memory leaves an error behind on some drivers
+  *streamed = locked && ctx->write_value && sh.ring_elements >= (uint64_t)TABLE_PARTS;
+  if (*streamed) {
+    const uint32_t epoch = ++ctx->epoch == 0 ? ++ctx->epoch : ctx->epoch;  // never 0, the flags' initial value
+    const int part_elems = (int)((sh.ring_elements + TABLE_PARTS - 1) / TABLE_PARTS);
+    const size_t pitch = (size_t)16 << sh.rl;  // one column
+    for (int i = 0; i < TABLE_PARTS; ++i) {
+      const uint64_t m0 = (uint64_t)i * part_elems, m1 = std::min<uint64_t>(sh.ring_elements, m0 + part_elems);
+      if (m0 >= m1) break;
+      CK(cudaMemcpy2DAsync(ctx->table.as<uint8_t>() + 64 * m0, pitch, static_cast<const uint8_t*>(table) + 64 * m0,
+                           pitch, 64 * (m1 - m0), COLUMNS, cudaMemcpyHostToDevice, ctx->upload_stream));
+      if (ctx->write_value(reinterpret_cast<CUstream>(ctx->upload_stream), reinterpret_cast<CUdeviceptr>(ctx->ready + i),
+                         epoch, CU_STREAM_WRITE_VALUE_DEFAULT) != CUDA_SUCCESS)
+        return fail(ctx, LF_E_CUDA, "stream write of a table part's ready flag failed");
+    }
+    *ts = TableStream{ctx->ready, epoch, part_elems, ctx->uploaded[0]};
+  } else {
+    CK(cudaMemcpyAsync(ctx->table.p, table, table_bytes, cudaMemcpyHostToDevice, ctx->upload_stream));
+  }
+  CK(cudaEventRecord(ctx->uploaded[0], ctx->upload_stream));
+  CK(cudaEventRecord(ctx->up_t1, ctx->upload_stream));
+  return LF_OK;
+}
+
+// A job's proof; a host table is copied by start_table_upload (streamed into the commitment when
+// it is page-locked).
+int run_job(lf_ctx* ctx, const lf_job& j, size_t* proof_len) {
   u128 q;
   Shape sh;
   int rc = check_job(ctx, j, q, sh);
@@ -862,7 +901,16 @@ int run_job(lf_ctx* ctx, const lf_job& j, const uint4* table_dev, size_t* proof_
   cudaSetDevice(ctx->device);
   ctx->prof = lf_profile{};
   cudaEventRecord(ctx->ev[0], ctx->stream);
-  return prove_device(ctx, j.seed, q, sh, table_dev, j.proof, proof_len);
+  if (j.table_on_device)
+    return prove_device(ctx, j.seed, q, sh, reinterpret_cast<const uint4*>(j.table), j.proof, proof_len);
+  if (j.table_bytes != sh.words * 16) return fail(ctx, LF_E_TABLE_LEN, "witness table has the wrong length");
+  TableStream ts{};
+  bool streamed = false;
+  if ((rc = start_table_upload(ctx, j.table, j.table_bytes, sh, &ts, &streamed))) return rc;
+  rc = prove_device(ctx, j.seed, q, sh, ctx->table.as<uint4>(), j.proof, proof_len, ctx->uploaded[0], nullptr,
+                    streamed ? &ts : nullptr);
+  cudaStreamSynchronize(ctx->upload_stream);  // (a proof that failed early may not have waited for it)
+  return rc;
 }
 
 // One serving lane: `c` (the owner or one of its lanes) proves requests from the owner's FIFO. The front
@@ -891,20 +939,7 @@ void serve_loop(lf_ctx* owner, lf_ctx* c) {
     r.queue_ms = ms_between(item.submitted, start);
     {
       std::lock_guard<std::mutex> g(c->mu);
-      const lf_job& j = item.job;
-      const uint4* table = reinterpret_cast<const uint4*>(j.table);
-      r.status = LF_OK;
-      if (!j.table_on_device) {
-        Shape sh;
-        if (sh.set(j.log_vars) && j.table_bytes == sh.words * 16) {
-          cudaSetDevice(c->device);
-          if (c->table.ensure(j.table_bytes) != cudaSuccess ||
-              cudaMemcpyAsync(c->table.p, j.table, j.table_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
-            r.status = fail(c, LF_E_CUDA, "table upload failed");
-          table = c->table.as<uint4>();
-        }
-      }
-      if (r.status == LF_OK) r.status = run_job(c, j, table, &r.proof_len);
+      r.status = run_job(c, item.job, &r.proof_len);
     }
     r.run_ms = ms_between(start, clk::now());
     {
@@ -1485,40 +1520,14 @@ int lf_prove(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32
   cudaSetDevice(ctx->device);
   auto t0 = std::chrono::steady_clock::now();
   ctx->prof = lf_profile{};
-  CK(ctx->table.ensure(table_bytes));
-  if ((rc = side_streams(ctx))) return rc;
   // The table goes up on the copy stream while the prover's stream builds (or finds) the key; the
-  // commitment waits for it. A pageable proof buffer is touched by the device meanwhile, so the
-  // first-access cost of its pages is not paid by the proof's own copies.
+  // commitment reads it as it arrives (page-locked) or waits for it. A pageable proof buffer is
+  // touched by the device meanwhile, so the first-access cost of its pages is not paid by the
+  // proof's own copies.
   cudaEventRecord(ctx->ev[0], ctx->stream);
-  CK(cudaEventRecord(ctx->up_t0, ctx->upload_stream));
-  // Page-locked tables go up in TABLE_PARTS element ranges of every column (one 2-D copy each),
-  // each followed by its ready flag; the commitment reads a part as soon as it has arrived.
-  cudaPointerAttributes ta{};
-  const bool locked = cudaPointerGetAttributes(&ta, table) == cudaSuccess && ta.type == cudaMemoryTypeHost;
-  cudaGetLastError();
   TableStream tstream{};
-  const bool streamed = locked && ctx->write_value && sh.ring_elements >= (uint64_t)TABLE_PARTS;
-  if (streamed) {
-    const uint32_t epoch = ++ctx->epoch == 0 ? ++ctx->epoch : ctx->epoch;  // never 0, the flags' initial value
-    const int part_elems = (int)((sh.ring_elements + TABLE_PARTS - 1) / TABLE_PARTS);
-    const size_t pitch = (size_t)16 << sh.rl;  // one column
-    for (int i = 0; i < TABLE_PARTS; ++i) {
-      const uint64_t m0 = (uint64_t)i * part_elems, m1 = std::min<uint64_t>(sh.ring_elements, m0 + part_elems);
-      if (m0 >= m1) break;
-      CK(cudaMemcpy2DAsync(ctx->table.as<uint8_t>() + 64 * m0, pitch, static_cast<const uint8_t*>(table) + 64 * m0,
-                           pitch, 64 * (m1 - m0), COLUMNS, cudaMemcpyHostToDevice, ctx->upload_stream));
-      if (ctx->write_value(reinterpret_cast<CUstream>(ctx->upload_stream),
-                           reinterpret_cast<CUdeviceptr>(ctx->ready + i), epoch, CU_STREAM_WRITE_VALUE_DEFAULT) !=
-          CUDA_SUCCESS)
-        return fail(ctx, LF_E_CUDA, "stream write of a table part's ready flag failed");
-    }
-    tstream = TableStream{ctx->ready, epoch, part_elems, ctx->uploaded[0]};
-  } else {
-    CK(cudaMemcpyAsync(ctx->table.p, table, table_bytes, cudaMemcpyHostToDevice, ctx->upload_stream));
-  }
-  CK(cudaEventRecord(ctx->uploaded[0], ctx->upload_stream));
-  CK(cudaEventRecord(ctx->up_t1, ctx->upload_stream));
+  bool streamed = false;
+  if ((rc = start_table_upload(ctx, table, table_bytes, sh, &tstream, &streamed))) return rc;
   cudaEvent_t proof_ready = nullptr;
   cudaPointerAttributes pa{};
   if (ctx->pageable_access && cudaPointerGetAttributes(&pa, proof) == cudaSuccess &&
@@ -1630,16 +1639,8 @@ void batch_lane(lf_ctx* c, bool lock, const lf_job* jobs, lf_result* results, co
     r = lf_result{};
     const auto start = clk::now();
     r.queue_ms = ms_between(t_batch, start);
-    const lf_job& j = jobs[i];
     r.status = pre[i];
-    const uint4* table = reinterpret_cast<const uint4*>(j.table);
-    if (r.status == LF_OK && !j.table_on_device) {
-      if (c->table.ensure(j.table_bytes) != cudaSuccess ||
-          cudaMemcpyAsync(c->table.p, j.table, j.table_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
-        r.status = fail(c, LF_E_CUDA, "table upload failed");
-      table = c->table.as<uint4>();
-    }
-    if (r.status == LF_OK) r.status = run_job(c, j, table, &r.proof_len);
+    if (r.status == LF_OK) r.status = run_job(c, jobs[i], &r.proof_len);
     r.run_ms = ms_between(start, clk::now());
   }
 }
@@ -1701,7 +1702,14 @@ int lf_prove_batch(lf_ctx* ctx, size_t n, const lf_job* jobs, lf_result* results
     }
     // The other buffer's job finished (prove_device ends in a stream synchronisation): fill it.
     up = i + 1 < n ? upload(i + 1, b ^ 1) : LF_OK;
-    if (r.status == LF_OK) r.status = run_job(ctx, j, table, &r.proof_len);
+    if (r.status == LF_OK) {
+      u128 q;
+      Shape sh;
+      check_job(ctx, j, q, sh);  // passed in pre[i]
+      ctx->prof = lf_profile{};
+      cudaEventRecord(ctx->ev[0], ctx->stream);
+      r.status = prove_device(ctx, j.seed, q, sh, table, j.proof, &r.proof_len);
+    }
     r.run_ms = ms_between(start, clk::now());
     if (r.status != LF_OK && first == LF_OK) first = r.status;
   }
