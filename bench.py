@@ -357,7 +357,7 @@ def micro_leg(lfgpu, prover, stream, ghash_log=28, moduli=("baseline", "2^64", "
     return out
 
 
-def serving_leg(lfgpu, prover, requests=100, rate=8.0, seed=20261):
+def serving_leg(lfgpu, prover, requests=500, rate=8.0, seed=20261):
     """Poisson arrivals at `rate`/s, L uniform over the integers 22..31 (log-uniform table sizes),
     a fresh seed per request, one page-locked table per shape; latency = queueing + proving as
     the server reports it. p50/p99 over the requests, for the context's lanes and, on the same
@@ -432,7 +432,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-table (lf_prove) leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched (lf_prove_batch) leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving (lf_submit/lf_poll) leg")
-    ap.add_argument("--serve-requests", type=int, default=100, help="requests of the serving leg (Poisson, 8/s)")
+    ap.add_argument("--serve-requests", type=int, default=500, help="requests of the serving leg (Poisson, 8/s)")
     ap.add_argument("--lanes", type=int, default=0, help="proofs in flight per context (0 = the library default)")
     ap.add_argument("--no-micro", action="store_true", help="skip the ring / GHASH / a_times_v microbenchmark")
     ap.add_argument("--only-batch", action="store_true", help="run only the batched leg and exit")
