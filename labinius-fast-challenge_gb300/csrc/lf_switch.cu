@@ -472,7 +472,7 @@ void launch_switch_round_blocks(const b128* R, uint64_t X, b128 rho, const f162*
   const int smem = 16 * 256 * 24;
   static std::atomic<unsigned long long> attr{0};
   smem_limit(k_switch_round_blocks, smem, attr);
-  unsigned g = (unsigned)(X < (uint64_t)sms ? X : (uint64_t)sms);
+  unsigned g = (unsigned)(X < 2ull * sms ? X : 2ull * sms);  // two blocks per SM (98 KB tables each)
   k_switch_round_blocks<<<g, 128, smem, s>>>(R, X, rho, phi, w, msg, out);
 }
 void launch_g_update(const f162* psi, b128 rho, f162 rp, f162* Gn, cudaStream_t s) {
