@@ -663,7 +663,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   const uint64_t nsmall = 4096;
   const uint64_t xmax = 1ull << HB;
   CK(ctx->batch.ensure(2 * 128 * 24));
-  CK(ctx->psi.ensure(16 * 256 * 24));
+  CK(ctx->psi.ensure(2 * 16 * 256 * 24));
   CK(ctx->soa.ensure(6 * nsmall * 8));
   CK(ctx->wbuf.ensure(2 * xmax * 24 + 48));
   CK(ctx->rbuf.ensure((xmax > 2 ? xmax : 2) * 128 * 16));
@@ -688,10 +688,12 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   int launches = HB > 1 ? HB - 1 : 0;
   std::vector<f162> coords, rounds;
   int cur = 0;
+  f162* PSI[2] = {ctx->psi.as<f162>(), ctx->psi.as<f162>() + 16 * 256};  // byte tables of Phi_r, Phi_r+1
+  launch_psi_tables(G[0], PSI[0], st);
+  ++launches;
   for (int r = 0; r < HB; ++r) {
     const uint64_t X = 1ull << r;
-    launch_psi_tables(G[cur], ctx->psi.as<f162>(), st);
-    launch_switch_round_blocks(R[HB - 1 - r], X, hi[r], ctx->psi.as<f162>(), W[cur],
+    launch_switch_round_blocks(R[HB - 1 - r], X, hi[r], PSI[cur], W[cur],
                                ctx->msg.as<unsigned long long>(), ctx->msg_out_dev, ctx->sms, st);
     f162 m[2];
     CK(cudaStreamSynchronize(st));
@@ -701,26 +703,28 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
     rounds.push_back(m[0]);
     rounds.push_back(m[1]);
     coords.push_back(rr);
-    launch_g_update(ctx->psi.as<f162>(), hi[r], rr, G[cur ^ 1], st);
-    launch_w_update(W[cur], X, rr, W[cur ^ 1], st);
+    launch_round_update(PSI[cur], hi[r], rr, PSI[cur ^ 1], W[cur], X, W[cur ^ 1], st);
     cur ^= 1;
-    launches += 4;
+    launches += 2;
   }
   CKL("switch rounds on blocks");
   cudaEventRecord(ctx->ev[14], st);
   uint64_t* sb = ctx->soa.as<uint64_t>();
   Soa A = {sb, sb + nsmall, sb + 2 * nsmall}, P = {sb + 3 * nsmall, sb + 4 * nsmall, sb + 5 * nsmall};
-  launch_psi_tables(G[cur], ctx->psi.as<f162>(), st);
-  launch_phi_apply(ctx->elo.as<b128>(), nsmall, ctx->psi.as<f162>(), A, st);
+  launch_phi_apply(ctx->elo.as<b128>(), nsmall, PSI[cur], A, st);
   CK(cudaMemsetAsync(P.w0, 0, 3 * nsmall * 8, st));
   launch_materialize(table, W[cur], xmax, P, st);
-  launches += 3;
+  launches += 2;
   CKL("switch materialisation");
   cudaEventRecord(ctx->ev[15], st);
-  uint64_t half = nsmall;
-  for (int r = HB; r < sh.lp; ++r) {
-    half >>= 1;
+  // The last rounds on the 4096 entries: each launch folds a round and computes the next
+  // round's message (the last fold alone).
+  uint64_t half = nsmall >> 1;
+  if (HB < sh.lp) {
     launch_switch_msg(A, P, half, ctx->msg.as<unsigned long long>(), ctx->msg_out_dev, ctx->sms, st);
+    ++launches;
+  }
+  for (int r = HB; r < sh.lp; ++r, half >>= 1) {
     f162 m[2];
     CK(cudaStreamSynchronize(st));
     memcpy(m, ctx->msg_out, 48);
@@ -729,8 +733,11 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
     rounds.push_back(m[0]);
     rounds.push_back(m[1]);
     coords.push_back(rr);
-    launch_switch_fold(A, P, half, rr, ctx->sms, st);
-    launches += 2;
+    if (r + 1 < sh.lp)
+      launch_switch_fold_msg(A, P, half, rr, ctx->msg.as<unsigned long long>(), ctx->msg_out_dev, ctx->sms, st);
+    else
+      launch_switch_fold(A, P, half, rr, ctx->sms, st);
+    ++launches;
   }
   CKL("switch rounds");
   f162 opened;

@@ -132,14 +132,18 @@ void launch_rblock_level(const b128* in, uint64_t nout, b128 rho, b128* out, cud
 // memory).
 void launch_switch_round_blocks(const b128* R, uint64_t X, b128 rho, const f162* phi, const f162* w,
                                 unsigned long long* msg, unsigned long long* out, int sms, cudaStream_t s);
-// G_{r+1} from the round's byte tables of Phi_r (launch_psi_tables of G_r).
-void launch_g_update(const f162* psi, b128 rho, f162 rp, f162* Gn, cudaStream_t s);
-void launch_w_update(const f162* w, uint64_t X, f162 rp, f162* wn, cudaStream_t s);
+// After block round r: psi_next = the byte tables of Phi_{r+1} (from those of Phi_r, rho = r_hi[r],
+// the challenge rp) and wn = the weights w_{r+1} of the 2X entries (from w_r).
+void launch_round_update(const f162* psi, b128 rho, f162 rp, f162* psi_next, const f162* w, uint64_t X, f162* wn,
+                         cudaStream_t s);
 void launch_phi_apply(const b128* e, uint64_t n, const f162* phi, Soa a, cudaStream_t s);
 void launch_materialize(const uint4* table, const f162* w, uint64_t X, Soa p, cudaStream_t s);
 void launch_switch_msg(Soa a, Soa p, uint64_t half, unsigned long long* msg, unsigned long long* out, int sms,
                        cudaStream_t s);
 void launch_switch_fold(Soa a, Soa p, uint64_t half, f162 r, int sms, cudaStream_t s);
+// The fold of a round (half pairs) and the message of the next (half / 2 pairs) in one launch.
+void launch_switch_fold_msg(Soa a, Soa p, uint64_t half, f162 r, unsigned long long* msg, unsigned long long* out,
+                            int sms, cudaStream_t s);
 
 // ---- launch wrappers (lf_open.cu) ----
 void launch_row_eval(const uint4* table, int rl, const f162* eqt, f162* row, cudaStream_t s);

@@ -278,6 +278,59 @@ __global__ void __launch_bounds__(256) k_switch_fold(Soa a, Soa p, uint64_t half
   }
 }
 
+// The fold of a round and the message of the next in one pass. Four lanes per pair j < half / 2
+// of the next round: lane q folds entry j (q = 0, 2) or j + half / 2 (q = 1, 3) of a (q < 2) or
+// p (q >= 2), reading it and its partner half entries up, which no other lane touches, and writes
+// it back; the four values then meet by shuffles and lanes 0 and 1 add the pair's terms of the
+// next message (sumcheck.rs:128-245).
+__global__ void __launch_bounds__(256) k_switch_fold_msg(Soa a, Soa p, uint64_t half, f162 r,
+                                                         unsigned long long* __restrict__ msg,
+                                                         unsigned long long* __restrict__ out) {
+  const uint64_t h2 = half >> 1;
+  const int q = threadIdx.x & 3, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const Soa& x = q < 2 ? a : p;
+  f162 e0 = {0, 0, 0}, ei = {0, 0, 0};
+  // every lane of a warp runs the same number of iterations (the shuffles below are warp-wide)
+  const uint64_t stride = (uint64_t)gridDim.x * (blockDim.x >> 2);
+  const uint64_t j0 = blockIdx.x * (uint64_t)(blockDim.x >> 2) + (threadIdx.x >> 2);
+  for (uint64_t jb = j0 - (threadIdx.x >> 2) % 8; jb < h2; jb += stride) {
+    const uint64_t j = jb + (threadIdx.x >> 2) % 8;
+    const bool live = j < h2;
+    f162 v = {0, 0, 0};
+    if (live) {
+      const uint64_t i = j + (q & 1) * h2;
+      const f162 x0 = x.get(i);
+      v = f162_add(x0, f162_mul(r, f162_add(x0, x.get(i + half))));
+      x.put(i, v);
+    }
+    const int base = lane & ~3;
+    f162 a0, a1, p0, p1;
+    a0.w0 = __shfl_sync(0xffffffffu, v.w0, base), a0.w1 = __shfl_sync(0xffffffffu, v.w1, base),
+    a0.w2 = __shfl_sync(0xffffffffu, v.w2, base);
+    a1.w0 = __shfl_sync(0xffffffffu, v.w0, base + 1), a1.w1 = __shfl_sync(0xffffffffu, v.w1, base + 1),
+    a1.w2 = __shfl_sync(0xffffffffu, v.w2, base + 1);
+    p0.w0 = __shfl_sync(0xffffffffu, v.w0, base + 2), p0.w1 = __shfl_sync(0xffffffffu, v.w1, base + 2),
+    p0.w2 = __shfl_sync(0xffffffffu, v.w2, base + 2);
+    p1.w0 = __shfl_sync(0xffffffffu, v.w0, base + 3), p1.w1 = __shfl_sync(0xffffffffu, v.w1, base + 3),
+    p1.w2 = __shfl_sync(0xffffffffu, v.w2, base + 3);
+    if (live && q == 0) e0 = f162_add(e0, f162_mul(a0, p0));
+    if (live && q == 1) ei = f162_add(ei, f162_mul(f162_add(a0, a1), f162_add(p0, p1)));
+  }
+  for (int m = 16; m; m >>= 1) e0 = shfl_xor_f162(e0, m), ei = shfl_xor_f162(ei, m);
+  __shared__ f162 part[2][8];
+  if (lane == 0) part[0][warp] = e0, part[1][warp] = ei;
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    f162 s = {0, 0, 0};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s = f162_add(s, part[threadIdx.x][w]);
+    unsigned long long* o = msg + 3 * threadIdx.x;
+    atomicXor(o, (unsigned long long)s.w0);
+    atomicXor(o + 1, (unsigned long long)s.w1);
+    atomicXor(o + 2, (unsigned long long)s.w2);
+  }
+  msg_forward(msg, out);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Switch from the partials' blocks (rounds r < HB = LP - 12).
 //
@@ -398,25 +451,39 @@ __global__ void __launch_bounds__(128) k_switch_round_blocks(const b128* __restr
   msg_forward(msg, out);
 }
 
-// G_{r+1}[b] = Phi_r(y1) + r' (Phi_r(y1) + Phi_r(y2)), y1 = (1 + rho) X^b, y2 = rho X^b.
-// Phi_r is applied through the round's byte tables (psi, already built for the round's message),
-// and rho X^b is a shift: no GHASH product and no 128-term loop per output.
-__global__ void k_g_update(const f162* __restrict__ psi, b128 rho, f162 rp, f162* __restrict__ Gn) {
-  const int b = threadIdx.x;
-  const b128 xb = {b < 64 ? 1ull << b : 0, b >= 64 ? 1ull << (b - 64) : 0};
-  const b128 y2 = b128_shl(rho, b);
-  const b128 y1 = b128_add(xb, y2);
-  const f162 p1 = phi_apply(psi, y1), p2 = phi_apply(psi, y2);
-  Gn[b] = f162_add(p1, f162_mul(rp, f162_add(p1, p2)));
-}
-
-// w_{r+1}[2x] = (1 + r') w_r[x], w_{r+1}[2x + 1] = r' w_r[x]
-__global__ void k_w_update(const f162* __restrict__ w, uint64_t X, f162 rp, f162* __restrict__ wn) {
-  uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (x >= X) return;
-  const f162 t = f162_mul(w[x], rp);
-  wn[2 * x] = f162_add(w[x], t);
-  wn[2 * x + 1] = t;
+// After a block round: the next round's byte tables and weights in one launch.
+// Blocks c < 16: G_{r+1}[b] = Phi_r(y1) + r' (Phi_r(y1) + Phi_r(y2)), y1 = (1 + rho) X^b, y2 = rho X^b,
+// for the block's b = 8c .. 8c + 7 (Phi_r through the round's byte tables psi, rho X^b a shift:
+// no GHASH product), then table c of psi_next from them. Blocks c >= 16: the weights
+// w_{r+1}[2x] = (1 + r') w_r[x], w_{r+1}[2x + 1] = r' w_r[x].
+__global__ void __launch_bounds__(256) k_round_update(const f162* __restrict__ psi, b128 rho, f162 rp,
+                                                      f162* __restrict__ psi_next, const f162* __restrict__ w,
+                                                      uint64_t X, f162* __restrict__ wn) {
+  if (blockIdx.x >= 16) {
+    const uint64_t x = (blockIdx.x - 16) * (uint64_t)blockDim.x + threadIdx.x;
+    if (x >= X) return;
+    const f162 t = f162_mul(w[x], rp);
+    wn[2 * x] = f162_add(w[x], t);
+    wn[2 * x + 1] = t;
+    return;
+  }
+  __shared__ f162 gb[8];
+  const int c = blockIdx.x;
+  if (threadIdx.x < 8) {
+    const int b = 8 * c + threadIdx.x;
+    const b128 xb = {b < 64 ? 1ull << b : 0, b >= 64 ? 1ull << (b - 64) : 0};
+    const b128 y2 = b128_shl(rho, b);
+    const b128 y1 = b128_add(xb, y2);
+    const f162 p1 = phi_apply(psi, y1), p2 = phi_apply(psi, y2);
+    gb[threadIdx.x] = f162_add(p1, f162_mul(rp, f162_add(p1, p2)));
+  }
+  __syncthreads();
+  const int m = threadIdx.x;
+  f162 v = {0, 0, 0};
+#pragma unroll
+  for (int b = 0; b < 8; ++b)
+    if ((m >> b) & 1) v = f162_add(v, gb[b]);
+  psi_next[256 * c + m] = v;
 }
 
 // a[j] = Phi(E_lo[j]) for the 4096 low entries.
@@ -475,11 +542,9 @@ void launch_switch_round_blocks(const b128* R, uint64_t X, b128 rho, const f162*
   unsigned g = (unsigned)(X < 2ull * sms ? X : 2ull * sms);  // two blocks per SM (98 KB tables each)
   k_switch_round_blocks<<<g, 128, smem, s>>>(R, X, rho, phi, w, msg, out);
 }
-void launch_g_update(const f162* psi, b128 rho, f162 rp, f162* Gn, cudaStream_t s) {
-  k_g_update<<<1, 128, 0, s>>>(psi, rho, rp, Gn);
-}
-void launch_w_update(const f162* w, uint64_t X, f162 rp, f162* wn, cudaStream_t s) {
-  k_w_update<<<(unsigned)((X + 127) / 128), 128, 0, s>>>(w, X, rp, wn);
+void launch_round_update(const f162* psi, b128 rho, f162 rp, f162* psi_next, const f162* w, uint64_t X, f162* wn,
+                         cudaStream_t s) {
+  k_round_update<<<(unsigned)(16 + (X + 255) / 256), 256, 0, s>>>(psi, rho, rp, psi_next, w, X, wn);
 }
 void launch_phi_apply(const b128* e, uint64_t n, const f162* phi, Soa a, cudaStream_t s) {
   const int smem = 16 * 256 * 24;
@@ -521,6 +586,10 @@ void launch_psi_tables(const f162* batch, f162* tab, cudaStream_t s) { k_psi_tab
 void launch_switch_msg(Soa a, Soa p, uint64_t half, unsigned long long* msg, unsigned long long* out, int sms,
                        cudaStream_t s) {
   k_switch_msg<<<grid_for(half, 256, sms * 8), 256, 0, s>>>(a, p, half, msg, out);
+}
+void launch_switch_fold_msg(Soa a, Soa p, uint64_t half, f162 r, unsigned long long* msg, unsigned long long* out,
+                            int sms, cudaStream_t s) {
+  k_switch_fold_msg<<<grid_for(2 * half, 256, sms * 8), 256, 0, s>>>(a, p, half, r, msg, out);  // 4 lanes a pair
 }
 void launch_switch_fold(Soa a, Soa p, uint64_t half, f162 r, int sms, cudaStream_t s) {
   k_switch_fold<<<grid_for(half, 256, sms * 8), 256, 0, s>>>(a, p, half, r);
