@@ -713,7 +713,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   Soa A = {sb, sb + nsmall, sb + 2 * nsmall}, P = {sb + 3 * nsmall, sb + 4 * nsmall, sb + 5 * nsmall};
   launch_phi_apply(ctx->elo.as<b128>(), nsmall, PSI[cur], A, st);
   CK(cudaMemsetAsync(P.w0, 0, 3 * nsmall * 8, st));
-  launch_materialize(table, W[cur], xmax, P, st);
+  launch_materialize(table, W[cur], xmax, P, ctx->sms, st);
   launches += 2;
   CKL("switch materialisation");
   cudaEventRecord(ctx->ev[15], st);
@@ -755,7 +755,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   CK(ctx->row.ensure(COLUMNS * 24));
   CK(cudaMemcpyAsync(ctx->p0.p, p0.data(), 24 * p0.size(), cudaMemcpyHostToDevice, st));
   launch_eq_table_f162(ctx->p0.as<f162>(), sh.rl, ctx->eqt.as<f162>(), st);
-  launch_row_eval(table, sh.rl, ctx->eqt.as<f162>(), ctx->row.as<f162>(), st);
+  launch_row_eval(table, sh.rl, ctx->eqt.as<f162>(), ctx->row.as<f162>(), ctx->sms, st);
   CKL("row evaluation");
   std::vector<f162> row(COLUMNS);
   CK(cudaMemcpyAsync(row.data(), ctx->row.p, COLUMNS * 24, cudaMemcpyDeviceToHost, st));

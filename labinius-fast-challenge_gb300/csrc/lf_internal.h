@@ -137,7 +137,7 @@ void launch_switch_round_blocks(const b128* R, uint64_t X, b128 rho, const f162*
 void launch_round_update(const f162* psi, b128 rho, f162 rp, f162* psi_next, const f162* w, uint64_t X, f162* wn,
                          cudaStream_t s);
 void launch_phi_apply(const b128* e, uint64_t n, const f162* phi, Soa a, cudaStream_t s);
-void launch_materialize(const uint4* table, const f162* w, uint64_t X, Soa p, cudaStream_t s);
+void launch_materialize(const uint4* table, const f162* w, uint64_t X, Soa p, int sms, cudaStream_t s);
 void launch_switch_msg(Soa a, Soa p, uint64_t half, unsigned long long* msg, unsigned long long* out, int sms,
                        cudaStream_t s);
 void launch_switch_fold(Soa a, Soa p, uint64_t half, f162 r, int sms, cudaStream_t s);
@@ -146,7 +146,7 @@ void launch_switch_fold_msg(Soa a, Soa p, uint64_t half, f162 r, unsigned long l
                             int sms, cudaStream_t s);
 
 // ---- launch wrappers (lf_open.cu) ----
-void launch_row_eval(const uint4* table, int rl, const f162* eqt, f162* row, cudaStream_t s);
+void launch_row_eval(const uint4* table, int rl, const f162* eqt, f162* row, int sms, cudaStream_t s);
 struct HasherImage;  // a bk::Hasher copied to the device
 // PHASE[162][88] as f64 re, f64 im, f32 re, f32 im, one after the other.
 constexpr size_t PHASE_TABLE_BYTES = 162 * 88 * (8 + 8 + 4 + 4);

@@ -1,5 +1,6 @@
 // The opening on the GPU: row evaluation, folding challenges, the fold, and the BLAKE3 tree
 // hashing of the transcript's large absorb.
+#include <algorithm>
 #include <cstdio>
 
 #include "lf_blake3.cuh"
@@ -20,16 +21,15 @@ __device__ __forceinline__ f162 shfl_xor_f162(f162 v, int m) {
   return v;
 }
 
-// One block per run of RW_SHARE rows i, all columns (RW_COLS per thread): the window table of
+// One block per run of `share` rows i, all columns (RW_COLS per thread): the window table of
 // eq[i] serves the 1024 products of row i; each thread reads its columns' words in order of i.
 // row (1024 F162) is zeroed by the caller and receives the blocks' shares by XOR.
 constexpr int RW_COLS = COLUMNS / 256;
-constexpr uint64_t RW_SHARE = 32;
-__global__ void __launch_bounds__(256) k_row_eval(const uint4* __restrict__ table, int rl, const f162* __restrict__ eqt,
-                                                  f162* __restrict__ row) {
+__global__ void __launch_bounds__(256) k_row_eval(const uint4* __restrict__ table, int rl, uint64_t share,
+                                                  const f162* __restrict__ eqt, f162* __restrict__ row) {
   __shared__ WinTable T;
   const uint64_t n = 1ull << rl;
-  const uint64_t i0 = blockIdx.x * RW_SHARE, i1 = min(n, i0 + RW_SHARE);
+  const uint64_t i0 = blockIdx.x * share, i1 = min(n, i0 + share);
   f162 acc[RW_COLS];
 #pragma unroll
   for (int k = 0; k < RW_COLS; ++k) acc[k] = {0, 0, 0};
@@ -51,10 +51,12 @@ __global__ void __launch_bounds__(256) k_row_eval(const uint4* __restrict__ tabl
   }
 }
 
-void launch_row_eval(const uint4* table, int rl, const f162* eqt, f162* row, cudaStream_t s) {
+void launch_row_eval(const uint4* table, int rl, const f162* eqt, f162* row, int sms, cudaStream_t s) {
+  // one wave: the runs of rows split over the blocks resident at once (three per SM)
   const uint64_t n = 1ull << rl;
+  const uint64_t share = std::max<uint64_t>(1, (n + 3ull * sms - 1) / (3ull * sms));
   cudaMemsetAsync(row, 0, COLUMNS * sizeof(f162), s);
-  k_row_eval<<<(unsigned)((n + RW_SHARE - 1) / RW_SHARE), 256, 0, s>>>(table, rl, eqt, row);
+  k_row_eval<<<(unsigned)((n + share - 1) / share), 256, 0, s>>>(table, rl, share, eqt, row);
 }
 
 // ---------------------------------------------------------------------------------------------

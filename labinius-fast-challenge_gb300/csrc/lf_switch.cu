@@ -10,6 +10,7 @@
 // So the table pass is a 128 x 4096 by 4096 x 128 bit-matrix product per block of 4096 words,
 // done with AND/XOR on 32-bit planes and a final parity, and only 128 * 2^(LP-12) GHASH products
 // remain.
+#include <algorithm>
 #include <cstdio>
 
 #include "lf_internal.h"
@@ -552,10 +553,13 @@ void launch_phi_apply(const b128* e, uint64_t n, const f162* phi, Soa a, cudaStr
   smem_limit(k_phi_apply, smem, attr);
   k_phi_apply<<<16, 256, smem, s>>>(e, n, phi, a);
 }
-void launch_materialize(const uint4* table, const f162* w, uint64_t X, Soa p, cudaStream_t s) {
-  uint64_t shares = X >= 64 ? 64 : X;
-  uint64_t x_share = (X + shares - 1) / shares;
-  k_materialize<<<dim3(4096 / (256 * MW_J), (unsigned)shares), 256, 0, s>>>(table, w, X, x_share, p);
+void launch_materialize(const uint4* table, const f162* w, uint64_t X, Soa p, int sms, cudaStream_t s) {
+  // one wave: 8 j tiles x shares = the blocks resident at once (five per SM)
+  const uint64_t tiles = 4096 / (256 * MW_J);
+  uint64_t shares = std::max<uint64_t>(1, std::min<uint64_t>(X, 5ull * sms / tiles));
+  const uint64_t x_share = (X + shares - 1) / shares;
+  shares = (X + x_share - 1) / x_share;
+  k_materialize<<<dim3((unsigned)tiles, (unsigned)shares), 256, 0, s>>>(table, w, X, x_share, p);
 }
 static unsigned grid_for(uint64_t n, int threads, unsigned cap) {
   uint64_t g = (n + threads - 1) / threads;
