@@ -93,6 +93,18 @@ def test_page_locked_table_streams_into_the_commitment(prover, oracle, log_vars)
         assert got == oracle.prove(seed, oracle.write_table(seed, log_vars), log_vars)
 
 
+@pytest.mark.parametrize("q", [(1 << 64) - 59, (1 << 96) - 17], ids=["2^64-59", "2^96-17"])
+def test_page_locked_table_streams_under_other_moduli(prover, oracle, q):
+    # the exact-lift commitment (more transform primes, hence more blocks per element range)
+    # reading a table that is still arriving
+    torch = pytest.importorskip("torch")
+    log_vars, seed = 22, SEEDS[2]
+    table = oracle.write_table(seed, log_vars)
+    host = torch.empty(len(table), dtype=torch.uint8, pin_memory=True)
+    host.numpy()[:] = bytearray(table)
+    assert prover.prove(seed, host.numpy(), log_vars, q=q) == oracle.prove(seed, table, log_vars, q=q)
+
+
 def test_repeatable(prover, oracle):
     log_vars = 20
     seed = SEEDS[1]
