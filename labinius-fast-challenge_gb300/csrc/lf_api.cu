@@ -301,7 +301,8 @@ struct lf_ctx {
 
 namespace {
 
-constexpr int TABLE_PARTS = 16;  // parts of a page-locked host table (lf_prove)
+constexpr int TABLE_PARTS = 16;       // parts of a page-locked host table (lf_prove)
+constexpr int TABLE_FIRST_PARTS = 2;  // queued before the commitment's launch
 
 int fail(lf_ctx* c, int code, const std::string& msg) {
   if (c) {
@@ -581,14 +582,38 @@ struct TableStream {
   uint32_t epoch;
   int part_elems;
   cudaEvent_t done;
+  const uint8_t* host;  // the page-locked table
+  size_t pitch;         // bytes of one column
+  uint64_t elements;    // ring elements per column
+  int next;             // parts not yet queued: [next, TABLE_PARTS)
 };
+
+// Queues parts [ts->next, end) of a streamed table on the copy stream, each followed by its ready
+// flag; once every part is queued, `done` (and the upload's end) is recorded after them.
+int enqueue_table_parts(lf_ctx* ctx, TableStream* ts, int end) {
+  for (int i = ts->next; i < end; ++i) {
+    const uint64_t m0 = (uint64_t)i * ts->part_elems, m1 = std::min<uint64_t>(ts->elements, m0 + ts->part_elems);
+    if (m0 < m1)
+      CK(cudaMemcpy2DAsync(ctx->table.as<uint8_t>() + 64 * m0, ts->pitch, ts->host + 64 * m0, ts->pitch, 64 * (m1 - m0),
+                           COLUMNS, cudaMemcpyHostToDevice, ctx->upload_stream));
+    if (ctx->write_value(reinterpret_cast<CUstream>(ctx->upload_stream), reinterpret_cast<CUdeviceptr>(ctx->ready + i),
+                         ts->epoch, CU_STREAM_WRITE_VALUE_DEFAULT) != CUDA_SUCCESS)
+      return fail(ctx, LF_E_CUDA, "stream write of a table part's ready flag failed");
+  }
+  if (end > ts->next) ts->next = end;
+  if (ts->next >= TABLE_PARTS) {
+    CK(cudaEventRecord(ctx->uploaded[0], ctx->upload_stream));
+    CK(cudaEventRecord(ctx->up_t1, ctx->upload_stream));
+  }
+  return LF_OK;
+}
 
 // table_ready / proof_ready (may be null): events the prover's stream waits for before the first
 // kernel that reads the table and before the first device write into `proof`. With ts, the
 // commitment starts before the table is complete (table_ready is then unused).
 int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, const uint4* table, uint8_t* proof,
                  size_t* proof_len, cudaEvent_t table_ready = nullptr, cudaEvent_t proof_ready = nullptr,
-                 const TableStream* ts = nullptr) {
+                 TableStream* ts = nullptr) {
   cudaStream_t st = ctx->stream;
   const size_t width = coefficient_bytes(q);
   const size_t commit_bytes = width * COLUMNS * RING_N;
@@ -622,6 +647,8 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
     launch_commit(mp, sh, table, ctx->key->key.as<uint32_t>(), ctx->key->btiles.as<uint16_t>(),
                   ctx->partial.as<uint32_t>(), splits, ctx->status.as<int>(), st, 0, -1, ts->ready, ts->epoch,
                   ts->part_elems);
+    // the parts after the first few are queued only now, off the commitment's critical path
+    if ((rc = enqueue_table_parts(ctx, ts, TABLE_PARTS))) return rc;
     CK(cudaStreamWaitEvent(st, ts->done, 0));  // every later kernel reads the whole table
   } else {
     if (table_ready) CK(cudaStreamWaitEvent(st, table_ready, 0));
@@ -864,8 +891,10 @@ double ms_between(clk::time_point a, clk::time_point b) { return std::chrono::du
 // Starts the copy of a host table into ctx->table on ctx's copy stream. A page-locked table goes up
 // in TABLE_PARTS element ranges of every column (one 2-D copy each), each followed by a stream
 // write of the proof's epoch into its ready flag, and *ts describes them (streamed = true): the
-// commitment reads a range as soon as it has arrived. Any other table goes up in one copy whose
-// completion is ctx->uploaded[0].
+// commitment reads a range as soon as it has arrived. The first TABLE_FIRST_PARTS are queued here,
+// the rest by prove_device right after it launches the commitment (so the host's queueing of them
+// does not delay that launch). Any other table goes up in one copy whose completion is
+// ctx->uploaded[0].
 int start_table_upload(lf_ctx* ctx, const void* table, size_t table_bytes, const Shape& sh, TableStream* ts,
                        bool* streamed) {
   int rc = side_streams(ctx);
@@ -879,20 +908,11 @@ int start_table_upload(lf_ctx* ctx, const void* table, size_t table_bytes, const
   if (*streamed) {
     const uint32_t epoch = ++ctx->epoch == 0 ? ++ctx->epoch : ctx->epoch;  // never 0, the flags' initial value
     const int part_elems = (int)((sh.ring_elements + TABLE_PARTS - 1) / TABLE_PARTS);
-    const size_t pitch = (size_t)16 << sh.rl;  // one column
-    for (int i = 0; i < TABLE_PARTS; ++i) {
-      const uint64_t m0 = (uint64_t)i * part_elems, m1 = std::min<uint64_t>(sh.ring_elements, m0 + part_elems);
-      if (m0 >= m1) break;
-      CK(cudaMemcpy2DAsync(ctx->table.as<uint8_t>() + 64 * m0, pitch, static_cast<const uint8_t*>(table) + 64 * m0,
-                           pitch, 64 * (m1 - m0), COLUMNS, cudaMemcpyHostToDevice, ctx->upload_stream));
-      if (ctx->write_value(reinterpret_cast<CUstream>(ctx->upload_stream), reinterpret_cast<CUdeviceptr>(ctx->ready + i),
-                         epoch, CU_STREAM_WRITE_VALUE_DEFAULT) != CUDA_SUCCESS)
-        return fail(ctx, LF_E_CUDA, "stream write of a table part's ready flag failed");
-    }
-    *ts = TableStream{ctx->ready, epoch, part_elems, ctx->uploaded[0]};
-  } else {
-    CK(cudaMemcpyAsync(ctx->table.p, table, table_bytes, cudaMemcpyHostToDevice, ctx->upload_stream));
+    *ts = TableStream{ctx->ready, epoch, part_elems, ctx->uploaded[0], static_cast<const uint8_t*>(table),
+                      (size_t)16 << sh.rl, sh.ring_elements, 0};
+    return enqueue_table_parts(ctx, ts, TABLE_FIRST_PARTS);  // the rest after the commitment's launch
   }
+  CK(cudaMemcpyAsync(ctx->table.p, table, table_bytes, cudaMemcpyHostToDevice, ctx->upload_stream));
   CK(cudaEventRecord(ctx->uploaded[0], ctx->upload_stream));
   CK(cudaEventRecord(ctx->up_t1, ctx->upload_stream));
   return LF_OK;
@@ -916,6 +936,7 @@ int run_job(lf_ctx* ctx, const lf_job& j, size_t* proof_len) {
   if ((rc = start_table_upload(ctx, j.table, j.table_bytes, sh, &ts, &streamed))) return rc;
   rc = prove_device(ctx, j.seed, q, sh, ctx->table.as<uint4>(), j.proof, proof_len, ctx->uploaded[0], nullptr,
                     streamed ? &ts : nullptr);
+  if (streamed && ts.next < TABLE_PARTS) enqueue_table_parts(ctx, &ts, TABLE_PARTS);  // (an early failure)
   cudaStreamSynchronize(ctx->upload_stream);  // (a proof that failed early may not have waited for it)
   return rc;
 }
@@ -1547,6 +1568,7 @@ int lf_prove(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32
   cudaGetLastError();  // cudaPointerGetAttributes on plain host memory leaves no error behind
   rc = prove_device(ctx, seed, q, sh, ctx->table.as<uint4>(), proof, proof_len, ctx->uploaded[0], proof_ready,
                     streamed ? &tstream : nullptr);
+  if (streamed && tstream.next < TABLE_PARTS) enqueue_table_parts(ctx, &tstream, TABLE_PARTS);  // (an early failure)
   // (a proof that failed early may not have waited for the side streams)
   cudaStreamSynchronize(ctx->upload_stream);
   cudaStreamSynchronize(ctx->touch_stream);
