@@ -76,6 +76,9 @@ int lf_key_prepare(lf_ctx* ctx, const uint8_t q_le[16], uint32_t log_vars);
 
 /* One proof of the table (host memory, table_bytes = 2^log_vars / 8, little-endian u128 words as
  * the table file holds them) for seed and modulus q. Writes *proof_len bytes into proof.
+ * A page-locked table is copied in element ranges that the commitment starts on as they arrive;
+ * any other host memory (a mapped file included) is copied whole first. The table must stay
+ * unchanged until the call returns.
  * Replaces prove() + Output::write (solution/proof_generate/src/main.rs:1692-2009, 1650-1689). */
 int lf_prove(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars, const void* table,
              size_t table_bytes, uint8_t* proof, size_t proof_cap, size_t* proof_len);
