@@ -207,7 +207,8 @@ int lf_sample_challenges_traced(lf_ctx* ctx, const char* domain, const uint8_t* 
  * in the reference (its sampler runs on the host, challenge.rs:707-737); it exists for callers
  * that must not allocate on the device. Output as lf_sample_challenges. Limits: 1 <= n <=
  * LF_NOALLOC_MAX_CHALLENGES, larger n returns LF_E_LIMIT before any device work; device < 64.
- * Scratch is one fixed device array per device (about 390 KB), shared by all calls: calls are
+ * Scratch is one fixed device array per device (just under 512 KB: the 342,144 bytes of phase
+ * tables, 40 bytes per challenge slot and the transcript state), shared by all calls: calls are
  * serialised by a process-wide lock and return after `stream` (a cudaStream_t; NULL = the
  * legacy default stream) has drained. The first call on a device locates that array and
  * uploads the phase tables with synchronous copies; make it before any stream of the device
@@ -215,6 +216,25 @@ int lf_sample_challenges_traced(lf_ctx* ctx, const char* domain, const uint8_t* 
 #define LF_NOALLOC_MAX_CHALLENGES 4096
 int lf_sample_challenges_noalloc(int device, const char* domain, const uint8_t* prefix, size_t prefix_len, uint32_t n,
                                  uint8_t* out, void* stream);
+/* Test hooks. No counterpart in the reference: they let tests reach paths that seeded inputs
+ * reach with negligible probability. Each changes the NEXT proof of this context (lf_prove,
+ * lf_prove_device, or a job of lf_prove_batch / lf_submit run on the context itself), once.
+ *
+ * lf_test_set_point: that proof takes r_hi (n = LOG_VARS - 7 GHASH elements, 16 bytes little-endian
+ * each) as the packed coordinates of its evaluation point instead of sampling them ("r-hi",
+ * verifier/proof_verify/src/main.rs:177-182). Its transcript then no longer matches the checker's,
+ * but every later field of the proof is a deterministic function of that point, so it can be
+ * compared with another prover given the same point, e.g. one with a coordinate equal to one,
+ * where solution/proof_generate/src/main.rs:1929-1962 switches to its generic prover. n = 0 clears
+ * a pending point. LF_E_ARGS from the proof if n does not match its shape.
+ *
+ * lf_test_withhold_table_part: if that proof streams a page-locked table (lf_prove), the ready flag
+ * of element range `part` (0..15) is not written, and the commitment kernel gives up waiting for it
+ * after wait_cycles SM cycles (0 = its default of about a second): the proof returns LF_E_INTERNAL
+ * and the context stays usable. */
+int lf_test_set_point(lf_ctx* ctx, const uint8_t* r_hi, uint32_t n);
+int lf_test_withhold_table_part(lf_ctx* ctx, int part, uint64_t wait_cycles);
+
 const char* lf_strerror(int code);
 const char* lf_last_error(lf_ctx* ctx);
 

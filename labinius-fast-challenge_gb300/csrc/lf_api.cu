@@ -276,6 +276,10 @@ struct lf_ctx {
   // at once and each block waits for the part it reads.
   uint32_t* ready = nullptr;  // device, TABLE_PARTS flags
   uint32_t epoch = 0;
+  // Test hooks (lf_test_set_point, lf_test_withhold_table_part), used by the next proof only.
+  std::vector<b128> test_hi;          // r_hi to use instead of the sampled one (empty: none)
+  int test_withhold = -1;             // a streamed table part whose ready flag is not written
+  long long test_ready_wait = 0;      // SM cycles the commitment waits for a part (0: its default)
   CUresult (*write_value)(CUstream, CUdeviceptr, cuuint32_t, unsigned int) = nullptr;
   // serving: FIFO of submitted jobs, drained by one worker thread per lane
   struct Queued {
@@ -586,6 +590,8 @@ struct TableStream {
   size_t pitch;         // bytes of one column
   uint64_t elements;    // ring elements per column
   int next;             // parts not yet queued: [next, TABLE_PARTS)
+  int withhold;         // a part whose flag is left unset (test hook), else -1
+  long long wait;       // SM cycles the commitment waits for a part (0: its default)
 };
 
 // Queues parts [ts->next, end) of a streamed table on the copy stream, each followed by its ready
@@ -596,6 +602,7 @@ int enqueue_table_parts(lf_ctx* ctx, TableStream* ts, int end) {
     if (m0 < m1)
       CK(cudaMemcpy2DAsync(ctx->table.as<uint8_t>() + 64 * m0, ts->pitch, ts->host + 64 * m0, ts->pitch, 64 * (m1 - m0),
                            COLUMNS, cudaMemcpyHostToDevice, ctx->upload_stream));
+    if (i == ts->withhold) continue;  // a test hook: the commitment's wait for this part runs out
     if (ctx->write_value(reinterpret_cast<CUstream>(ctx->upload_stream), reinterpret_cast<CUdeviceptr>(ctx->ready + i),
                          ts->epoch, CU_STREAM_WRITE_VALUE_DEFAULT) != CUDA_SUCCESS)
       return fail(ctx, LF_E_CUDA, "stream write of a table part's ready flag failed");
@@ -646,7 +653,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   if (ts) {
     launch_commit(mp, sh, table, ctx->key->key.as<uint32_t>(), ctx->key->btiles.as<uint16_t>(),
                   ctx->partial.as<uint32_t>(), splits, ctx->status.as<int>(), st, 0, -1, ts->ready, ts->epoch,
-                  ts->part_elems);
+                  ts->part_elems, ts->wait);
     // the parts after the first few are queued only now, off the commitment's critical path
     if ((rc = enqueue_table_parts(ctx, ts, TABLE_PARTS))) return rc;
     CK(cudaStreamWaitEvent(st, ts->done, 0));  // every later kernel reads the whole table
@@ -670,6 +677,11 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   // ---- point and partials (main.rs:177-189; crossfield.rs:548-573) ----
   std::vector<b128> lo = t.sample_b128("r-lo", 7);
   std::vector<b128> hi = t.sample_b128("r-hi", sh.lp);
+  if (!ctx->test_hi.empty()) {  // lf_test_set_point: this proof runs at the given coordinates
+    if (ctx->test_hi.size() != hi.size()) return fail(ctx, LF_E_ARGS, "test point has the wrong number of coordinates");
+    hi.swap(ctx->test_hi);
+    ctx->test_hi.clear();
+  }
   const int HB = sh.lp - 12;
   std::vector<b128> partials;
   if ((rc = device_partials(ctx, table, sh, hi, partials))) return rc;
@@ -801,8 +813,8 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   CK(cudaMemcpyAsync(ctx->hasher.p, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, st));
   // status[0] was zeroed before the commitment: 3 = commitment pipeline timeout, 1 = sampling
   // bound, 2 = fold range.
-  launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.p,
-                    ctx->chal.as<Challenge>(), COLUMNS, ctx->status.as<int>(), st);
+  CK(launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.p, ctx->chal.as<Challenge>(), COLUMNS,
+                       ctx->status.as<int>(), st));
   t.counter += COLUMNS;
   CKL("challenges");
   cudaEventRecord(ctx->ev[8], st);
@@ -909,7 +921,7 @@ int start_table_upload(lf_ctx* ctx, const void* table, size_t table_bytes, const
     const uint32_t epoch = ++ctx->epoch == 0 ? ++ctx->epoch : ctx->epoch;  // never 0, the flags' initial value
     const int part_elems = (int)((sh.ring_elements + TABLE_PARTS - 1) / TABLE_PARTS);
     *ts = TableStream{ctx->ready, epoch, part_elems, ctx->uploaded[0], static_cast<const uint8_t*>(table),
-                      (size_t)16 << sh.rl, sh.ring_elements, 0};
+                      (size_t)16 << sh.rl, sh.ring_elements, 0, ctx->test_withhold, ctx->test_ready_wait};
     return enqueue_table_parts(ctx, ts, TABLE_FIRST_PARTS);  // the rest after the commitment's launch
   }
   CK(cudaMemcpyAsync(ctx->table.p, table, table_bytes, cudaMemcpyHostToDevice, ctx->upload_stream));
@@ -934,6 +946,8 @@ int run_job(lf_ctx* ctx, const lf_job& j, size_t* proof_len) {
   TableStream ts{};
   bool streamed = false;
   if ((rc = start_table_upload(ctx, j.table, j.table_bytes, sh, &ts, &streamed))) return rc;
+  ctx->test_withhold = -1;  // the test hooks apply to one proof
+  ctx->test_ready_wait = 0;
   rc = prove_device(ctx, j.seed, q, sh, ctx->table.as<uint4>(), j.proof, proof_len, ctx->uploaded[0], nullptr,
                     streamed ? &ts : nullptr);
   if (streamed && ts.next < TABLE_PARTS) enqueue_table_parts(ctx, &ts, TABLE_PARTS);  // (an early failure)
@@ -1225,8 +1239,8 @@ int verify_device(lf_ctx* ctx, const uint8_t seed[32], const Shape& sh, const ui
   CK(ctx->eqt.ensure(sh.column_len * 24));
   CK(cudaMemcpyAsync(ctx->hasher.p, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(ctx->status.p, 0, 16, st));
-  launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.p,
-                    ctx->chal.as<Challenge>(), COLUMNS, ctx->status.as<int>(), st);
+  CK(launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.p, ctx->chal.as<Challenge>(), COLUMNS,
+                       ctx->status.as<int>(), st));
   t.counter += COLUMNS;
   CK(cudaMemcpyAsync(ctx->p0.p, p0.data(), 24 * p0.size(), cudaMemcpyHostToDevice, st));
   launch_eq_table_f162(ctx->p0.as<f162>(), sh.rl, ctx->eqt.as<f162>(), st);
@@ -1338,6 +1352,7 @@ __global__ void k_table_prg(bk::Pending root, uint64_t blocks, uint4* out) {
 // returns only after its stream has drained; work on other streams never touches the array.
 // ---------------------------------------------------------------------------------------------
 constexpr uint32_t NOALLOC_MAX_CHALLENGES = 4096;
+static_assert(NOALLOC_MAX_CHALLENGES == LF_NOALLOC_MAX_CHALLENGES, "the header's limit is the array's");
 constexpr int NOALLOC_MAX_DEVICES = 64;
 
 struct NoAllocScratch {
@@ -1348,6 +1363,7 @@ struct NoAllocScratch {
 };
 
 static __device__ __align__(256) uint8_t g_noalloc_scratch[sizeof(NoAllocScratch)];
+static_assert(sizeof(NoAllocScratch) < 512 * 1024, "the header states the array as under 512 KB");
 
 struct NoAllocDevice {
   bool ready = false;
@@ -1379,16 +1395,16 @@ int noalloc_sample(NoAllocDevice& d, const char* domain, const uint8_t* prefix, 
   t.absorb_bytes(prefix, prefix_len);
   NoAllocScratch* sc = d.scratch;
   int status[4] = {0, 0, 0, 0};
-  if (cudaMemcpyAsync(&sc->hasher, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-      cudaMemsetAsync(sc->status, 0, sizeof(sc->status), st) != cudaSuccess)
-    return LF_E_CUDA;
-  launch_challenges(&sc->hasher, t.counter, d.sign_key, sc->phase, sc->chal, (int)n, sc->status,
-                    st);
-  if (cudaGetLastError() != cudaSuccess) return LF_E_CUDA;
-  if (cudaMemcpyAsync(out, sc->chal, (size_t)n * sizeof(Challenge), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaMemcpyAsync(status, sc->status, sizeof(status), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess)
-    return LF_E_CUDA;
+  // From the first enqueue on, every return waits for the stream: the array is shared, and the
+  // next call (on any stream) must not overwrite it while this one's copies or kernel still run.
+  bool ok = cudaMemcpyAsync(&sc->hasher, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+            cudaMemsetAsync(sc->status, 0, sizeof(sc->status), st) == cudaSuccess &&
+            launch_challenges(&sc->hasher, t.counter, d.sign_key, sc->phase, sc->chal, (int)n, sc->status, st) ==
+                cudaSuccess &&
+            cudaMemcpyAsync(out, sc->chal, (size_t)n * sizeof(Challenge), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+            cudaMemcpyAsync(status, sc->status, sizeof(status), cudaMemcpyDeviceToHost, st) == cudaSuccess;
+  ok = cudaStreamSynchronize(st) == cudaSuccess && ok;
+  if (!ok) return LF_E_CUDA;
   return status[0] ? LF_E_INTERNAL : LF_OK;
 }
 
@@ -1556,6 +1572,8 @@ int lf_prove(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32
   TableStream tstream{};
   bool streamed = false;
   if ((rc = start_table_upload(ctx, table, table_bytes, sh, &tstream, &streamed))) return rc;
+  ctx->test_withhold = -1;  // the test hooks apply to one proof
+  ctx->test_ready_wait = 0;
   cudaEvent_t proof_ready = nullptr;
   cudaPointerAttributes pa{};
   if (ctx->pageable_access && cudaPointerGetAttributes(&pa, proof) == cudaSuccess &&
@@ -1644,13 +1662,14 @@ int lf_sample_challenges_traced(lf_ctx* ctx, const char* domain, const uint8_t* 
   CK(cudaMemsetAsync(ctx->scratch_small.p, 0, 64 * 4, ctx->stream));
   CK(cudaMemcpyAsync(ctx->hasher.p, &t.h, sizeof(bk::Hasher), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemsetAsync(ctx->status.p, 0, 16, ctx->stream));
-  launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.p,
-                    ctx->chal.as<Challenge>(), (int)n, ctx->status.as<int>(), ctx->stream,
-                    trace64 ? ctx->scratch_small.as<uint32_t>() : nullptr);
-  CKL("challenges");
+  CK(launch_challenges(ctx->hasher.p, t.counter, ctx->sign_key, ctx->phase.p, ctx->chal.as<Challenge>(), (int)n,
+                       ctx->status.as<int>(), ctx->stream, trace64 ? ctx->scratch_small.as<uint32_t>() : nullptr));
+  int status[4] = {0, 0, 0, 0};
   CK(cudaMemcpyAsync(out, ctx->chal.p, n * sizeof(Challenge), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(status, ctx->status.p, sizeof(status), cudaMemcpyDeviceToHost, ctx->stream));
   if (trace64) CK(cudaMemcpyAsync(trace64, ctx->scratch_small.p, 64 * 4, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  if (status[0]) return fail(ctx, LF_E_INTERNAL, "challenge sampling exceeded its attempt bound");
   return LF_OK;
 }
 
@@ -1994,6 +2013,22 @@ int lf_verify(lf_ctx* ctx, const uint8_t seed[32], uint32_t log_vars, const void
 int lf_last_profile(lf_ctx* ctx, lf_profile* out) {
   if (!ctx || !out) return LF_E_ARGS;
   *out = ctx->prof;
+  return LF_OK;
+}
+
+int lf_test_set_point(lf_ctx* ctx, const uint8_t* r_hi, uint32_t n) {
+  if (!ctx || (!r_hi && n)) return LF_E_ARGS;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ctx->test_hi.assign(n, b128{0, 0});
+  if (n) memcpy(ctx->test_hi.data(), r_hi, 16 * (size_t)n);
+  return LF_OK;
+}
+
+int lf_test_withhold_table_part(lf_ctx* ctx, int part, uint64_t wait_cycles) {
+  if (!ctx || part < 0 || part >= TABLE_PARTS) return LF_E_ARGS;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ctx->test_withhold = part;
+  ctx->test_ready_wait = (long long)std::min<uint64_t>(wait_cycles, (uint64_t)1 << 40);
   return LF_OK;
 }
 

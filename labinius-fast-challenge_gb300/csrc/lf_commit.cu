@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     k_commit_tc(const uint4* __restrict__ table, const uint32_t* __restrict__ key, const uint4* __restrict__ btiles,
                 const PrimeConst* __restrict__ pcs, uint32_t* __restrict__ partial, int rl, int elements,
                 int per_split, int nprimes, int split_base, int* status, const uint32_t* ready, uint32_t epoch,
-                int part_elems) {
+                int part_elems, long long ready_wait) {
   extern __shared__ __align__(1024) uint8_t tsm[];
   uint8_t* sB = tsm;
   int* sKey = reinterpret_cast<int*>(tsm + TC_B_BYTES);                            // [4][TC_KEY_INTS]
@@ -634,7 +634,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int part = (m_begin + e) / part_elems;
         const long long t0 = clock64();
         while ((int)(ld_acquire_u32(ready + part) - epoch) < 0) {
-          if (*abort_flag || *reinterpret_cast<volatile int*>(status) || clock64() - t0 > TC_WAIT_CYCLES) {
+          if (*abort_flag || *reinterpret_cast<volatile int*>(status) || clock64() - t0 > ready_wait) {
             if (!*abort_flag) {
               *abort_flag = 1;
               atomicExch(status, 3);
@@ -857,7 +857,7 @@ int commit_splits(uint64_t elements, int nprimes, int sms) {
 
 void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint32_t* key,
                    const uint16_t* btiles, uint32_t* partial, int splits, int* status, cudaStream_t s, int split_begin,
-                   int split_end, const uint32_t* ready, uint32_t epoch, int part_elems) {
+                   int split_end, const uint32_t* ready, uint32_t epoch, int part_elems, long long ready_wait) {
   const int elements = (int)sh.ring_elements;
   const int per = (elements + splits - 1) / splits;
   if (split_end < 0) split_end = splits;
@@ -867,7 +867,8 @@ void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, c
   dim3 grid(mp.nprimes * 3, COLUMNS / TC_COLS, split_end - split_begin);
   k_commit_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(table, key, reinterpret_cast<const uint4*>(btiles), mp.dconsts, partial,
                                                  sh.rl, elements, per, mp.nprimes, split_begin, status, ready, epoch,
-                                                 part_elems > 0 ? part_elems : elements);
+                                                 part_elems > 0 ? part_elems : elements,
+                                                 ready_wait > 0 ? ready_wait : TC_WAIT_CYCLES);
 }
 
 // Element range [m0, m1) of split range [s0, s1): the part of every column those splits read.

@@ -150,8 +150,10 @@ void launch_row_eval(const uint4* table, int rl, const f162* eqt, f162* row, int
 struct HasherImage;  // a bk::Hasher copied to the device
 // PHASE[162][88] as f64 re, f64 im, f32 re, f32 im, one after the other.
 constexpr size_t PHASE_TABLE_BYTES = 162 * 88 * (8 + 8 + 4 + 4);
-void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint32_t sign_key[8], const void* phase,
-                       Challenge* out, int n, int* status, cudaStream_t s, uint32_t* dbg = nullptr);
+// Returns the launch's own status (cudaLaunchKernel), not the thread's last error.
+cudaError_t launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint32_t sign_key[8],
+                              const void* phase, Challenge* out, int n, int* status, cudaStream_t s,
+                              uint32_t* dbg = nullptr);
 int fold_splits(uint64_t ring_elements, int sms);
 constexpr size_t FOLD_STRIP_BYTES = 53 * 128;  // per column
 void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Challenge* ch, uint8_t* strips,
@@ -180,11 +182,12 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
 int commit_splits(uint64_t elements, int nprimes, int sms);
 // Splits [split_begin, split_end) of the `splits` element splits (split_end < 0: all of them).
 // ready (device, may be null): the table is still being copied in parts of part_elems ring
-// elements (of every column); part i may be read once ready[i] - epoch >= 0 (as int32).
+// elements (of every column); part i may be read once ready[i] - epoch >= 0 (as int32), and a
+// block gives up waiting for it after ready_wait SM cycles (0: about a second), setting *status = 3.
 void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, const uint32_t* key,
                    const uint16_t* btiles, uint32_t* partial, int splits, int* status, cudaStream_t s,
                    int split_begin = 0, int split_end = -1, const uint32_t* ready = nullptr, uint32_t epoch = 0,
-                   int part_elems = 0);
+                   int part_elems = 0, long long ready_wait = 0);
 void commit_split_elements(uint64_t elements, int splits, int s0, int s1, uint64_t& m0, uint64_t& m1);
 void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t* partial, int splits, uint8_t* out,
                           cudaStream_t s, int ncols = COLUMNS);

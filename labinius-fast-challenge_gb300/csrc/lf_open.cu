@@ -235,8 +235,8 @@ __global__ void __launch_bounds__(32 * CH_WARPS) k_challenges(const bk::Hasher* 
   if (lane == 0) atomicExch(status, 1);
 }
 
-void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint32_t sign_key[8], const void* phase,
-                       Challenge* out, int n, int* status, cudaStream_t s, uint32_t* dbg) {
+cudaError_t launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint32_t sign_key[8],
+                              const void* phase, Challenge* out, int n, int* status, cudaStream_t s, uint32_t* dbg) {
   const size_t np = 162 * PHASE_LANES;
   const double* phase_re = static_cast<const double*>(phase);
   const double* phase_im = phase_re + np;
@@ -248,10 +248,13 @@ void launch_challenges(const void* hasher_dev, uint64_t base_counter, const uint
   sk.t = 0;
   sk.len = 0;
   sk.flags = bk::F_DERIVE_MAT | bk::F_CHUNK_START | bk::F_CHUNK_END;
-  const double bound_sq = 12.0 * 12.0 + 1e-12;
-  k_challenges<<<(n + CH_WARPS - 1) / CH_WARPS, 32 * CH_WARPS, 0, s>>>(
-      reinterpret_cast<const bk::Hasher*>(hasher_dev), base_counter, sk, phase_re, phase_im, re32, im32, bound_sq, out, n,
-      status, dbg);
+  double bound_sq = 12.0 * 12.0 + 1e-12;
+  // cudaLaunchKernel reports this launch's own outcome (a triple-chevron launch leaves it in the
+  // thread's last-error state, where an earlier error of the caller's may also wait).
+  const bk::Hasher* h = reinterpret_cast<const bk::Hasher*>(hasher_dev);
+  void* args[] = {&h, &base_counter, &sk, &phase_re, &phase_im, &re32, &im32, &bound_sq, &out, &n, &status, &dbg};
+  return cudaLaunchKernel(reinterpret_cast<const void*>(k_challenges), dim3((n + CH_WARPS - 1) / CH_WARPS),
+                          dim3(32 * CH_WARPS), args, 0, s);
 }
 
 // ---------------------------------------------------------------------------------------------

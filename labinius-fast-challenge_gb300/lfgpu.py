@@ -30,7 +30,7 @@ EXPORTS = [
     "lf_last_profile", "lf_strerror", "lf_last_error", "lf_last_challenges",
     "lf_sample_challenges", "lf_sample_challenges_noalloc", "lf_prove_batch", "lf_submit", "lf_poll",
     "lf_verify", "lf_verify_device", "lf_request_footprint", "lf_ring_mul", "lf_ghash_mul", "lf_ajtai_matrix_device",
-    "lf_a_times_v", "lf_tune",
+    "lf_a_times_v", "lf_tune", "lf_test_set_point", "lf_test_withhold_table_part",
 ]
 
 
@@ -119,6 +119,8 @@ def load(path=LIB_PATH):
     lib.lf_a_times_v.argtypes = [p, ctypes.c_char_p, ctypes.c_uint64, p, u8p]
     lib.lf_sample_challenges_noalloc.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p, sz, ctypes.c_uint32,
                                                  u8p, p]
+    lib.lf_test_set_point.argtypes = [p, ctypes.c_char_p, ctypes.c_uint32]
+    lib.lf_test_withhold_table_part.argtypes = [p, ctypes.c_int, ctypes.c_uint64]
     _lib = lib
     return lib
 
@@ -335,6 +337,17 @@ class Prover:
         buf = (ctypes.c_uint8 * (40 * 1024))()
         self._check(self.lib.lf_last_challenges(self.ctx, buf, 40 * 1024))
         return _parse_challenges(bytes(buf), 1024)
+
+    def test_set_point(self, r_hi):
+        """Test hook: the next proof uses r_hi (a list of 16-byte GHASH elements, or ints) as its
+        packed point coordinates instead of sampling them."""
+        raw = b"".join(x if isinstance(x, (bytes, bytearray)) else int(x).to_bytes(16, "little") for x in r_hi)
+        self._check(self.lib.lf_test_set_point(self.ctx, raw, len(raw) // 16))
+
+    def test_withhold_table_part(self, part, wait_cycles=0):
+        """Test hook: the next streamed table upload leaves `part`'s ready flag unset; the commitment
+        gives up after wait_cycles SM cycles and the proof returns LF_E_INTERNAL."""
+        self._check(self.lib.lf_test_withhold_table_part(self.ctx, part, wait_cycles))
 
     def profile(self):
         p = Profile()

@@ -1277,9 +1277,11 @@ int lfo_commit(const uint8_t q_le[16], uint32_t log_vars, const uint8_t* table, 
   return LFO_OK;
 }
 
-// reference.rs:137-177 (prove)
-int lfo_prove(const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars, const uint8_t* table_bytes,
-              int commit_mode, uint8_t* proof_out, size_t cap, size_t* len, uint8_t* trace, size_t trace_cap) {
+// reference.rs:137-177 (prove). r_hi_at, when not NULL, replaces the sampled packed coordinates
+// (lfo_prove_at_point); the transcript still draws them, so every later sample is the same.
+static int prove_impl(const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars, const uint8_t* table_bytes,
+                      int commit_mode, uint8_t* proof_out, size_t cap, size_t* len, uint8_t* trace, size_t trace_cap,
+                      const uint8_t* r_hi_at) {
   Shape s;
   if (!s.set(log_vars)) return LFO_E_SHAPE;
   u128 q = q_from_le(q_le);
@@ -1310,6 +1312,7 @@ int lfo_prove(const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars,
   Transcript t = transcript(seed, s, q, pr.commitment);
   std::vector<B128> lo = t.sample_b128("r-lo", 7);
   std::vector<B128> hi = t.sample_b128("r-hi", s.lp);
+  if (r_hi_at) memcpy(hi.data(), r_hi_at, 16 * (size_t)s.lp);
   tw.b128(lo), tw.b128(hi);
   std::vector<B128> eq(s.words);
   eq_expand_b128_par(hi.data(), s.lp, eq.data());
@@ -1389,6 +1392,17 @@ int lfo_prove(const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars,
   memcpy(proof_out, bytes.data(), need);
   if (trace && !tw.ok) return LFO_E_CAP;
   return LFO_OK;
+}
+
+int lfo_prove(const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars, const uint8_t* table_bytes,
+              int commit_mode, uint8_t* proof_out, size_t cap, size_t* len, uint8_t* trace, size_t trace_cap) {
+  return prove_impl(seed, q_le, log_vars, table_bytes, commit_mode, proof_out, cap, len, trace, trace_cap, nullptr);
+}
+
+int lfo_prove_at_point(const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars, const uint8_t* table_bytes,
+                       const uint8_t* r_hi, uint8_t* proof_out, size_t cap, size_t* len) {
+  if (!r_hi) return LFO_E_ARGS;
+  return prove_impl(seed, q_le, log_vars, table_bytes, 1, proof_out, cap, len, nullptr, 0, r_hi);
 }
 
 // main.rs:293-409 (check_proof_shape, verify, check_field_switch, check_opening)

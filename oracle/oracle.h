@@ -42,6 +42,11 @@ int lfo_commit(const uint8_t q_le[16], uint32_t log_vars, const uint8_t* table, 
 // The reference prover. `trace`, when not NULL, receives the intermediate values (see oracle.cc).
 int lfo_prove(const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars, const uint8_t* table,
               int commit_mode, uint8_t* proof, size_t cap, size_t* len, uint8_t* trace, size_t trace_cap);
+// The same proof with the packed point coordinates r_hi (LOG_VARS - 7 GHASH elements, 16 bytes LE
+// each) in place of the sampled ones: the generic switch (crossfield.rs:600-634) at any point,
+// including coordinates equal to one (solution/proof_generate/src/main.rs:1929-1962).
+int lfo_prove_at_point(const uint8_t seed[32], const uint8_t q_le[16], uint32_t log_vars, const uint8_t* table,
+                       const uint8_t* r_hi, uint8_t* proof, size_t cap, size_t* len);
 // The checker, shape-parameterised. table == NULL regenerates the table from the seed.
 // Returns LFO_OK or LFO_E_REJECT with a message in err.
 int lfo_verify(const uint8_t seed[32], uint32_t log_vars, const uint8_t* table, const uint8_t* proof,

@@ -41,6 +41,8 @@ def load():
     lib.lfo_commit.argtypes = [c8, ctypes.c_uint32, c8, ctypes.c_int, u8p]
     lib.lfo_prove.argtypes = [c8, c8, ctypes.c_uint32, c8, ctypes.c_int, u8p, ctypes.c_size_t,
                               ctypes.POINTER(ctypes.c_size_t), u8p, ctypes.c_size_t]
+    lib.lfo_prove_at_point.argtypes = [c8, c8, ctypes.c_uint32, c8, c8, u8p, ctypes.c_size_t,
+                                       ctypes.POINTER(ctypes.c_size_t)]
     lib.lfo_verify.argtypes = [c8, ctypes.c_uint32, c8, c8, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t]
     lib.lfo_accept_modulus.argtypes = [c8, ctypes.c_uint32]
     lib.lfo_fold_cap.argtypes = [ctypes.c_uint32]
@@ -179,6 +181,20 @@ def prove(seed, table, log_vars, q=BASELINE_Q, commit_mode=1, trace=False):
     if trace:
         return proof, bytes(tb[:tcap])
     return proof
+
+
+def prove_at_point(seed, table, log_vars, r_hi, q=BASELINE_Q):
+    """The proof with the packed point coordinates r_hi (list of 16-byte elements or ints) in place of
+    the sampled ones."""
+    raw = b"".join(x if isinstance(x, (bytes, bytearray)) else int(x).to_bytes(16, "little") for x in r_hi)
+    assert len(raw) == 16 * (log_vars - 7)
+    cap = proof_size(q, log_vars)
+    out = _buf(cap)
+    n = ctypes.c_size_t()
+    rc = load().lfo_prove_at_point(bytes(seed), qb(q), log_vars, bytes(table), raw, out, cap, ctypes.byref(n))
+    if rc != 0:
+        raise ValueError(f"oracle prove failed {rc}")
+    return bytes(out[: n.value])
 
 
 def verify(seed, proof, log_vars, table=None):

@@ -66,3 +66,9 @@ def test_noalloc_sampler_limits_checked_on_the_host(gpu_lib):
     assert lib.lf_sample_challenges_noalloc(64, b"d", b"", 0, 1, buf, None) == -1
     assert lib.lf_sample_challenges_noalloc(0, None, b"", 0, 1, buf, None) == -1
     assert b"4096" in lib.lf_strerror(-10)
+
+
+def test_test_hooks_check_their_arguments(gpu_lib):
+    lib = gpu_lib.load()
+    assert lib.lf_test_set_point(None, b"", 0) == -1
+    assert lib.lf_test_withhold_table_part(None, 0, 0) == -1

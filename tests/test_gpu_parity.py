@@ -1,9 +1,13 @@
 """GPU prover vs the CPU oracle: byte-identical proofs on the same (seed, table, Q), and the
 oracle's checker accepting the GPU proof (verifier/proof_verify/src/main.rs:402-409).
 
-Small shapes are compared byte for byte; the 2^31-bit instance through verifier acceptance and
-field-by-field comparison with the oracle's own proof."""
+Every shape is compared byte for byte, the full 2^31-bit instance included (the oracle proves it
+on all host cores in about half a minute), through the library and through the drop-in
+`labinius-fast` executable. Edge tables, the reference's moduli and degenerate points are in
+test_gpu_edges.py."""
 import hashlib
+import os
+import subprocess
 
 import pytest
 
@@ -70,11 +74,12 @@ def test_device_table_writer_matches_oracle(prover, oracle):
         prover.free(dev)
 
 
-@pytest.mark.parametrize("log_vars", [22, 27, 31])
+@pytest.mark.parametrize("log_vars", [23, 27, 31])
 def test_page_locked_table_streams_into_the_commitment(prover, oracle, log_vars):
     # lf_prove from page-locked host memory copies the table in 16 element ranges while the
-    # commitment already runs, each block waiting for its range: the proof is the one of the same
-    # table proven from device memory (and, at 2^22 bits, the oracle's).
+    # commitment already runs, each block waiting for its range (tables of at least 16 ring
+    # elements per column: 2^23 bits and up): the proof is the one of the same table proven from
+    # device memory (and, at 2^23 bits, the oracle's).
     torch = pytest.importorskip("torch")
     seed = SEEDS[0]
     n = (1 << log_vars) // 8
@@ -89,7 +94,7 @@ def test_page_locked_table_streams_into_the_commitment(prover, oracle, log_vars)
     for _ in range(2):  # the second run finds the ready flags set by the first, under a new epoch
         got = prover.prove(seed, host.numpy(), log_vars)
         assert got == bytes(proof_dev[:n_dev])
-    if log_vars == 22:
+    if log_vars == 23:
         assert got == oracle.prove(seed, oracle.write_table(seed, log_vars), log_vars)
 
 
@@ -98,7 +103,7 @@ def test_page_locked_table_streams_under_other_moduli(prover, oracle, q):
     # the exact-lift commitment (more transform primes, hence more blocks per element range)
     # reading a table that is still arriving
     torch = pytest.importorskip("torch")
-    log_vars, seed = 22, SEEDS[2]
+    log_vars, seed = 23, SEEDS[2]
     table = oracle.write_table(seed, log_vars)
     host = torch.empty(len(table), dtype=torch.uint8, pin_memory=True)
     host.numpy()[:] = bytearray(table)
@@ -143,3 +148,64 @@ def test_tuned_split_count_keeps_the_proof(gpu_lib, oracle):
         finally:
             p.free(dev)
     assert got == oracle.prove(seed, table, log_vars)
+
+
+def test_full_instance_matches_oracle(prover, oracle):
+    # The challenge's own instance: 2^31 bits, baseline Q. The table is written on the device by
+    # the table PRG, proven from device memory, and the oracle proves the same bytes on the host.
+    log_vars, seed = 31, SEEDS[2]
+    n = (1 << log_vars) // 8
+    dev = prover.alloc(n)
+    try:
+        prover.write_table_device(seed, log_vars, dev)
+        proof, plen = prover.prove_device(seed, dev, log_vars)
+        got = bytes(proof[:plen])
+    finally:
+        prover.free(dev)
+    assert plen == 13_958_612
+    table = oracle.write_table(seed, log_vars)
+    want = oracle.prove(seed, table, log_vars)
+    assert got == want, f"fields differ: {_first_diff(got, want, log_vars, oracle)}"
+    ok, msg = oracle.verify(seed, got, log_vars, table)
+    assert ok, msg
+
+
+@pytest.mark.parametrize("modulus", [None, 35_039_150_080, 55_144_219_393, (1 << 96) - 17],
+                         ids=["default", "x86-default", "recorded-run", "2^96-17"])
+@pytest.mark.parametrize("log_vars", [20, 22])
+def test_cli_proof_file_matches_oracle(gpu_lib, oracle, tmp_path, log_vars, modulus):
+    # The drop-in boundary (solution/proof_generate/src/main.rs:2050-2090): the table file, the
+    # seed in LABINIUS_SEED, the proof file; without --modulus the proof is made (and carries) the
+    # baseline Q 3889 * 9721 * 17497.
+    seed = hashlib.sha256(b"lf-test/cli").digest()
+    table = oracle.write_table(seed, log_vars)
+    tpath, ppath = tmp_path / "witness-table.bin", tmp_path / "proof.bin"
+    tpath.write_bytes(table)
+    args = [gpu_lib.CLI_PATH, "--prove", str(ppath), "--table", str(tpath), "--log-vars", str(log_vars)]
+    if modulus is not None:
+        args += ["--modulus", str(modulus)]
+    env = dict(os.environ, LABINIUS_SEED=seed.hex())
+    r = subprocess.run(args, env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "labinius-gb300" in r.stderr  # the phase line
+    got = ppath.read_bytes()
+    q = modulus if modulus is not None else 3889 * 9721 * 17497
+    assert got == oracle.prove(seed, table, log_vars, q=q)
+    assert oracle.verify(seed, got, log_vars, table)[0]
+
+
+def test_cli_rejects_bad_inputs(gpu_lib, oracle, tmp_path):
+    # any failure exits nonzero and leaves no proof file (main.rs:2056-2069, 391-392)
+    seed = bytes(range(32))
+    tpath, ppath = tmp_path / "t.bin", tmp_path / "p.bin"
+    tpath.write_bytes(oracle.write_table(seed, 20)[:-16])
+    env = dict(os.environ, LABINIUS_SEED=seed.hex())
+    base = [gpu_lib.CLI_PATH, "--prove", str(ppath), "--table", str(tpath), "--log-vars", "20"]
+    r = subprocess.run(base, env=env, capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0 and "wrong length" in r.stderr
+    tpath.write_bytes(oracle.write_table(seed, 20))
+    r = subprocess.run(base + ["--modulus", "34816965048"], env=env, capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0 and "modulus" in r.stderr
+    r = subprocess.run(base, env=dict(os.environ, LABINIUS_SEED="zz" * 32), capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0
+    assert not ppath.exists()

@@ -160,3 +160,20 @@ def test_other_moduli(oracle):
 
 def test_full_size_layout(oracle):
     assert oracle.proof_size(Q, 31) == 13_958_612
+
+
+def test_prove_at_the_sampled_point_is_the_proof(oracle):
+    # lfo_prove_at_point only replaces the sampled r_hi: at the sampled coordinates (read from the
+    # prover's trace, after the 7 r_lo elements) it is the proof itself, and any other point
+    # changes the switch and every field after it, not the commitment or the partials' point.
+    log_vars = 20
+    seed = bytes([9] * 32)
+    table = oracle.write_table(seed, log_vars)
+    proof, trace = oracle.prove(seed, table, log_vars, trace=True)
+    lp = log_vars - 7
+    hi = [trace[112 + 16 * i:112 + 16 * (i + 1)] for i in range(lp)]
+    assert oracle.prove_at_point(seed, table, log_vars, hi) == proof
+    other = oracle.prove_at_point(seed, table, log_vars, [1] * lp)
+    a, b = oracle.parse_proof(proof, log_vars), oracle.parse_proof(other, log_vars)
+    assert a["commitment"] == b["commitment"]
+    assert a["rounds"] != b["rounds"] and a["folded"] != b["folded"]
