@@ -33,8 +33,10 @@ constexpr int TC_K = 256;                            // MMA K: 128 bits x 2 limb
 constexpr int TC_THREADS = 32 * 32;                  // 24 epilogue, 4 producer and 4 issuer warps
 constexpr int TC_B_BYTES = TC_N * TC_K * 2;          // 32 KB
 constexpr int TC_KEY_INTS = TC_LEAVES * 16;          // one element's key rows for the block's leaves
-constexpr int TC_SMEM =
+constexpr int TC_SMEM0 =
     TC_B_BYTES + 4 * TC_KEY_INTS * 4 + 3 * TC_COLS * 64 + 3 * TC_KEY_INTS * 4 + 4 * TC_LEAVES * 16 + 16 * 8 + 16;
+constexpr int TC_CONST_AT = (TC_SMEM0 + 127) / 128 * 128;  // A (128 x 16) and B (64 x 16) of the init MMA
+constexpr int TC_SMEM = TC_CONST_AT + 4096 + 2048;
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;   // ~1 s at 2 GHz
 
 static void fill_btiles(const PrimePlan& pl, const PrimeConst& c, uint16_t* out);
@@ -109,8 +111,8 @@ static void fill_consts(const PrimePlan& pl, PrimeConst& c) {
   c.w5 = (uint32_t)pw(405);
   c.inv_split = inv_mod((c.w + p - c.w5) % p, p);
   {
-    // |r| <= (p - 1) / 2 + 1, |key| <= (p - 1) / 2, 4 products per element; stay inside int32
-    const uint64_t h = (p - 1) / 2, per = 4 * (h + 1) * h;
+    // |r| <= (p - 1) / 2 + 3, |key| <= (p - 1) / 2, 4 products per element; stay inside int32
+    const uint64_t h = (p - 1) / 2, per = 4 * (h + 4) * h;
     uint64_t r = (0x7fffffffull - p) / per;
     c.reduce_every = (uint32_t)(r < 1 ? 1 : r);
   }
@@ -485,10 +487,15 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
 //   A (M = 128 table columns x 128 bits) holds each set bit as a power of two a_kappa (bf16 with
 //   one exponent bit, see commit_expand_word) and is read twice;
 //   B (N = 64 x K = 256) holds per leaf (V mod 256) / a against the first reading and
-//   (V >> 8) * 256 / a against the second (both exact in bf16), so the f32 accumulator is
-//   sum_j bit_j V[s][j] < 2^22, an exact integer.
-// The epilogue reduces that sum mod p in f32 (every intermediate is an integer below 2^24), then
-// does the 4x4 base multiplication with the key on the integer pipe.
+//   (V >> 8) * 256 / a against the second (both exact in bf16), so the product adds
+//   L = sum_j bit_j V[s][j] < 2^22, an exact integer.
+// One more MMA per word (A and B constant tiles in shared memory) first sets every accumulator
+// to k p, the least multiple of p at or above 2^23, so D = k p + L is an integer in [2^23, 2^24)
+// (exact in f32 throughout: every partial sum is a nonnegative integer below 2^24) and its bit
+// pattern is 0x4A800000 + D. The epilogue then reduces with one FFMA and one IMAD:
+// bits(D * (1/p) + 1.5 * 2^23 - k) = 0x4B400000 + rint(L / p), and bits(D) - p * that = r + OFF
+// (mod 2^32) with |r| <= p/2 + 3 and OFF a per-prime constant, and does the 4x4 base
+// multiplication with the key on the integer pipe.
 //
 // Block = one prime x one third of its 162 leaves (54) x 128 table columns x an element range.
 // Tensor memory (512 columns) holds four word stages k = 0..3 (the four words of an element):
@@ -502,8 +509,11 @@ void launch_key_transform(const ModulusPlan& mp, uint64_t elements, const uint32
 //     the previous D of stage k), issues the word's 16 MMAs (A from TMEM, B = the leaf tile in
 //     shared memory) from lane 0 and commits them to done[k]. A thread issues a small MMA only
 //     every 50-70 cycles, so each stage has its own issuer and no issuer does other work;
-//   warps 0-23 (epilogue; warp w reads TMEM lanes 32 (w % 4) .. +31, leaves 9 (w / 4) + i):
+//   warps 0-23 (epilogue; warp w reads TMEM lanes 32 (w % 4) .. +31, leaves 9 (w / 4) + i, whose
+//     D columns are 8 (w / 4) .. + 7 and 48 + w / 4, so two tcgen05.ld per word):
 //     per word wait done[k], load the 9 sums, arrive dfree[k], reduce and accumulate 9 x 4 values.
+// Registers: the block launches with 64 a thread; the issuers give theirs down to 32 and the
+// producers to 48 (setmaxnreg), so each epilogue thread holds its 36 accumulators in 72.
 // So the expansion, the MMAs and the epilogue of different words run at the same time, and no
 // table bits pass through shared memory. Every wait is bounded (about a second); a timeout sets
 // *status = 3 and the abort flag, on which every role leaves its loop; TMEM is released after the
@@ -582,6 +592,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   {
     const uint4* src = btiles + (size_t)blockIdx.x * (TC_B_BYTES / 16);
     for (int i = tid; i < TC_B_BYTES / 16; i += TC_THREADS) reinterpret_cast<uint4*>(sB)[i] = src[i];
+    // the init MMA: A row = (1, 1, 1, 0, ...), B row = the three 8-bit pieces of k p (bf16-exact), so
+    // every D entry starts at k p = the least multiple of p at or above 2^23
+    const uint32_t pp = pcs[pi].p, kp = ((0x800000u + pp - 1) / pp) * pp;
+    const uint16_t one = 0x3F80;
+    const uint16_t pc[3] = {(uint16_t)(__float_as_uint((float)(kp & 0xFF0000u)) >> 16),
+                            (uint16_t)(__float_as_uint((float)(kp & 0xFF00u)) >> 16),
+                            (uint16_t)(__float_as_uint((float)(kp & 0xFFu)) >> 16)};
+    uint16_t* ca = reinterpret_cast<uint16_t*>(tsm + TC_CONST_AT);
+    for (int i = tid; i < (4096 + 2048) / 2; i += TC_THREADS) {
+      uint16_t val = 0;
+      // both tiles: core (row group, k core) at group * 256 + kcore * 128, row r at r * 16, k % 8 at 2 (k % 8)
+      const int off = (i < 2048 ? i : i - 2048) * 2;
+      const int kcore = (off >> 7) & 1, within = off & 127, k = kcore * 8 + ((within & 15) >> 1);
+      if (k < 3) val = i < 2048 ? one : pc[k];
+      ca[i] = val;
+    }
   }
   tc::fence_proxy_async();
   tc::fence_before_sync();
@@ -591,11 +617,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t p = pcs[pi].p;
   int last_e = -1;  // an issuer's last commit
 
+  // Registers: the launch gives 64 a thread (65,536); issuers keep 32, producers 48 and the
+  // 24 epilogue warps take the rest, 72 each (768 x 72 + 128 x 48 + 128 x 32 = 65,536).
   if (warp >= 28) {
     // ---------------- issuer of stage k ----------------
+    tc::regs_dec<32>();
     const int k = warp - 28;
     const uint32_t idesc = tc::idesc_bf16_f32(TC_COLS, TC_N);
     const uint64_t bdesc0 = tc::sdesc(tc::smem_u32(sB), 128, 4096);
+    const uint64_t adesc_c = tc::sdesc(tc::smem_u32(tsm + TC_CONST_AT), 128, 256);
+    const uint64_t bdesc_c = tc::sdesc(tc::smem_u32(tsm + TC_CONST_AT + 4096), 128, 256);
     const uint32_t st = tbase + 128 * k;
     for (int e = 0; e < nelem; ++e) {
       int iok = 1;
@@ -604,9 +635,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               (e == 0 || tc::mbar_wait(&dfree[k], (e - 1) & 1, abort_flag, TC_WAIT_CYCLES));
         if (iok) {
           tc::fence_after_sync();
+          tc::mma_bf16(st + 64, adesc_c, bdesc_c, idesc, 0u);
 #pragma unroll
           for (int kk = 0; kk < TC_K / 16; ++kk)
-            tc::mma_bf16_ta(st + 64, st + 8 * (kk & 7), bdesc0 + (uint64_t)(kk * 16), idesc, kk > 0 ? 1u : 0u);
+            tc::mma_bf16_ta(st + 64, st + 8 * (kk & 7), bdesc0 + (uint64_t)(kk * 16), idesc, 1u);
           tc::mma_commit(&done[k]);
           last_e = e;
         } else if (!*abort_flag) {
@@ -618,6 +650,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   } else if (warp >= 24) {
     // ---------------- producers ----------------
+    tc::regs_dec<48>();
     const int t = tid - 24 * 32;  // table column, TMEM lane
     const uint4* wsrc = table + ((size_t)(col0 + t) << rl);
     const uint4* ksrc = reinterpret_cast<const uint4*>(key) +
@@ -714,16 +747,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     tc::cp_async_wait<0>();
   } else {
     // ---------------- epilogue ----------------
+    tc::regs_inc<72>();
     const uint32_t bar = pcs[pi].bar;
     const int reduce_every = (int)pcs[pi].reduce_every;
     const int g = warp >> 2, qd = warp & 3;
     const int c = 32 * qd + lane;
-    const float pf = (float)p, invp = 1.0f / (float)p;
-    const float MAGIC = 12582912.0f;  // 1.5 * 2^23: adding it rounds to an integer
+    const float invp = 1.0f / (float)p;
     const uint32_t bias = (0x80000000u / p) * p;
-    // acc accumulates key * (0x4B400000 + r) mod 2^32; settling a reduction window subtracts
-    // 0x4B400000 times the window's key sums (kept by the producers), which leaves the exact
-    // sum of key * r (it fits in 32 bits over reduce_every elements), and reduces it mod p.
+    // D = k p + L (an integer in [2^23, 2^24): bits(D) = 0x4A800000 + D); rint(D / p) - k + 1.5 * 2^23
+    // by one FFMA (Cq = 1.5 * 2^23 - k, exact); then bits(D) - p * bits(that) = r + OFF (mod 2^32)
+    const uint32_t kk_ = (0x800000u + p - 1) / p, kp = kk_ * p;
+    const float Cq = (float)(12582912u - kk_);
+    const uint32_t OFF = 0x4A800000u + kp - p * 0x4B400000u;
+    // acc accumulates key * (r + OFF) mod 2^32; settling a reduction window subtracts OFF times
+    // the window's key sums (kept by the producers), which leaves the exact sum of key * r (it
+    // fits in 32 bits over reduce_every elements), and reduces it mod p.
     uint32_t acc[9][4];
 #pragma unroll
     for (int i = 0; i < 9; ++i)
@@ -734,13 +772,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
       for (int i = 0; i < 9; ++i) {
         const uint4 w = cs[i];
-        acc[i][0] = reduce32(acc[i][0] - 0x4B400000u * w.x + bias, bar, p);
-        acc[i][1] = reduce32(acc[i][1] - 0x4B400000u * w.y + bias, bar, p);
-        acc[i][2] = reduce32(acc[i][2] - 0x4B400000u * w.z + bias, bar, p);
-        acc[i][3] = reduce32(acc[i][3] - 0x4B400000u * w.w + bias, bar, p);
+        acc[i][0] = reduce32(acc[i][0] - OFF * w.x + bias, bar, p);
+        acc[i][1] = reduce32(acc[i][1] - OFF * w.y + bias, bar, p);
+        acc[i][2] = reduce32(acc[i][2] - OFF * w.z + bias, bar, p);
+        acc[i][3] = reduce32(acc[i][3] - OFF * w.w + bias, bar, p);
       }
     };
-    const uint32_t tb = tbase + ((uint32_t)(32 * qd) << 16) + 64 + 10 * g;
+    const uint32_t tb = tbase + ((uint32_t)(32 * qd) << 16) + 64 + 8 * g;  // leaves 9 g .. + 7; 9 g + 8 at 48 + g
     int since = 0;
     bool ok = true;
     for (int e = 0; e < nelem && ok; ++e) {
@@ -752,21 +790,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tc::fence_after_sync();
         const uint32_t ta = tb + 128 * k;
         uint32_t v[9];
-        tc::tmem_ld_x2(ta + 0, v[0], v[1]);
-        tc::tmem_ld_x2(ta + 2, v[2], v[3]);
-        tc::tmem_ld_x2(ta + 4, v[4], v[5]);
-        tc::tmem_ld_x2(ta + 6, v[6], v[7]);
-        tc::tmem_ld_x1(ta + 8, v[8]);
+        tc::tmem_ld_x8(ta, v);
+        tc::tmem_ld_x1(ta - 8 * g + 48 + g, v[8]);
         tc::tmem_wait_ld(v);
         tc::fence_before_sync();
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&dfree[k]);
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
-          const float L = __uint_as_float(v[i]);
-          const float q = fmaf(L, invp, MAGIC) - MAGIC;
-          const float r = fmaf(-q, pf, L);
-          const uint32_t ri = __float_as_uint(r + MAGIC);  // 0x4B400000 + r
+          const uint32_t qb = __float_as_uint(fmaf(__uint_as_float(v[i]), invp, Cq));  // 0x4B400000 + q
+          const uint32_t ri = v[i] - p * qb;                                             // r + OFF
           const uint4 kv = reinterpret_cast<const uint4*>(kp)[i * 4 + k];
           acc[i][0] += kv.x * ri;
           acc[i][1] += kv.y * ri;
@@ -804,8 +837,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (warp == 0) tc::tmem_dealloc(tbase, 512);
 }
 
-// B tiles of K1 on the tensor cores, per (prime, third): row 10 g + i = leaf 9 g + i of the third
-// (rows 10 g + 9 and 60..63 zero); K position kappa < 128 carries the low limb of bit j(kappa),
+// B tiles of K1 on the tensor cores, per (prime, third): row 8 g + i = leaf 9 g + i of the third
+// for i < 8, row 48 + g = leaf 9 g + 8 (rows 54..63 zero); K position kappa < 128 carries the low limb of bit j(kappa),
 // kappa >= 128 the high limb of bit j(kappa - 128), j in the K order of tc::write_row; bf16 in
 // the no-swizzle K-major core-matrix layout (8 x 16 B cores, K-adjacent 128 B apart, 8-row
 // groups 4096 B apart).
@@ -816,7 +849,7 @@ static void fill_btiles(const PrimePlan& pl, const PrimeConst& c, uint16_t* out 
     memset(tile, 0, TC_B_BYTES);
     for (int g = 0; g < 6; ++g)
       for (int i = 0; i < 9; ++i) {
-        const int n = 10 * g + i, s = TC_LEAVES * third + 9 * g + i;
+        const int n = i < 8 ? 8 * g + i : 48 + g, s = TC_LEAVES * third + 9 * g + i;
         uint64_t pw[128];  // V[s][j] = zeta_s^j
         pw[0] = 1;
         for (int j = 1; j < 128; ++j) pw[j] = pw[j - 1] * c.leaf_root[s] % p;

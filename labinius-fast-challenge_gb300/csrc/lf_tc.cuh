@@ -71,6 +71,12 @@ __device__ __forceinline__ bool mbar_wait_fast(uint64_t* bar, uint32_t parity, c
   return mbar_test_wait(bar, parity) || mbar_wait(bar, parity, abort, limit_cycles);
 }
 
+// ---- register redistribution between warpgroups (all four warps of a warpgroup execute it) ----
+template <int N>
+__device__ __forceinline__ void regs_inc() { asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(N)); }
+template <int N>
+__device__ __forceinline__ void regs_dec() { asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(N)); }
+
 // ---- proxy fences ----
 // Generic-proxy shared-memory writes become visible to the tensor core (async proxy).
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
@@ -95,6 +101,11 @@ __device__ __forceinline__ void tmem_ld_x2(uint32_t taddr, uint32_t& a, uint32_t
 }
 __device__ __forceinline__ void tmem_ld_x1(uint32_t taddr, uint32_t& a) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(a) : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_x8(uint32_t taddr, uint32_t* v) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+               : "r"(taddr));
 }
 __device__ __forceinline__ void tmem_ld_x16(uint32_t taddr, uint32_t (&v)[16]) {
   asm volatile(
