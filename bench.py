@@ -201,23 +201,40 @@ def device_table(prover, seed, log_vars):
     return t
 
 
-def process_e2e(lfgpu, prover, log_vars, n=5):
-    """labinius-fast as the harness runs it: process start -> proof file written (wall clock)."""
-    times = []
+def process_e2e(lfgpu, prover, log_vars, n=5, modulus=None):
+    """labinius-fast as the harness runs it: process start -> proof file written and the process
+    gone (wall clock), median of n fresh seeds; also the median of each phase: start (exec and
+    dynamic loading, before main), load (table and proof file mapped), ctx and key (CUDA context and
+    commitment key, made on a thread meanwhile), wait (what was left of them), prove, write, exit
+    (after the proof is written: process exit and the CUDA context's teardown)."""
+    times, phases = [], []
     with tempfile.TemporaryDirectory() as d:
         for i, seed in enumerate(seeds(n, 99)):
             tpath = os.path.join(d, f"t{i}.bin")
             with open(tpath, "wb") as f:
                 f.write(device_table(prover, seed, log_vars).cpu().numpy().tobytes())
             env = dict(os.environ, LABINIUS_SEED=seed.hex())
+            args = [lfgpu.CLI_PATH, "--prove", os.path.join(d, f"p{i}.bin"), "--table", tpath,
+                    "--log-vars", str(log_vars)]
+            if modulus is not None:
+                args += ["--modulus", str(modulus)]
+            m0 = time.monotonic_ns()
             t0 = time.perf_counter()
-            p = subprocess.run([lfgpu.CLI_PATH, "--prove", os.path.join(d, f"p{i}.bin"), "--table", tpath,
-                                "--log-vars", str(log_vars)], env=env, capture_output=True, text=True)
+            p = subprocess.run(args, env=env, capture_output=True, text=True)
             times.append((time.perf_counter() - t0) * 1e3)
+            m1 = time.monotonic_ns()
             if p.returncode != 0:
                 raise RuntimeError(p.stderr)
+            for ln in p.stderr.splitlines():
+                if ln.startswith("labinius-gb300 "):
+                    ph = {k: float(v) for k, v in (x.split("=") for x in ln.split()[1:])}
+                    ph["start_ms"] = (ph.pop("main_ns") - m0) / 1e6
+                    ph["exit_ms"] = (m1 - ph.pop("end_ns")) / 1e6
+                    phases.append(ph)
             os.unlink(tpath)
-    return statistics.median(times), times
+    keys = ("start_ms", "load_ms", "ctx_ms", "key_ms", "wait_ms", "prove_ms", "write_ms", "exit_ms")
+    med = {k: round(statistics.median(ph[k] for ph in phases), 2) for k in keys} if phases else None
+    return statistics.median(times), times, med
 
 
 def timed(stream, fn, steps):
@@ -281,9 +298,10 @@ def batched_leg(lfgpu, prover, n=32, seed=20260):
     big = max(range(n), key=lambda i: shapes[i])
     for _ in range(2):  # the largest shape once per lane, so no lane grows a buffer while timed
         prover.prove_batch([prover.make_job(seeds(1, 200 + big)[0], hosts[big].data_ptr(), shapes[big],
-                                            nbytes=hosts[big].numel()) for _ in range(max(prover.lanes or 4, 1))])
+                                            nbytes=hosts[big].numel()) for _ in range(max(prover.lanes or 8, 1))])
     for lv in sorted(set(shapes)):
-        prover.key_prepare(lv)  # every lane holds every shape's key
+        prover.key_prepare(lv)  # every lane holds every shape's key and that shape's work buffers
+    prover.prove_batch(jobs)  # untimed, right before the timed ones (lanes, streams, clocks warm)
     runs = []
     for _ in range(3):  # the median of three timed batches
         t0 = time.perf_counter()
@@ -307,7 +325,7 @@ def batched_leg(lfgpu, prover, n=32, seed=20260):
     return {"proofs_per_s": round(n / dt, 1), "jobs": n, "total_ms": round(dt * 1e3, 2),
             "runs_ms": [round(x * 1e3, 2) for x in runs],
             "plain_proofs_per_s": round(n / dt_plain, 1), "vs_plain": round(dt_plain / dt, 2),
-            "lanes": prover.lanes or 4, "log_vars": shapes, "verified": f"{accepted}/{n} accepted by the GPU checker",
+            "lanes": prover.lanes or 8, "log_vars": shapes, "verified": f"{accepted}/{n} accepted by the GPU checker",
             "tables": "page-locked host memory, H2D inside the timed batch"}
 
 
@@ -357,6 +375,11 @@ def micro_leg(lfgpu, prover, stream, ghash_log=28, moduli=("baseline", "2^64", "
     return out
 
 
+def pct(xs, q):
+    """The q-quantile of a sorted list (nearest rank below)."""
+    return xs[min(len(xs) - 1, int(q * len(xs)))] if xs else None
+
+
 def serving_leg(lfgpu, prover, requests=500, rate=8.0, seed=20261):
     """Poisson arrivals at `rate`/s, L uniform over the integers 22..31 (log-uniform table sizes),
     a fresh seed per request, one page-locked table per shape; latency = queueing + proving as
@@ -381,11 +404,11 @@ def serving_leg(lfgpu, prover, requests=500, rate=8.0, seed=20261):
     shapes = [rng.randint(22, 31) for _ in range(requests)]
 
     def run(p):
+        for lv in range(22, 32):
+            p.key_prepare(lv)  # every lane holds every shape's key and its work buffers
         warm = [p.make_job(seeds(1, 400 + lv)[0], pool[lv].data_ptr(), lv, nbytes=pool[lv].numel())
                 for lv in [31] * 8 + list(range(22, 32))]
-        p.prove_batch(warm)  # every lane's buffers grown to the largest shape
-        for lv in range(22, 32):
-            p.key_prepare(lv)  # every lane holds every shape's key
+        p.prove_batch(warm)
         jobs, tickets = [], []
         t0 = time.perf_counter()
         for i, (at, lv) in enumerate(zip(arrivals, shapes)):
@@ -406,15 +429,41 @@ def serving_leg(lfgpu, prover, requests=500, rate=8.0, seed=20261):
         # every served proof through the GPU checker (the shape's device table)
         ok = sum(p.verify_device(seeds(1, 1000 + i)[0], p.job_proof(j, r), shapes[i], dev_pool[shapes[i]].data_ptr())[0]
                  for i, (j, r) in enumerate(zip(jobs, done)))
+        qs = sorted(r.queue_ms for r in done)
+        big = sorted(r.run_ms for r, lv in zip(done, shapes) if lv == 31)
+        worst = sorted(zip(lat, shapes, done), key=lambda x: -x[0])[:5]
+        detail = {"queue_p50_ms": round(pct(qs, 0.5), 3), "queue_p99_ms": round(pct(qs, 0.99), 3),
+                  "run_2^31_p50_ms": round(pct(big, 0.5), 3) if big else None,
+                  "run_2^31_max_ms": round(big[-1], 3) if big else None,
+                  "slowest": [{"log_vars": lv, "queue_ms": round(r.queue_ms, 2), "run_ms": round(r.run_ms, 2)}
+                              for _, lv, r in worst]}
         lat.sort()
-        pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))]
-        return round(pct(0.50), 3), round(pct(0.99), 3), round(requests / wall, 2), round(wall, 2), ok
+        return round(pct(lat, 0.50), 3), round(pct(lat, 0.99), 3), round(requests / wall, 2), round(wall, 2), ok, detail
 
-    p50, p99, pps, wall, ok = run(prover)
+    def saturated(p, n):
+        """Closed loop: n requests (the same shape mix) submitted at once; served proofs/s until the
+        last one is reported."""
+        jobs = [p.make_job(seeds(1, 5000 + i)[0], pool[lv].data_ptr(), lv, nbytes=pool[lv].numel())
+                for i, lv in enumerate(shapes[:n])]
+        t0 = time.perf_counter()
+        tickets = [p.submit(j) for j in jobs]
+        for t_ in tickets:
+            rc, r = p.poll(t_, 120000)
+            if rc != 0 or r.status != 0:
+                raise RuntimeError(f"saturated request failed: {rc} {r.status}")
+        return round(n / (time.perf_counter() - t0), 1)
+
+    nsat = min(200, requests)
+    p50, p99, pps, wall, ok, detail = run(prover)
+    sat = saturated(prover, nsat)
     with lfgpu.Prover(prover.device, lanes=1) as one:
-        p50_1, p99_1, _, _, _ = run(one)
+        p50_1, p99_1, _, _, _, detail_1 = run(one)
+        sat_1 = saturated(one, nsat)
     return {"p50_ms": p50, "p99_ms": p99, "proofs_per_s": pps, "requests": requests, "rate_per_s": rate,
-            "lanes": prover.lanes or 4, "plain": {"p50_ms": p50_1, "p99_ms": p99_1, "lanes": 1},
+            "lanes": prover.lanes or 8, "detail": detail,
+            "plain": {"p50_ms": p50_1, "p99_ms": p99_1, "lanes": 1, "detail": detail_1},
+            "saturated": {"requests": nsat, "proofs_per_s": sat, "plain_proofs_per_s": sat_1,
+                          "vs_plain": round(sat / sat_1, 2)},
             "verified": f"{ok}/{requests} accepted by the GPU checker",
             "log_vars": "uniform 22..31", "wall_s": wall, "latency": "queue + prove, host tables (H2D included)"}
 
@@ -529,10 +578,13 @@ def main():
          for _ in range(3)])
     if not all(r == (True, "") for r in vres):
         raise RuntimeError(f"the GPU checker rejected the benchmarked proof: {vres}")
-    proc_ms = None
+    proc_ms, proc_phases, proc_ref_q = None, None, None
     if not args.no_process:
         try:
-            proc_ms, _ = process_e2e(lfgpu, prover, log_vars)
+            proc_ms, _, proc_phases = process_e2e(lfgpu, prover, log_vars)
+            # the same window at the modulus of the reference harness's recorded run (.yukon/README.md:161-170)
+            rq_ms, _, rq_phases = process_e2e(lfgpu, prover, log_vars, modulus=55_144_219_393)
+            proc_ref_q = {"modulus": 55_144_219_393, "process_e2e_ms": round(rq_ms, 2), "phases_ms": rq_phases}
         except Exception as e:  # reported, not fatal
             proc_ms = f"failed: {e}"
     batched = None
@@ -558,7 +610,9 @@ def main():
         cms, cores = cpu_baseline(log_vars, bytes(host.numpy()), e2e_seed, proof)
         cpu = {"value": round(cms, 1), "unit": "ms/proof", "cores": cores, "kind": "port",
                "sample": f"one full 2^{log_vars}-bit proof of the e2e table (oracle restatement of the reference "
-                         "prover, 3-prime transform commit), all host threads; its proof equals the GPU proof"}
+                         "prover, 3-prime transform commit), all host threads; its proof equals the GPU proof. "
+                         "A slow restatement (the checker's plain switch, row and fold, not the reference's "
+                         "SIMD kernels): reference_recorded_run holds the reference's own figure"}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "ms/proof", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": False, "scaling": "weak",
@@ -572,6 +626,14 @@ def main():
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms/proof", "h2d_bytes_per_step": tbytes,
                 "d2h_bytes_per_step": cap},
         "process_e2e_ms": proc_ms,
+        "process_phases_ms": proc_phases,
+        "process_at_recorded_q": proc_ref_q,
+        # the reference's one recorded scored run (.yukon/README.md:161-170): its x86 prover, median of
+        # 5 process windows at 2^31 bits on 8 Xeon 8488C cores, Q = 55,144,219,393 (another host)
+        "reference_recorded_run": {
+            "value_ms": 2972.27, "host": "Intel Xeon Platinum 8488C, 8 CPUs (c7i.2xlarge)", "modulus": 55_144_219_393,
+            "gpu_process_ms_same_q": proc_ref_q["process_e2e_ms"] if isinstance(proc_ref_q, dict) else None,
+            "ratio": round(2972.27 / proc_ref_q["process_e2e_ms"], 2) if isinstance(proc_ref_q, dict) else None},
         "verify_ms": round(vms, 3),
         "batched": batched,
         "serving": serving,

@@ -39,7 +39,7 @@ typedef struct lf_config {
   int device;             /* CUDA ordinal */
   size_t hbm_budget;      /* bytes the context may hold on the device; 0 = no limit */
   int lanes;              /* proofs a batch or the serving queue may run at once, each on its own
-                             stream and host thread (1..8); 0 = the default, 4 */
+                             stream and host thread (1..8); 0 = the default, 8 */
 } lf_config;
 
 /* Per-phase device times of the last lf_prove* call on a context, in milliseconds
@@ -71,7 +71,10 @@ size_t lf_proof_size(const uint8_t q_le[16], uint32_t log_vars);
 int lf_accept_modulus(const uint8_t q_le[16], uint32_t log_vars);
 
 /* Expand the public matrix A for (q, 2^log_vars) and transform it to the device key; cached on
- * the context (solution/proof_generate/src/keygen.rs:139-266, build-time key images main.rs:1712-1757). */
+ * the context and each of its lanes (solution/proof_generate/src/keygen.rs:139-266, build-time key
+ * images main.rs:1712-1757). Also grows every device work buffer a proof of this shape uses (a
+ * host-table copy included) on the context and its lanes, so that later proofs of the shape
+ * allocate and free no device memory (a free waits for the whole device). */
 int lf_key_prepare(lf_ctx* ctx, const uint8_t q_le[16], uint32_t log_vars);
 
 /* One proof of the table (host memory, table_bytes = 2^log_vars / 8, little-endian u128 words as
@@ -128,7 +131,7 @@ typedef struct lf_result {
 
 /* Proves n independent jobs (any mix of shapes and moduli; each (Q, shape) key is built once and
  * cached) on the context's GPU. With two or more jobs they run on the lanes of the context
- * (lf_config.lanes, four by default: one stream and host thread each, taking jobs in order from
+ * (lf_config.lanes, eight by default: one stream and host thread each, taking jobs in order from
  * one counter), so one proof's host work overlaps other proofs' kernels; with one lane the next
  * job's host table is copied on a second stream while the current job is proven. results[i] receives job i's outcome; the return value
  * is LF_OK if every job succeeded, else the first failing job's code.

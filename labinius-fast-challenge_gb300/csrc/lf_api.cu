@@ -258,7 +258,7 @@ struct lf_ctx {
   // it from the last block of the round's kernel
   unsigned long long* msg_out = nullptr;
   unsigned long long* msg_out_dev = nullptr;
-  int nlanes = 4;                // proofs in flight at once: this context and nlanes - 1 lanes
+  int nlanes = 8;                // proofs in flight at once: this context and nlanes - 1 lanes
   std::vector<lf_ctx*> lanes;    // contexts on the same device (own stream, buffers, keys)
   std::mutex lanemu;             // guards lanes (created on first use, only added to)
   bool is_lane = false;          // this context is another context's lane
@@ -452,6 +452,43 @@ int ensure_key(lf_ctx* ctx, u128 q, const Shape& sh, int extra_bits = 0) {
     ctx->key = ctx->keys.back().get();
   }
   ctx->key->last_use = ++ctx->key_clock;
+  return LF_OK;
+}
+
+// Every work buffer a proof of this shape and modulus grows to (the sizes prove_device and the
+// functions it calls ask for), grown now: a proof whose buffers are already this large allocates
+// nothing, so no cudaFree (a device-wide wait) stalls the other lanes or a table upload mid-batch.
+int reserve_buffers(lf_ctx* ctx, u128 q, const Shape& sh, int nprimes, bool host_table) {
+  const size_t commit_bytes = coefficient_bytes(q) * COLUMNS * RING_N;
+  const uint64_t nblocks = 1ull << (sh.lp - 12), xmax = nblocks;
+  const uint64_t nchunks = (STREAM_PREFIX + commit_bytes - 1) / 1024;
+  const size_t fold_bytes = 4 * RING_N * sh.ring_elements;
+  if (host_table) CK(ctx->table.ensure(sh.words * 16));
+  if (host_table && ctx->nlanes == 1) CK(ctx->table2.ensure(sh.words * 16));  // one-lane batches alternate two
+  CK(ctx->partial.ensure((size_t)ctx->split_for(sh, nprimes) * nprimes * COLUMNS * LEAVES * 4 * 4));
+  CK(ctx->stream_buf.ensure(STREAM_PREFIX + commit_bytes + 1024));
+  CK(ctx->status.ensure(16));
+  CK(ctx->cvs.ensure(nchunks * 32 + 32));
+  CK(ctx->cvs_scratch.ensure(2 * nchunks * 32 + 64));
+  CK(ctx->subtrees.ensure(64 * 32));
+  CK(ctx->rhi.ensure(64 * 16));
+  CK(ctx->elo.ensure(4096 * 16));
+  CK(ctx->ehi.ensure(nblocks * 16));
+  CK(ctx->sblk.ensure(nblocks * 128 * 16));
+  CK(ctx->vparts.ensure(256 * 8));
+  CK(ctx->batch.ensure(2 * 128 * 24));
+  CK(ctx->psi.ensure(2 * 16 * 256 * 24));
+  CK(ctx->soa.ensure(6 * 4096 * 8));
+  CK(ctx->wbuf.ensure(2 * xmax * 24 + 48));
+  CK(ctx->rbuf.ensure((xmax > 2 ? xmax : 2) * 128 * 16));
+  CK(ctx->p0.ensure(64 * 24));
+  CK(ctx->eqt.ensure(sh.column_len * 24));
+  CK(ctx->row.ensure(COLUMNS * 24));
+  CK(ctx->hasher.ensure(sizeof(bk::Hasher)));
+  CK(ctx->chal.ensure(COLUMNS * sizeof(Challenge)));
+  CK(ctx->fold.ensure(fold_bytes));
+  CK(ctx->fold_strips.ensure(COLUMNS * FOLD_STRIP_BYTES));
+  CK(ctx->fold_part.ensure((size_t)fold_splits(sh.ring_elements, ctx->sms) * fold_bytes));
   return LF_OK;
 }
 
@@ -930,8 +967,29 @@ int start_table_upload(lf_ctx* ctx, const void* table, size_t table_bytes, const
   return LF_OK;
 }
 
+// A pageable proof buffer on a device that reaches host memory through the host's page tables:
+// a kernel on the touch stream writes one byte per 4 KB page while the commitment runs, so the
+// proof's own copies into the buffer find its pages already mapped for the device (a first
+// device access to a page is slow). *ready is the event the first device write into the buffer
+// must wait for, or stays null (page-locked or otherwise registered memory needs no touch).
+int touch_proof_buffer(lf_ctx* ctx, uint8_t* proof, size_t len, cudaEvent_t* ready) {
+  *ready = nullptr;
+  cudaPointerAttributes pa{};
+  if (ctx->pageable_access && cudaPointerGetAttributes(&pa, proof) == cudaSuccess &&
+      pa.type == cudaMemoryTypeUnregistered) {
+    int rc = side_streams(ctx);
+    if (rc) return rc;
+    launch_touch_pages(proof, len, ctx->touch_stream);
+    CKL("proof buffer touch");
+    CK(cudaEventRecord(ctx->touched, ctx->touch_stream));
+    *ready = ctx->touched;
+  }
+  cudaGetLastError();  // cudaPointerGetAttributes on plain host memory leaves no error behind
+  return LF_OK;
+}
+
 // A job's proof; a host table is copied by start_table_upload (streamed into the commitment when
-// it is page-locked).
+// it is page-locked); a pageable proof buffer is touched meanwhile (touch_proof_buffer).
 int run_job(lf_ctx* ctx, const lf_job& j, size_t* proof_len) {
   u128 q;
   Shape sh;
@@ -940,18 +998,26 @@ int run_job(lf_ctx* ctx, const lf_job& j, size_t* proof_len) {
   cudaSetDevice(ctx->device);
   ctx->prof = lf_profile{};
   cudaEventRecord(ctx->ev[0], ctx->stream);
-  if (j.table_on_device)
-    return prove_device(ctx, j.seed, q, sh, reinterpret_cast<const uint4*>(j.table), j.proof, proof_len);
+  cudaEvent_t proof_ready = nullptr;
+  if (j.table_on_device) {
+    if ((rc = touch_proof_buffer(ctx, j.proof, proof_size(q, sh), &proof_ready))) return rc;
+    rc = prove_device(ctx, j.seed, q, sh, reinterpret_cast<const uint4*>(j.table), j.proof, proof_len, nullptr,
+                      proof_ready);
+    if (proof_ready) cudaStreamSynchronize(ctx->touch_stream);
+    return rc;
+  }
   if (j.table_bytes != sh.words * 16) return fail(ctx, LF_E_TABLE_LEN, "witness table has the wrong length");
   TableStream ts{};
   bool streamed = false;
   if ((rc = start_table_upload(ctx, j.table, j.table_bytes, sh, &ts, &streamed))) return rc;
   ctx->test_withhold = -1;  // the test hooks apply to one proof
   ctx->test_ready_wait = 0;
-  rc = prove_device(ctx, j.seed, q, sh, ctx->table.as<uint4>(), j.proof, proof_len, ctx->uploaded[0], nullptr,
-                    streamed ? &ts : nullptr);
+  if ((rc = touch_proof_buffer(ctx, j.proof, proof_size(q, sh), &proof_ready)) == LF_OK)
+    rc = prove_device(ctx, j.seed, q, sh, ctx->table.as<uint4>(), j.proof, proof_len, ctx->uploaded[0], proof_ready,
+                      streamed ? &ts : nullptr);
   if (streamed && ts.next < TABLE_PARTS) enqueue_table_parts(ctx, &ts, TABLE_PARTS);  // (an early failure)
   cudaStreamSynchronize(ctx->upload_stream);  // (a proof that failed early may not have waited for it)
+  if (proof_ready) cudaStreamSynchronize(ctx->touch_stream);
   return rc;
 }
 
@@ -1425,7 +1491,7 @@ int lf_ctx_create(const lf_config* cfg, lf_ctx** out) {
     delete ctx;
     return LF_E_ARGS;
   }
-  ctx->nlanes = cfg && cfg->lanes ? cfg->lanes : 4;
+  ctx->nlanes = cfg && cfg->lanes ? cfg->lanes : 8;
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) {
     delete ctx;
@@ -1524,12 +1590,15 @@ int lf_key_prepare(lf_ctx* ctx, const uint8_t q_le[16], uint32_t log_vars) {
   if (!accept_modulus(q, s)) return fail(ctx, LF_E_MODULUS, "invalid commitment modulus");
   cudaSetDevice(ctx->device);
   int rc = ensure_key(ctx, q, s);
-  for (lf_ctx* l : lanes_of(ctx)) {  // each lane keeps its own copy of the key
+  if (rc == LF_OK) rc = reserve_buffers(ctx, q, s, ctx->key->mp.nprimes, true);
+  for (lf_ctx* l : lanes_of(ctx)) {  // each lane keeps its own copy of the key and its own buffers
     if (rc != LF_OK) break;
     std::lock_guard<std::mutex> gl(l->mu);
     rc = ensure_key(l, q, s);
+    if (rc == LF_OK) rc = reserve_buffers(l, q, s, l->key->mp.nprimes, true);
     if (rc) fail(ctx, rc, lf_last_error(l));
   }
+  if (rc == LF_OK) CK(cudaDeviceSynchronize());  // the reservations are complete before any proof
   return rc;
 }
 
@@ -1575,15 +1644,7 @@ int lf_prove(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32
   ctx->test_withhold = -1;  // the test hooks apply to one proof
   ctx->test_ready_wait = 0;
   cudaEvent_t proof_ready = nullptr;
-  cudaPointerAttributes pa{};
-  if (ctx->pageable_access && cudaPointerGetAttributes(&pa, proof) == cudaSuccess &&
-      pa.type == cudaMemoryTypeUnregistered) {
-    launch_touch_pages(proof, *proof_len, ctx->touch_stream);
-    CKL("proof buffer touch");
-    CK(cudaEventRecord(ctx->touched, ctx->touch_stream));
-    proof_ready = ctx->touched;
-  }
-  cudaGetLastError();  // cudaPointerGetAttributes on plain host memory leaves no error behind
+  if ((rc = touch_proof_buffer(ctx, proof, *proof_len, &proof_ready))) return rc;
   rc = prove_device(ctx, seed, q, sh, ctx->table.as<uint4>(), proof, proof_len, ctx->uploaded[0], proof_ready,
                     streamed ? &tstream : nullptr);
   if (streamed && tstream.next < TABLE_PARTS) enqueue_table_parts(ctx, &tstream, TABLE_PARTS);  // (an early failure)
