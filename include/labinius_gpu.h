@@ -127,6 +127,10 @@ typedef struct lf_result {
   size_t proof_len; /* bytes written to the job's proof buffer */
   double queue_ms;  /* submission (or batch start) to the start of the proof */
   double run_ms;    /* start of the proof to its bytes in the proof buffer */
+  /* where run_ms went: device time of the proof's own work on its stream (commitment through the
+   * proof's download; lf_profile's phases summed), of its commitment kernel, and of the host
+   * table's copy on the copy stream (0 for a device table) */
+  double device_ms, commit_ms, upload_ms;
 } lf_result;
 
 /* Proves n independent jobs (any mix of shapes and moduli; each (Q, shape) key is built once and

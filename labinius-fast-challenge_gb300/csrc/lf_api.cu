@@ -464,7 +464,6 @@ int reserve_buffers(lf_ctx* ctx, u128 q, const Shape& sh, int nprimes, bool host
   const uint64_t nchunks = (STREAM_PREFIX + commit_bytes - 1) / 1024;
   const size_t fold_bytes = 4 * RING_N * sh.ring_elements;
   if (host_table) CK(ctx->table.ensure(sh.words * 16));
-  if (host_table && ctx->nlanes == 1) CK(ctx->table2.ensure(sh.words * 16));  // one-lane batches alternate two
   CK(ctx->partial.ensure((size_t)ctx->split_for(sh, nprimes) * nprimes * COLUMNS * LEAVES * 4 * 4));
   CK(ctx->stream_buf.ensure(STREAM_PREFIX + commit_bytes + 1024));
   CK(ctx->status.ensure(16));
@@ -652,11 +651,33 @@ int enqueue_table_parts(lf_ctx* ctx, TableStream* ts, int end) {
   return LF_OK;
 }
 
-// table_ready / proof_ready (may be null): events the prover's stream waits for before the first
-// kernel that reads the table and before the first device write into `proof`. With ts, the
-// commitment starts before the table is complete (table_ready is then unused).
+// A pageable proof buffer on a device that reaches host memory through the host's page tables:
+// while the commitment runs, a kernel on the touch stream writes one byte per 4 KB page, so the
+// proof's own copies into the buffer find its pages already mapped for the device (a first
+// device access to a page is slow). *ready is the event the first device write into the buffer
+// must wait for, or stays null (page-locked or otherwise registered memory needs no touch).
+int touch_proof_buffer(lf_ctx* ctx, uint8_t* proof, size_t len, cudaEvent_t* ready) {
+  *ready = nullptr;
+  cudaPointerAttributes pa{};
+  if (ctx->pageable_access && len && cudaPointerGetAttributes(&pa, proof) == cudaSuccess &&
+      pa.type == cudaMemoryTypeUnregistered) {
+    int rc = side_streams(ctx);
+    if (rc) return rc;
+    launch_touch_pages(proof, len, ctx->touch_stream);
+    CKL("proof buffer touch");
+    CK(cudaEventRecord(ctx->touched, ctx->touch_stream));
+    *ready = ctx->touched;
+  }
+  cudaGetLastError();  // cudaPointerGetAttributes on plain host memory leaves no error behind
+  return LF_OK;
+}
+
+// table_ready (may be null): an event the prover's stream waits for before the first kernel that
+// reads the table. With ts, the commitment starts before the table is complete (table_ready is
+// then unused). touch: `proof` is host memory that may need touch_proof_buffer (done while the
+// commitment runs).
 int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, const uint4* table, uint8_t* proof,
-                 size_t* proof_len, cudaEvent_t table_ready = nullptr, cudaEvent_t proof_ready = nullptr,
+                 size_t* proof_len, cudaEvent_t table_ready = nullptr, bool touch = false,
                  TableStream* ts = nullptr) {
   cudaStream_t st = ctx->stream;
   const size_t width = coefficient_bytes(q);
@@ -706,6 +727,8 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
 
   // ---- transcript (main.rs:166-174): the prefix on the host, the commitment's chunks on the device ----
   Transcript t;
+  cudaEvent_t proof_ready = nullptr;
+  if (touch && (rc = touch_proof_buffer(ctx, proof, plen, &proof_ready))) return rc;
   if (proof_ready) CK(cudaStreamWaitEvent(st, proof_ready, 0));
   rc = absorb_commitment(ctx, t, seed, sh, q, commit_bytes, nullptr, proof + at_commit);
   if (rc) return rc;
@@ -967,27 +990,6 @@ int start_table_upload(lf_ctx* ctx, const void* table, size_t table_bytes, const
   return LF_OK;
 }
 
-// A pageable proof buffer on a device that reaches host memory through the host's page tables:
-// a kernel on the touch stream writes one byte per 4 KB page while the commitment runs, so the
-// proof's own copies into the buffer find its pages already mapped for the device (a first
-// device access to a page is slow). *ready is the event the first device write into the buffer
-// must wait for, or stays null (page-locked or otherwise registered memory needs no touch).
-int touch_proof_buffer(lf_ctx* ctx, uint8_t* proof, size_t len, cudaEvent_t* ready) {
-  *ready = nullptr;
-  cudaPointerAttributes pa{};
-  if (ctx->pageable_access && cudaPointerGetAttributes(&pa, proof) == cudaSuccess &&
-      pa.type == cudaMemoryTypeUnregistered) {
-    int rc = side_streams(ctx);
-    if (rc) return rc;
-    launch_touch_pages(proof, len, ctx->touch_stream);
-    CKL("proof buffer touch");
-    CK(cudaEventRecord(ctx->touched, ctx->touch_stream));
-    *ready = ctx->touched;
-  }
-  cudaGetLastError();  // cudaPointerGetAttributes on plain host memory leaves no error behind
-  return LF_OK;
-}
-
 // A job's proof; a host table is copied by start_table_upload (streamed into the commitment when
 // it is page-locked); a pageable proof buffer is touched meanwhile (touch_proof_buffer).
 int run_job(lf_ctx* ctx, const lf_job& j, size_t* proof_len) {
@@ -998,12 +1000,9 @@ int run_job(lf_ctx* ctx, const lf_job& j, size_t* proof_len) {
   cudaSetDevice(ctx->device);
   ctx->prof = lf_profile{};
   cudaEventRecord(ctx->ev[0], ctx->stream);
-  cudaEvent_t proof_ready = nullptr;
   if (j.table_on_device) {
-    if ((rc = touch_proof_buffer(ctx, j.proof, proof_size(q, sh), &proof_ready))) return rc;
-    rc = prove_device(ctx, j.seed, q, sh, reinterpret_cast<const uint4*>(j.table), j.proof, proof_len, nullptr,
-                      proof_ready);
-    if (proof_ready) cudaStreamSynchronize(ctx->touch_stream);
+    rc = prove_device(ctx, j.seed, q, sh, reinterpret_cast<const uint4*>(j.table), j.proof, proof_len, nullptr, true);
+    if (ctx->touch_stream) cudaStreamSynchronize(ctx->touch_stream);  // (a proof that failed early)
     return rc;
   }
   if (j.table_bytes != sh.words * 16) return fail(ctx, LF_E_TABLE_LEN, "witness table has the wrong length");
@@ -1012,13 +1011,26 @@ int run_job(lf_ctx* ctx, const lf_job& j, size_t* proof_len) {
   if ((rc = start_table_upload(ctx, j.table, j.table_bytes, sh, &ts, &streamed))) return rc;
   ctx->test_withhold = -1;  // the test hooks apply to one proof
   ctx->test_ready_wait = 0;
-  if ((rc = touch_proof_buffer(ctx, j.proof, proof_size(q, sh), &proof_ready)) == LF_OK)
-    rc = prove_device(ctx, j.seed, q, sh, ctx->table.as<uint4>(), j.proof, proof_len, ctx->uploaded[0], proof_ready,
-                      streamed ? &ts : nullptr);
+  rc = prove_device(ctx, j.seed, q, sh, ctx->table.as<uint4>(), j.proof, proof_len, ctx->uploaded[0], true,
+                    streamed ? &ts : nullptr);
   if (streamed && ts.next < TABLE_PARTS) enqueue_table_parts(ctx, &ts, TABLE_PARTS);  // (an early failure)
-  cudaStreamSynchronize(ctx->upload_stream);  // (a proof that failed early may not have waited for it)
-  if (proof_ready) cudaStreamSynchronize(ctx->touch_stream);
+  // (a proof that failed early may not have waited for the side streams)
+  cudaStreamSynchronize(ctx->upload_stream);
+  cudaStreamSynchronize(ctx->touch_stream);
   return rc;
+}
+
+// The device-side breakdown of a job's run (lf_result): the phases of the proof on its own stream,
+// its commitment kernel, and the host table's copy (timed by events on the copy stream).
+void result_times(lf_ctx* c, const lf_job& j, lf_result& r) {
+  const lf_profile& p = c->prof;
+  r.device_ms = p.key_ms + p.commit_ms + p.finish_ms + p.transcript_ms + p.partials_ms + p.switch_ms + p.row_ms +
+                p.challenges_ms + p.fold_ms + p.download_ms;
+  r.commit_ms = p.commit_ms;
+  r.upload_ms = 0;
+  float up = 0;
+  if (!j.table_on_device && c->up_t0 && cudaEventElapsedTime(&up, c->up_t0, c->up_t1) == cudaSuccess) r.upload_ms = up;
+  cudaGetLastError();
 }
 
 // One serving lane: `c` (the owner or one of its lanes) proves requests from the owner's FIFO. The front
@@ -1048,8 +1060,9 @@ void serve_loop(lf_ctx* owner, lf_ctx* c) {
     {
       std::lock_guard<std::mutex> g(c->mu);
       r.status = run_job(c, item.job, &r.proof_len);
+      r.run_ms = ms_between(start, clk::now());
+      if (r.status == LF_OK) result_times(c, item.job, r);
     }
-    r.run_ms = ms_between(start, clk::now());
     {
       std::lock_guard<std::mutex> lk(owner->qmu);
       owner->outcomes[item.ticket] = lf_ctx::Outcome{true, r};
@@ -1615,7 +1628,8 @@ int lf_prove_device(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16],
   auto t0 = std::chrono::steady_clock::now();
   ctx->prof = lf_profile{};
   cudaEventRecord(ctx->ev[0], ctx->stream);
-  rc = prove_device(ctx, seed, q, sh, reinterpret_cast<const uint4*>(table_dev), proof, proof_len);
+  rc = prove_device(ctx, seed, q, sh, reinterpret_cast<const uint4*>(table_dev), proof, proof_len, nullptr, true);
+  if (ctx->touch_stream) cudaStreamSynchronize(ctx->touch_stream);  // (a proof that failed early)
   ctx->prof.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return rc;
 }
@@ -1643,9 +1657,7 @@ int lf_prove(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32
   if ((rc = start_table_upload(ctx, table, table_bytes, sh, &tstream, &streamed))) return rc;
   ctx->test_withhold = -1;  // the test hooks apply to one proof
   ctx->test_ready_wait = 0;
-  cudaEvent_t proof_ready = nullptr;
-  if ((rc = touch_proof_buffer(ctx, proof, *proof_len, &proof_ready))) return rc;
-  rc = prove_device(ctx, seed, q, sh, ctx->table.as<uint4>(), proof, proof_len, ctx->uploaded[0], proof_ready,
+  rc = prove_device(ctx, seed, q, sh, ctx->table.as<uint4>(), proof, proof_len, ctx->uploaded[0], true,
                     streamed ? &tstream : nullptr);
   if (streamed && tstream.next < TABLE_PARTS) enqueue_table_parts(ctx, &tstream, TABLE_PARTS);  // (an early failure)
   // (a proof that failed early may not have waited for the side streams)
@@ -1751,6 +1763,7 @@ void batch_lane(lf_ctx* c, bool lock, const lf_job* jobs, lf_result* results, co
     r.status = pre[i];
     if (r.status == LF_OK) r.status = run_job(c, jobs[i], &r.proof_len);
     r.run_ms = ms_between(start, clk::now());
+    if (r.status == LF_OK) result_times(c, jobs[i], r);
   }
 }
 
@@ -1817,7 +1830,7 @@ int lf_prove_batch(lf_ctx* ctx, size_t n, const lf_job* jobs, lf_result* results
       check_job(ctx, j, q, sh);  // passed in pre[i]
       ctx->prof = lf_profile{};
       cudaEventRecord(ctx->ev[0], ctx->stream);
-      r.status = prove_device(ctx, j.seed, q, sh, table, j.proof, &r.proof_len);
+      r.status = prove_device(ctx, j.seed, q, sh, table, j.proof, &r.proof_len, nullptr, true);
     }
     r.run_ms = ms_between(start, clk::now());
     if (r.status != LF_OK && first == LF_OK) first = r.status;

@@ -56,7 +56,8 @@ class Job(ctypes.Structure):
 
 class Result(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("proof_len", ctypes.c_size_t), ("queue_ms", ctypes.c_double),
-                ("run_ms", ctypes.c_double)]
+                ("run_ms", ctypes.c_double), ("device_ms", ctypes.c_double), ("commit_ms", ctypes.c_double),
+                ("upload_ms", ctypes.c_double)]
 
 
 class Profile(ctypes.Structure):
