@@ -375,6 +375,24 @@ def micro_leg(lfgpu, prover, stream, ghash_log=28, moduli=("baseline", "2^64", "
     return out
 
 
+def h2d_gbs(nbytes=256 << 20, reps=5):
+    """Plain host-to-device copy bandwidth right now (a page-locked 256 MiB buffer, CUDA events,
+    median of reps): what the host-table legs' uploads can get from host memory at that moment."""
+    import torch
+
+    src = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    dst = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    xs = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        dst.copy_(src, non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        xs.append(nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    return round(statistics.median(xs), 1)
+
+
 def pct(xs, q):
     """The q-quantile of a sorted list (nearest rank below)."""
     return xs[min(len(xs) - 1, int(q * len(xs)))] if xs else None
@@ -466,11 +484,15 @@ def serving_leg(lfgpu, prover, requests=500, rate=8.0, seed=20261):
         return round(n / (time.perf_counter() - t0), 1)
 
     nsat = min(200, requests)
+    bw0 = h2d_gbs()
     p50, p99, pps, wall, ok, detail = run(prover)
+    detail["h2d_gbs_before_after"] = [bw0, h2d_gbs()]
     d50, d99, _, _, dok, ddetail = run(prover, on_device=True)
     sat = saturated(prover, nsat)
     with lfgpu.Prover(prover.device, lanes=1) as one:
+        bw1 = h2d_gbs()
         p50_1, p99_1, _, _, _, detail_1 = run(one)
+        detail_1["h2d_gbs_before_after"] = [bw1, h2d_gbs()]
         sat_1 = saturated(one, nsat)
     return {"p50_ms": p50, "p99_ms": p99, "proofs_per_s": pps, "requests": requests, "rate_per_s": rate,
             "lanes": prover.lanes or 8, "detail": detail,
@@ -583,6 +605,7 @@ def main():
     e2e_total = max_over_ranks(e2e_total, world)
     barrier(world)
     e2e_ms = e2e_total / args.steps / world
+    e2e_h2d = h2d_gbs()
     if rank != 0:
         return
     proof = ctypes.string_at(pout, cap)
@@ -639,7 +662,7 @@ def main():
                    "parallelism": f"replicas x{world}",
                    "timing": "CUDA events on the prover's stream around the timed steps", "tuned": tuned},
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms/proof", "h2d_bytes_per_step": tbytes,
-                "d2h_bytes_per_step": cap},
+                "d2h_bytes_per_step": cap, "h2d_gbs_after": e2e_h2d},
         "process_e2e_ms": proc_ms,
         "process_phases_ms": proc_phases,
         "process_at_recorded_q": proc_ref_q,
