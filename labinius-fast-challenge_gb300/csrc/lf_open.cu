@@ -264,17 +264,24 @@ cudaError_t launch_challenges(const void* hasher_dev, uint64_t base_counter, con
 // raw positions y = x + pos in [0, 289), then Y^162 = Y^81 - 1 (so Y^y = Y^(y-81) - Y^(y-162)
 // for 162 <= y < 243 and Y^y = -Y^(y-243) above).
 //
-// On the tensor cores this is one product per block of 128 table words (rows) and run of columns:
-//   D[row][n] = sum_j sum_x bit_x(word_j of the row) * C_j[303 - n - x],   n = 303 - y,
-// C_j the signed challenge (+-1 at its 28 positions). A = the words expanded to bf16 (2.0 per set
-// bit, bits in natural order, K-major); B[x][n] = C_j[303 - n - x] / 2 depends on x + n only, so
-// its 8 x 8 core matrices depend only on (k group + n group): one strip of 53 cores per column
-// (k_fold_cores) read through an MN-major descriptor whose k-group and n-group strides are both
-// one core. D (128 x 304, two MMAs of N = 160 and 144) is exact in f32 (|.| <= 28 x 1024).
+// On the tensor cores this is one product per block of 128 table words (rows) and run of columns,
+// with the reduction already in the second operand. Output coefficient i receives the raw
+// positions y = i (+), y = i + 81 (+, when 81 <= i), y = i + 162 (-, when i < 81) and y = i + 243
+// (-, when i < 46), and a raw position is x + pos, so with d = i - x and C_j the signed challenge
+// (+-1 at its 28 positions, 0 outside [0, 162)):
+//   i <  81:  coefficient += bit_x * (C_j[d] - C_j[d + 162] - C_j[d + 243])   (for 46 <= i < 81
+//             the last index is at least 162, so one formula serves the whole range)
+//   i >= 81:  coefficient += bit_x * (C_j[d] + C_j[d + 81])
+// Each range is a function of d alone. With n = 80 - i (low range) or n = 161 - i (high range),
+// B[x][n] = f(const - n - x) depends on x + n only, so its 8 x 8 core matrices depend only on
+// (k group + n group): one strip of 28 cores per range and column (k_fold_cores), read through an
+// MN-major descriptor whose k-group and n-group strides are both one core. A = the words expanded
+// to bf16 (2.0 per set bit, bits in natural order, K-major). D = 128 x 192 (two MMAs of N = 96,
+// 81 columns used in each), exact in f32 (integers well inside 2^24).
 // ---------------------------------------------------------------------------------------------
-constexpr int RAW_Y = 128 + 161;                // 289 raw positions
-constexpr int FT_CORES = 53;                    // cores per column strip
-constexpr int FT_STRIP = FT_CORES * 128;        // 6784 bytes
+constexpr int FT_RCORES = 28;                   // cores per range strip (k groups 0..15 + n groups 0..11)
+constexpr int FT_STRIP = 2 * FT_RCORES * 128;   // both ranges' strips of a column: 7168 bytes
+constexpr int FT_N = 96;                        // MMA N per range (81 coefficients used)
 constexpr int FT_TILE = 128 * 128 * 2;          // A tile: 128 words x 128 bits, bf16
 constexpr int FT_STAGES = 3;                    // A tiles (read by the MMAs)
 constexpr int FT_RING = 8;                      // strips and raw words, loaded FT_AHEAD columns early
@@ -284,25 +291,33 @@ constexpr int FT_THREADS = FT_PRODUCERS + 32;   // warp 0 issues the MMAs
 constexpr int FT_SMEM = FT_RING * FT_STRIP + FT_STAGES * FT_TILE + FT_RING * FT_PRODUCERS * 16 + 128;
 constexpr long long FT_WAIT_CYCLES = 2000000000LL;
 
-// Strip of column j: core e holds element (r, i) = C_j[303 - (8 e + r + i)] / 2 as bf16.
+// Strips of column j, low range then high range: core e of a range holds element (r, c) =
+// f(const - (8 e + r + c)) / 2 as bf16, with f and const of the range (80 and the three-term
+// difference below i = 81, 161 and the two-term sum above); sums of up to three +-0.5 are exact.
 __global__ void __launch_bounds__(128) k_fold_cores(const Challenge* __restrict__ ch, uint8_t* __restrict__ strips) {
-  __shared__ uint16_t dense[N162];
+  __shared__ float dense[N162];
   const int j = blockIdx.x, tid = threadIdx.x;
-  for (int i = tid; i < N162; i += 128) dense[i] = 0;
+  for (int i = tid; i < N162; i += 128) dense[i] = 0.0f;
   __syncthreads();
   if (tid < WEIGHT) {
     const int pos = ch[j].positions[tid];
     const bool neg = (((ch[j].signs >> tid) & 1) ^ (pos & 1)) != 0;
-    dense[pos] = neg ? 0xBF00 : 0x3F00;  // -0.5 / +0.5
+    dense[pos] = neg ? -0.5f : 0.5f;
   }
   __syncthreads();
+  auto C = [&](int z) { return (z >= 0 && z < N162) ? dense[z] : 0.0f; };
   uint32_t* out = reinterpret_cast<uint32_t*>(strips + (size_t)j * FT_STRIP);
   for (int u = tid; u < FT_STRIP / 4; u += 128) {  // two elements per u32
-    const int e = u >> 5, r = (u >> 2) & 7, i0 = 2 * (u & 3);
-    const int y0 = 303 - (8 * e + r + i0), y1 = y0 - 1;
-    const uint32_t lo = (y0 >= 0 && y0 < N162) ? dense[y0] : 0u;
-    const uint32_t hi = (y1 >= 0 && y1 < N162) ? dense[y1] : 0u;
-    out[u] = lo | (hi << 16);
+    const int high = u >= FT_RCORES * 32, uu = high ? u - FT_RCORES * 32 : u;
+    const int e = uu >> 5, r = (uu >> 2) & 7, c0 = 2 * (uu & 3);
+    uint32_t h[2];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      const int d = (high ? 161 : 80) - (8 * e + r + c0 + t);
+      const float f = high ? C(d) + C(d + 81) : C(d) - C(d + 162) - C(d + 243);
+      h[t] = __float_as_uint(f) >> 16;
+    }
+    out[u] = h[0] | (h[1] << 16);
   }
 }
 
@@ -356,13 +371,12 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
     }
     tc::mbar_init_fence();
   }
-  if (warp == 0) tc::tmem_alloc(tslot, 512);
+  if (warp == 0) tc::tmem_alloc(tslot, 256);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
-  const uint32_t id160 = tc::idesc_bf16_f32(128, 160) | (1u << 16);  // B MN-major
-  const uint32_t id144 = tc::idesc_bf16_f32(128, 144) | (1u << 16);
+  const uint32_t id96 = tc::idesc_bf16_f32(128, FT_N) | (1u << 16);  // B MN-major
 
   // Producers (warps 1-16) and the issuer (lane 0 of warp 0) meet only at the stage barriers: a
   // producer waits for done[s] (the MMAs that read stage s three columns ago), fills it and arrives
@@ -417,8 +431,8 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
       for (int kk = 0; kk < 8; ++kk) {
         const uint64_t ad = tc::sdesc(a0 + kk * 256, 128, 2048);
         const uint32_t acc = (it | kk) ? 1u : 0u;
-        tc::mma_bf16(tbase, ad, tc::sdesc(b0 + (2 * kk) * 128, 128, 128), id160, acc);
-        tc::mma_bf16(tbase + 160, ad, tc::sdesc(b0 + (2 * kk + 20) * 128, 128, 128), id144, acc);
+        tc::mma_bf16(tbase, ad, tc::sdesc(b0 + (2 * kk) * 128, 128, 128), id96, acc);
+        tc::mma_bf16(tbase + FT_N, ad, tc::sdesc(b0 + (FT_RCORES + 2 * kk) * 128, 128, 128), id96, acc);
       }
       tc::mma_commit(&done[s]);
       last = it;
@@ -438,30 +452,22 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   }
   ok = __syncthreads_and(ok);
   tc::fence_after_sync();
-  // Ring reduction per row into shared memory (the stages are free now): fin[row][i], i < 162.
+  // The coefficients per row into shared memory (the stages are free now): fin[row][i], i < 162.
   int32_t* fin = reinterpret_cast<int32_t*>(fsm);
   const int FS = N162 + 1;
   if (tid < 128)
     for (int i = 0; i < N162; ++i) fin[tid * FS + i] = 0;
   if (ok && ncols > 0 && tid < 128) {  // warps 0-3: TMEM lanes 32 w .. 32 w + 31 = the block's rows
 #pragma unroll 1
-    for (int n0 = 0; n0 < 304; n0 += 16) {
+    for (int n0 = 0; n0 < 2 * FT_N; n0 += 16) {
       uint32_t v[16];
       tc::tmem_ld_x16(tbase + ((uint32_t)(32 * warp) << 16) + n0, v);
       tc::tmem_wait_ld(v);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int y = 303 - (n0 + i);
-        if (y >= RAW_Y) continue;
-        const int32_t raw = (int32_t)__float2int_rn(__uint_as_float(v[i]));
-        if (y < N162) {
-          fin[tid * FS + y] += raw;
-        } else if (y < N162 + 81) {
-          fin[tid * FS + y - 81] += raw;
-          fin[tid * FS + y - N162] -= raw;
-        } else {
-          fin[tid * FS + y - 243] -= raw;
-        }
+      for (int t = 0; t < 16; ++t) {
+        const int n = n0 + t, high = n >= FT_N, nn = high ? n - FT_N : n;
+        if (nn >= 81) continue;  // padding columns of a range
+        fin[tid * FS + (high ? 161 - nn : 80 - nn)] = (int32_t)__float2int_rn(__uint_as_float(v[t]));
       }
     }
   }
@@ -481,7 +487,7 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 0) tc::tmem_dealloc(tbase, 512);
+  if (warp == 0) tc::tmem_dealloc(tbase, 256);
 }
 
 // out = sum over the column runs; every coefficient must fit the wire's i16 range (status 2).
