@@ -672,6 +672,31 @@ int touch_proof_buffer(lf_ctx* ctx, uint8_t* proof, size_t len, cudaEvent_t* rea
   return LF_OK;
 }
 
+// A switch round's message: the round's last block writes the six words into msg_out and then
+// sets msg_out[7] (system-scope release). arm_round_message clears the flag before the launch;
+// read_round_message spins on it and reads the message as soon as it lands, which saves the
+// kernel's and the stream's completion on each of the host's Fiat-Shamir round trips. The spin
+// asks the stream every few thousand tries: once the stream has finished (or failed) without the
+// flag, the stream's own status decides, so a failed launch never leaves the host spinning.
+void arm_round_message(lf_ctx* ctx) {
+  __atomic_store_n(ctx->msg_out + 7, 0ull, __ATOMIC_SEQ_CST);
+}
+
+cudaError_t read_round_message(lf_ctx* ctx, cudaStream_t st, f162 m[2]) {
+  for (unsigned tries = 1;; ++tries) {
+    if (__atomic_load_n(ctx->msg_out + 7, __ATOMIC_ACQUIRE)) {
+      memcpy(m, ctx->msg_out, 48);
+      return cudaSuccess;
+    }
+    if ((tries & 4095) == 0 && cudaStreamQuery(st) != cudaErrorNotReady) break;
+  }
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  if (!__atomic_load_n(ctx->msg_out + 7, __ATOMIC_ACQUIRE)) return cudaErrorUnknown;
+  memcpy(m, ctx->msg_out, 48);
+  return cudaSuccess;
+}
+
 // table_ready (may be null): an event the prover's stream waits for before the first kernel that
 // reads the table. With ts, the commitment starts before the table is complete (table_ready is
 // then unused). touch: `proof` is host memory that may need touch_proof_buffer (done while the
@@ -792,11 +817,11 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   ++launches;
   for (int r = 0; r < HB; ++r) {
     const uint64_t X = 1ull << r;
+    arm_round_message(ctx);
     launch_switch_round_blocks(R[HB - 1 - r], X, hi[r], PSI[cur], W[cur],
                                ctx->msg.as<unsigned long long>(), ctx->msg_out_dev, ctx->sms, st);
     f162 m[2];
-    CK(cudaStreamSynchronize(st));
-    memcpy(m, ctx->msg_out, 48);
+    CK(read_round_message(ctx, st, m));
     t.absorb_f162(m, 2);
     f162 rr = t.sample_f162("switch-round", 1)[0];
     rounds.push_back(m[0]);
@@ -820,22 +845,24 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   // round's message (the last fold alone).
   uint64_t half = nsmall >> 1;
   if (HB < sh.lp) {
+    arm_round_message(ctx);
     launch_switch_msg(A, P, half, ctx->msg.as<unsigned long long>(), ctx->msg_out_dev, ctx->sms, st);
     ++launches;
   }
   for (int r = HB; r < sh.lp; ++r, half >>= 1) {
     f162 m[2];
-    CK(cudaStreamSynchronize(st));
-    memcpy(m, ctx->msg_out, 48);
+    CK(read_round_message(ctx, st, m));
     t.absorb_f162(m, 2);
     f162 rr = t.sample_f162("switch-round", 1)[0];
     rounds.push_back(m[0]);
     rounds.push_back(m[1]);
     coords.push_back(rr);
-    if (r + 1 < sh.lp)
+    if (r + 1 < sh.lp) {
+      arm_round_message(ctx);
       launch_switch_fold_msg(A, P, half, rr, ctx->msg.as<unsigned long long>(), ctx->msg_out_dev, ctx->sms, st);
-    else
+    } else {
       launch_switch_fold(A, P, half, rr, ctx->sms, st);
+    }
     ++launches;
   }
   CKL("switch rounds");

@@ -230,19 +230,29 @@ __device__ __forceinline__ f162 shfl_xor_f162(f162 v, int m) {
 
 // A round message's blocks XOR their shares into msg[0..5] (device) and count themselves in
 // msg[6]; the last block to arrive forwards the message to `out` (host memory the device writes
-// through) and clears msg for the next round, so a round needs no separate clear or copy. Called
-// by every thread of the block after its shares were added; no block waits for another.
+// through) and clears msg for the next round, so a round needs no separate clear or copy. After
+// the six words it sets out[7] to 1 with a system-scope release, so the host, which cleared
+// out[7] before the launch, can read the message as soon as the flag lands instead of waiting
+// for the kernel and the stream to complete. Called by every thread of the block after its
+// shares were added; no block waits for another.
 __device__ __forceinline__ void msg_forward(unsigned long long* msg, unsigned long long* out) {
   __shared__ bool last;
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) last = atomicAdd(msg + 6, 1ull) == (unsigned long long)gridDim.x - 1;
   __syncthreads();
-  if (last && threadIdx.x < 6) {
-    __threadfence();
-    out[threadIdx.x] = atomicExch(msg + threadIdx.x, 0ull);
+  if (last && threadIdx.x < 32) {
+    if (threadIdx.x < 6) {
+      __threadfence();
+      out[threadIdx.x] = atomicExch(msg + threadIdx.x, 0ull);
+      __threadfence_system();
+    }
+    __syncwarp();
+    if (threadIdx.x == 0) {
+      msg[6] = 0;
+      asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(out + 7), "l"(1ull) : "memory");
+    }
   }
-  if (last && threadIdx.x == 0) msg[6] = 0;
 }
 
 // msg = [sum_{j<half} a_j p_j, sum (a_j + a_{j+half})(p_j + p_{j+half})] (sumcheck.rs:128-189)
