@@ -282,13 +282,17 @@ cudaError_t launch_challenges(const void* hasher_dev, uint64_t base_counter, con
 constexpr int FT_RCORES = 28;                   // cores per range strip (k groups 0..15 + n groups 0..11)
 constexpr int FT_STRIP = 2 * FT_RCORES * 128;   // both ranges' strips of a column: 7168 bytes
 constexpr int FT_N = 96;                        // MMA N per range (81 coefficients used)
-constexpr int FT_TILE = 128 * 128 * 2;          // A tile: 128 words x 128 bits, bf16
-constexpr int FT_STAGES = 3;                    // A tiles (read by the MMAs)
-constexpr int FT_RING = 8;                      // strips and raw words, loaded FT_AHEAD columns early
-constexpr int FT_AHEAD = 3;
-constexpr int FT_PRODUCERS = 512;                // four per table word (a quarter each): warps 1-16
-constexpr int FT_THREADS = FT_PRODUCERS + 32;   // warp 0 issues the MMAs
-constexpr int FT_SMEM = FT_RING * FT_STRIP + FT_STAGES * FT_TILE + FT_RING * FT_PRODUCERS * 16 + 128;
+constexpr int FT_WORDS = 128 * 16;              // a column's 128 table words of the block: 2048 bytes
+constexpr int FT_SLOT = FT_STRIP + FT_WORDS;    // one column's bulk copies
+constexpr int FT_STAGES = 4;                    // A stages in tensor memory, 64 columns each
+constexpr int FT_RING = 12;                     // column slots: the loader runs up to 12 columns ahead
+constexpr int FT_PRODUCERS = 512;               // four groups of 128 (a word each): warps 3-18
+constexpr int FT_THREADS = FT_PRODUCERS + 96;   // warps 0 and 1 issue the MMAs, lane 0 of warp 2 loads
+constexpr int FT_FIN = 128 * (N162 + 1) * 4;    // the epilogue's coefficients per row (reuses the ring)
+constexpr int FT_BARS = FT_RING * FT_SLOT > FT_FIN ? FT_RING * FT_SLOT : FT_FIN;
+// More than half of an SM's shared memory, so one block holds the SM's 512 tensor-memory columns.
+constexpr int FT_SMEM = 120 * 1024;
+static_assert(FT_BARS + (2 * FT_STAGES + 2 * FT_RING) * 8 + 16 <= FT_SMEM, "fold shared memory");
 constexpr long long FT_WAIT_CYCLES = 2000000000LL;
 
 // Strips of column j, low range then high range: core e of a range holds element (r, c) =
@@ -321,120 +325,146 @@ __global__ void __launch_bounds__(128) k_fold_cores(const Challenge* __restrict_
   }
 }
 
-// Word -> row r of an A tile, bits in natural order: u32 s of chunk q holds bits 8q + 2s (low
-// bf16) and 8q + 2s + 1 (high bf16) as 2.0 or 0.
-__device__ __forceinline__ void fold_write_row(uint8_t* tile, int r, uint4 v, int part) {
-  const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
+// A quarter (32 bits) of a table word -> its 16 tensor-memory A columns: column t holds K positions
+// 2t and 2t + 1 (bits 2t and 2t + 1 of x, natural order, the Hankel operand's order) as bf16 2.0
+// (0x4000) or 0. Per 16-bit half, y = even bits in place | odd bits moved up 15, so one shift and
+// one mask give a column.
+__device__ __forceinline__ void fold_expand_quarter(uint32_t x, uint32_t (&u)[16]) {
 #pragma unroll
-  for (int qq = 0; qq < 16 * 128 / FT_PRODUCERS; ++qq) {
-    const int q = 16 * 128 / FT_PRODUCERS * part + qq;  // this thread's share of the word's 16 chunks
-    const uint32_t x = xs[q >> 2];
-    uint32_t u[4];
+  for (int h = 0; h < 2; ++h) {
+    const uint32_t z = h ? x >> 16 : x & 0xFFFFu;
+    const uint32_t y = (z & 0x5555u) | ((z & 0xAAAAu) << 15);
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-      const int b0 = 8 * (q & 3) + 2 * t;  // bit of x for the low half; b0 + 1 for the high half
-      const uint32_t lo = b0 <= 14 ? x << (14 - b0) : x >> (b0 - 14);
-      const uint32_t hi = b0 <= 29 ? x << (29 - b0) : x >> (b0 - 29);
-      u[t] = (lo & 0x4000u) | (hi & 0x40000000u);
-    }
-    *reinterpret_cast<uint4*>(tile + (r >> 3) * 2048 + q * 128 + (r & 7) * 16) = make_uint4(u[0], u[1], u[2], u[3]);
+    for (int t = 0; t < 8; ++t) u[8 * h + t] = (y << (14 - 2 * t)) & 0x40004000u;
   }
 }
 
 // Block = 128 table words (32 ring elements) x a run of columns; out: part[split][m][4 y + k]
 // for the block's elements, the column run's share of the fold.
+//
+// Tensor memory (512 columns): D = columns 0..191 (two ranges of N = 96), A stages s = 0..3 at
+// 256 + 64 s (a column's 128 words, K = 128 bits, read by the MMAs from tensor memory, so the
+// shared-memory port carries only the strips). Roles, meeting on mbarriers:
+//   lane 0 of warp 2 (loader): per column, once the MMAs of the column that used the slot RING
+//     columns earlier are done (sfree), two bulk copies into slot c % RING (the column's strips,
+//     7168 bytes, and the block's 128 words, 2048 bytes) completing on wfull[slot];
+//   warps 3-18 (producers; warp w holds tensor-memory lanes 32 (w % 4) .. +31 = words, and group
+//     g = (w - 3) / 4 takes the columns it = g mod 4, so stage g): per column wait until the stage is
+//     free (done[g] of the group's previous column) and the words landed, expand the words with
+//     tcgen05.st, arrive full[g]. Four groups keep four columns' expansions in flight, so the
+//     latency of one (barrier waits, tensor-memory stores) is not on the tensor core's path;
+//   lane 0 of warp r (issuer of range r = 0, 1): per column wait full[s], issue the range's 8 MMAs
+//     (A from tensor memory, B = the range's strip through the Hankel descriptor), commit to done[s]
+//     and sfree[slot] (both count the two issuers). One thread issues an MMA of this size only
+//     about every 60 cycles, close to the tensor core's time for it, so each range has its own.
+// Every wait is bounded; a timeout sets *status = 5 and the abort flag, on which every role leaves
+// its loop. The loader waits for its own copies in flight before the block reuses the ring, and
+// tensor memory is freed only after the issuer's last commit drained.
 __global__ void __launch_bounds__(FT_THREADS, 1)
-    k_fold_tc(const uint4* __restrict__ table, int rl, uint64_t ring_elements, const uint4* __restrict__ strips,
+    k_fold_tc(const uint4* __restrict__ table, int rl, uint64_t ring_elements, const uint8_t* __restrict__ strips,
               int cols_per_split, int32_t* __restrict__ part, int* status) {
   extern __shared__ __align__(1024) uint8_t fsm[];
-  uint8_t* sS = fsm;                                   // [FT_RING][FT_STRIP] (first: reads past a strip stay in smem)
-  uint8_t* sA = fsm + FT_RING * FT_STRIP;              // [FT_STAGES][FT_TILE]
-  uint4* sW = reinterpret_cast<uint4*>(sA + FT_STAGES * FT_TILE);  // [FT_RING][FT_PRODUCERS] raw words
-  uint64_t* done = reinterpret_cast<uint64_t*>(sW + FT_RING * FT_PRODUCERS);  // [FT_STAGES] MMAs of a stage done
-  uint64_t* full = done + FT_STAGES;                                            // [FT_STAGES] a stage written
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(full + FT_STAGES);
+  uint8_t* ring = fsm;                                                  // [FT_RING][FT_SLOT]: strips, words
+  uint64_t* done = reinterpret_cast<uint64_t*>(fsm + FT_BARS);          // [FT_STAGES] MMAs of a stage done
+  uint64_t* full = done + FT_STAGES;                                    // [FT_STAGES] a stage written
+  uint64_t* wfull = full + FT_STAGES;                                   // [FT_RING] a slot's copies landed
+  uint64_t* sfree = wfull + FT_RING;                                    // [FT_RING] a slot's MMAs done
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sfree + FT_RING);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const bool producer = warp >= 1;
-  const int ptid = tid - 32;                          // producer index
-  const int row = ptid & 127, quarter = ptid >> 7;    // the word (A row) and which quarter of it
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool producer = warp >= 3;
+  const int row = 32 * (warp & 3) + lane, group = (warp - 3) >> 2;  // producers: word (A row), group
   const uint64_t words = 4 * ring_elements;
   const uint64_t w0 = (uint64_t)blockIdx.x * 128;  // first word (row) of the block
+  const int nw = (int)min((uint64_t)128, words - w0);
   const int split = blockIdx.y;
   const int c_begin = split * cols_per_split, c_end = min(COLUMNS, c_begin + cols_per_split);
-  const bool live = producer && w0 + row < words;
+  const int ncols = c_end - c_begin;
   if (tid == 0) {
     *abort_flag = 0;
     for (int i = 0; i < FT_STAGES; ++i) {
-      tc::mbar_init(&done[i], 1);
-      tc::mbar_init(&full[i], FT_PRODUCERS);
+      tc::mbar_init(&done[i], 2);
+      tc::mbar_init(&full[i], FT_PRODUCERS / FT_STAGES);
+    }
+    for (int i = 0; i < FT_RING; ++i) {
+      tc::mbar_init(&wfull[i], 1);
+      tc::mbar_init(&sfree[i], 2);
     }
     tc::mbar_init_fence();
   }
-  if (warp == 0) tc::tmem_alloc(tslot, 256);
+  if (warp == 0) tc::tmem_alloc(tslot, 512);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
   const uint32_t id96 = tc::idesc_bf16_f32(128, FT_N) | (1u << 16);  // B MN-major
+  auto give_up = [&]() {
+    if (!*abort_flag) {
+      *abort_flag = 1;
+      atomicExch(status, 5);
+    }
+  };
 
-  // Producers (warps 1-16) and the issuer (lane 0 of warp 0) meet only at the stage barriers: a
-  // producer waits for done[s] (the MMAs that read stage s three columns ago), fills it and arrives
-  // on full[s]; the issuer waits for full[s] and issues the column's MMAs, committing to done[s].
-  // So the expansion runs up to FT_STAGES columns ahead of the tensor core. Every wait is bounded
-  // and gives up at once after an abort; producers keep arriving so no phase is skipped.
   int last = -1;
   if (producer) {
-    // Column c's strip and this thread's word go to ring slot c % FT_RING, one commit group per
-    // column (empty past the run), FT_AHEAD columns before they are used.
-    auto fetch = [&](int c) {
-      if (c < c_end) {
-        const int slot = (c - c_begin) % FT_RING;
-        const uint4* src = strips + (size_t)c * (FT_STRIP / 16);
-        for (int i = ptid; i < FT_STRIP / 16; i += FT_PRODUCERS) tc::cp_async16(sS + slot * FT_STRIP + 16 * i, src + i);
-        if (live) tc::cp_async16(sW + slot * FT_PRODUCERS + ptid, table + ((uint64_t)c << rl) + w0 + row);
-      }
-      tc::cp_async_commit();
-    };
-    for (int a = 0; a < FT_AHEAD; ++a) fetch(c_begin + a);
-    for (int c = c_begin; c < c_end; ++c) {
-      const int it = c - c_begin, s = it % FT_STAGES, slot = it % FT_RING;
-      // A stage s was read by the MMAs of column it - FT_STAGES; the strip slot that fetch() is
-      // about to fill was read by those of it + FT_AHEAD - FT_RING, which are older.
-      if (it >= FT_STAGES) {
-        const bool r = tc::mbar_wait(&done[s], ((it / FT_STAGES) - 1) & 1, abort_flag, FT_WAIT_CYCLES);
-        if (!__all_sync(0xffffffffu, r) && !*abort_flag) {
-          *abort_flag = 1;
-          atomicExch(status, 5);
+    const int s = group;
+    const uint32_t tA = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + 256 + 64 * s;
+    for (int it = group; it < ncols; it += FT_STAGES) {
+      const int slot = it % FT_RING;
+      bool ok = it < FT_STAGES || tc::mbar_wait(&done[s], ((it / FT_STAGES) - 1) & 1, abort_flag, FT_WAIT_CYCLES);
+      ok = ok && tc::mbar_wait(&wfull[slot], (it / FT_RING) & 1, abort_flag, FT_WAIT_CYCLES);
+      if (!__all_sync(0xffffffffu, ok)) give_up();
+      if (!*abort_flag) {
+        tc::fence_after_sync();
+        const uint4 v = row < nw ? reinterpret_cast<const uint4*>(ring + slot * FT_SLOT + FT_STRIP)[row]
+                                 : make_uint4(0, 0, 0, 0);
+        const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          uint32_t u[16];
+          fold_expand_quarter(xs[q], u);
+          tc::tmem_st_x16(tA + 16 * q, u);
         }
+        tc::tmem_wait_st();
       }
-      fetch(c + FT_AHEAD);
-      tc::cp_async_wait<FT_AHEAD>();  // column c's group has landed
-      if (!*abort_flag)
-        fold_write_row(sA + s * FT_TILE, row, live ? sW[slot * FT_PRODUCERS + ptid] : make_uint4(0, 0, 0, 0),
-                       quarter);
-      tc::fence_proxy_async();
+      tc::fence_before_sync();
       tc::mbar_arrive(&full[s]);
     }
-    tc::cp_async_wait<0>();
-  } else if (tid == 0) {
-    for (int c = c_begin; c < c_end; ++c) {
-      const int it = c - c_begin, s = it % FT_STAGES, slot = it % FT_RING;
-      if (!tc::mbar_wait(&full[s], (it / FT_STAGES) & 1, abort_flag, FT_WAIT_CYCLES) && !*abort_flag) {
-        *abort_flag = 1;
-        atomicExch(status, 5);
+  } else if (tid == 64) {  // loader
+    int issued = 0;
+    for (int it = 0; it < ncols && !*abort_flag; ++it, ++issued) {
+      const int slot = it % FT_RING;
+      if (it >= FT_RING && !tc::mbar_wait(&sfree[slot], ((it / FT_RING) - 1) & 1, abort_flag, FT_WAIT_CYCLES)) {
+        give_up();
+        break;
       }
-      if (*abort_flag) continue;
+      const int c = c_begin + it;
+      uint8_t* dst = ring + slot * FT_SLOT;
+      tc::mbar_expect_tx(&wfull[slot], FT_STRIP + 16 * nw);
+      tc::bulk_load(dst, strips + (size_t)c * FT_STRIP, FT_STRIP, &wfull[slot]);
+      tc::bulk_load(dst + FT_STRIP, table + ((uint64_t)c << rl) + w0, 16 * nw, &wfull[slot]);
+    }
+    // the copies in flight land before the block leaves or reuses the ring
+    for (int it = issued > FT_RING ? issued - FT_RING : 0; it < issued; ++it) {
+      const long long t0 = clock64();
+      while (!tc::mbar_try_wait(&wfull[it % FT_RING], (it / FT_RING) & 1) && clock64() - t0 < FT_WAIT_CYCLES) {
+      }
+    }
+  } else if (lane == 0) {  // issuer of range warp (0: low, 1: high)
+    const uint32_t d = tbase + FT_N * warp, boff = FT_RCORES * 128 * warp;
+    for (int it = 0; it < ncols; ++it) {
+      const int s = it % FT_STAGES, slot = it % FT_RING;
+      if (!tc::mbar_wait(&full[s], (it / FT_STAGES) & 1, abort_flag, FT_WAIT_CYCLES) ||
+          !tc::mbar_wait_fast(&wfull[slot], (it / FT_RING) & 1, abort_flag, FT_WAIT_CYCLES))
+        give_up();
+      if (*abort_flag) break;
       tc::fence_after_sync();
-      const uint32_t a0 = tc::smem_u32(sA + s * FT_TILE), b0 = tc::smem_u32(sS + slot * FT_STRIP);
+      const uint32_t a0 = tbase + 256 + 64 * s, b0 = tc::smem_u32(ring + slot * FT_SLOT) + boff;
 #pragma unroll
-      for (int kk = 0; kk < 8; ++kk) {
-        const uint64_t ad = tc::sdesc(a0 + kk * 256, 128, 2048);
-        const uint32_t acc = (it | kk) ? 1u : 0u;
-        tc::mma_bf16(tbase, ad, tc::sdesc(b0 + (2 * kk) * 128, 128, 128), id96, acc);
-        tc::mma_bf16(tbase + FT_N, ad, tc::sdesc(b0 + (FT_RCORES + 2 * kk) * 128, 128, 128), id96, acc);
-      }
+      for (int kk = 0; kk < 8; ++kk)
+        tc::mma_bf16_ta(d, a0 + 8 * kk, tc::sdesc(b0 + (2 * kk) * 128, 128, 128), id96, (it | kk) ? 1u : 0u);
       tc::mma_commit(&done[s]);
+      tc::mma_commit(&sfree[slot]);
       last = it;
     }
     if (last >= 0) {  // drain: the last commit covers every MMA
@@ -443,7 +473,6 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
       }
     }
   }
-  const int ncols = c_end - c_begin;
   bool ok = !*abort_flag;
   if (ok && ncols > 0) {
     const int lt = ncols - 1;
@@ -452,7 +481,7 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   }
   ok = __syncthreads_and(ok);
   tc::fence_after_sync();
-  // The coefficients per row into shared memory (the stages are free now): fin[row][i], i < 162.
+  // The coefficients per row into shared memory (the ring is free now): fin[row][i], i < 162.
   int32_t* fin = reinterpret_cast<int32_t*>(fsm);
   const int FS = N162 + 1;
   if (tid < 128)
@@ -487,7 +516,7 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 0) tc::tmem_dealloc(tbase, 256);
+  if (warp == 0) tc::tmem_dealloc(tbase, 512);
 }
 
 // out = sum over the column runs; every coefficient must fit the wire's i16 range (status 2).
@@ -521,8 +550,7 @@ void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Chall
   k_fold_cores<<<COLUMNS, 128, 0, s>>>(ch, strips);
   const unsigned blocks = (unsigned)((4 * ring_elements + 127) / 128);
   const int per = (COLUMNS + splits - 1) / splits;
-  k_fold_tc<<<dim3(blocks, splits), FT_THREADS, FT_SMEM, s>>>(table, rl, ring_elements,
-                                                              reinterpret_cast<const uint4*>(strips), per, part, status);
+  k_fold_tc<<<dim3(blocks, splits), FT_THREADS, FT_SMEM, s>>>(table, rl, ring_elements, strips, per, part, status);
   k_fold_sum<<<1024, 256, 0, s>>>(part, splits, ring_elements * 648, out, status);
 }
 

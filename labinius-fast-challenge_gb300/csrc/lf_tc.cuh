@@ -204,6 +204,20 @@ __device__ __forceinline__ void write_row(uint8_t* tile, int r, uint4 v) {
 // Bit of the word held by position e (0..127) of an expanded row.
 __host__ __device__ constexpr int row_bit(int e) { return 32 * (e >> 5) + ((e >> 1) & 15) + 16 * (e & 1); }
 
+// ---- bulk copies (the tensor memory accelerator, no tensor map) ----
+// The calling thread arrives on `bar` and adds `bytes` to the transactions its phase waits for.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// Copies `bytes` (a multiple of 16; both addresses 16-byte aligned) from global to this CTA's
+// shared memory; the bytes count against the transactions of `bar`'s current phase on arrival.
+__device__ __forceinline__ void bulk_load(void* smem, const void* gmem, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(smem)),
+               "l"(gmem), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
 // ---- cp.async (16 bytes, L2 only) ----
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
