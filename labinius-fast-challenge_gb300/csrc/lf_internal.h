@@ -155,7 +155,7 @@ cudaError_t launch_challenges(const void* hasher_dev, uint64_t base_counter, con
                               const void* phase, Challenge* out, int n, int* status, cudaStream_t s,
                               uint32_t* dbg = nullptr);
 int fold_splits(uint64_t ring_elements, int sms);
-constexpr size_t FOLD_STRIP_BYTES = 2 * 28 * 128;  // per column: the low and the high range's strips
+constexpr size_t FOLD_STRIP_BYTES = 2 * 26 * 128;  // per column: the low and the high range's strips
 void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Challenge* ch, uint8_t* strips,
                  int32_t* part, int splits, int32_t* out, int* status, cudaStream_t s);
 void launch_chunk_cvs(const uint8_t* stream, uint64_t nchunks, const uint32_t key[8], uint32_t mode, uint32_t* cvs,

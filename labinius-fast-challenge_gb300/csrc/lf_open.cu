@@ -273,18 +273,22 @@ cudaError_t launch_challenges(const void* hasher_dev, uint64_t base_counter, con
 //             the last index is at least 162, so one formula serves the whole range)
 //   i >= 81:  coefficient += bit_x * (C_j[d] + C_j[d + 81])
 // Each range is a function of d alone. With n = 80 - i (low range) or n = 161 - i (high range),
-// B[x][n] = f(const - n - x) depends on x + n only, so its 8 x 8 core matrices depend only on
-// (k group + n group): one strip of 28 cores per range and column (k_fold_cores), read through an
-// MN-major descriptor whose k-group and n-group strides are both one core. A = the words expanded
-// to bf16 (2.0 per set bit, bits in natural order, K-major). D = 128 x 192 (two MMAs of N = 96,
-// 81 columns used in each), exact in f32 (integers well inside 2^24).
+// B[x][n] = f(const - n - x) depends on x + n only. The operands are 8-bit floats (e4m3, the
+// tensor cores' kind::f8f6f4 at twice the bf16 rate): every B value is a sum of up to three
+// +-0.5 (0, +-0.5, +-1, +-1.5 are exact in e4m3) and every A value 2.0 or 0, so each product is an
+// exact integer and D sums them exactly in f32. A K-major core matrix of B is 8 rows (n) x 16
+// bytes (x): core (n group g, k group h) holds f(const - (8 g + 16 h + r + c)), a function of
+// e = g + 2 h, so one strip of 26 cores per range and column (k_fold_cores) serves every MMA through
+// a descriptor whose 8-row-group stride is one core and whose K stride is two. A = the words
+// expanded to e4m3 (bits in natural order) in tensor memory. D = 128 x 192 (two MMAs of N = 96 per
+// K = 32, 81 columns used in each), exact in f32 (integers well inside 2^24).
 // ---------------------------------------------------------------------------------------------
-constexpr int FT_RCORES = 28;                   // cores per range strip (k groups 0..15 + n groups 0..11)
-constexpr int FT_STRIP = 2 * FT_RCORES * 128;   // both ranges' strips of a column: 7168 bytes
+constexpr int FT_RCORES = 26;                   // cores per range strip: e = g + 2 h <= 11 + 2 * 7
+constexpr int FT_STRIP = 2 * FT_RCORES * 128;   // both ranges' strips of a column: 6656 bytes
 constexpr int FT_N = 96;                        // MMA N per range (81 coefficients used)
 constexpr int FT_WORDS = 128 * 16;              // a column's 128 table words of the block: 2048 bytes
 constexpr int FT_SLOT = FT_STRIP + FT_WORDS;    // one column's bulk copies
-constexpr int FT_STAGES = 4;                    // A stages in tensor memory, 64 columns each
+constexpr int FT_STAGES = 4;                    // A stages in tensor memory, 32 columns each
 constexpr int FT_RING = 12;                     // column slots: the loader runs up to 12 columns ahead
 constexpr int FT_PRODUCERS = 512;               // four groups of 128 (a word each): warps 3-18
 constexpr int FT_THREADS = FT_PRODUCERS + 96;   // warps 0 and 1 issue the MMAs, lane 0 of warp 2 loads
@@ -295,9 +299,16 @@ constexpr int FT_SMEM = 120 * 1024;
 static_assert(FT_BARS + (2 * FT_STAGES + 2 * FT_RING) * 8 + 16 <= FT_SMEM, "fold shared memory");
 constexpr long long FT_WAIT_CYCLES = 2000000000LL;
 
-// Strips of column j, low range then high range: core e of a range holds element (r, c) =
-// f(const - (8 e + r + c)) / 2 as bf16, with f and const of the range (80 and the three-term
-// difference below i = 81, 161 and the two-term sum above); sums of up to three +-0.5 are exact.
+// e4m3 code of a sum of up to three +-0.5: 0, +-0.5 (0x30), +-1 (0x38) or +-1.5 (0x3C).
+__device__ __forceinline__ uint32_t e4m3_halves(float f) {
+  const float a = fabsf(f);
+  const uint32_t m = a == 0.5f ? 0x30u : a == 1.0f ? 0x38u : a == 1.5f ? 0x3Cu : 0u;
+  return m | (f < 0.0f && m ? 0x80u : 0u);
+}
+
+// Strips of column j, low range then high range: byte (r, c) of core e of a range (row r, byte c)
+// holds f(const - (8 e + r + c)) in e4m3, with f and const of the range (80 and the three-term
+// difference below i = 81, 161 and the two-term sum above) and the challenge's values +-0.5.
 __global__ void __launch_bounds__(128) k_fold_cores(const Challenge* __restrict__ ch, uint8_t* __restrict__ strips) {
   __shared__ float dense[N162];
   const int j = blockIdx.x, tid = threadIdx.x;
@@ -311,49 +322,47 @@ __global__ void __launch_bounds__(128) k_fold_cores(const Challenge* __restrict_
   __syncthreads();
   auto C = [&](int z) { return (z >= 0 && z < N162) ? dense[z] : 0.0f; };
   uint32_t* out = reinterpret_cast<uint32_t*>(strips + (size_t)j * FT_STRIP);
-  for (int u = tid; u < FT_STRIP / 4; u += 128) {  // two elements per u32
+  for (int u = tid; u < FT_STRIP / 4; u += 128) {  // four elements per u32
     const int high = u >= FT_RCORES * 32, uu = high ? u - FT_RCORES * 32 : u;
-    const int e = uu >> 5, r = (uu >> 2) & 7, c0 = 2 * (uu & 3);
-    uint32_t h[2];
+    const int e = uu >> 5, r = (uu >> 2) & 7, c0 = 4 * (uu & 3);
+    uint32_t w = 0;
 #pragma unroll
-    for (int t = 0; t < 2; ++t) {
+    for (int t = 0; t < 4; ++t) {
       const int d = (high ? 161 : 80) - (8 * e + r + c0 + t);
       const float f = high ? C(d) + C(d + 81) : C(d) - C(d + 162) - C(d + 243);
-      h[t] = __float_as_uint(f) >> 16;
+      w |= e4m3_halves(f) << (8 * t);
     }
-    out[u] = h[0] | (h[1] << 16);
+    out[u] = w;
   }
 }
 
-// A quarter (32 bits) of a table word -> its 16 tensor-memory A columns: column t holds K positions
-// 2t and 2t + 1 (bits 2t and 2t + 1 of x, natural order, the Hankel operand's order) as bf16 2.0
-// (0x4000) or 0. Per 16-bit half, y = even bits in place | odd bits moved up 15, so one shift and
-// one mask give a column.
-__device__ __forceinline__ void fold_expand_quarter(uint32_t x, uint32_t (&u)[16]) {
+// A table word -> its 32 tensor-memory A columns: column o holds K positions 4 o .. 4 o + 3 (bits
+// 4 o .. 4 o + 3 of the word, natural order, the Hankel operand's order), byte i = e4m3 2.0 (0x40)
+// when bit 4 o + i is set. The nibble times 0x08102040 puts its bits at 6, 14, 22 and 30 (the four
+// shifted copies do not overlap, so nothing carries).
+__device__ __forceinline__ void fold_expand_word(uint4 v, uint32_t (&u)[32]) {
+  const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const uint32_t z = h ? x >> 16 : x & 0xFFFFu;
-    const uint32_t y = (z & 0x5555u) | ((z & 0xAAAAu) << 15);
+  for (int q = 0; q < 4; ++q)
 #pragma unroll
-    for (int t = 0; t < 8; ++t) u[8 * h + t] = (y << (14 - 2 * t)) & 0x40004000u;
-  }
+    for (int t = 0; t < 8; ++t) u[8 * q + t] = (((xs[q] >> (4 * t)) & 0xFu) * 0x08102040u) & 0x40404040u;
 }
 
 // Block = 128 table words (32 ring elements) x a run of columns; out: part[split][m][4 y + k]
 // for the block's elements, the column run's share of the fold.
 //
 // Tensor memory (512 columns): D = columns 0..191 (two ranges of N = 96), A stages s = 0..3 at
-// 256 + 64 s (a column's 128 words, K = 128 bits, read by the MMAs from tensor memory, so the
-// shared-memory port carries only the strips). Roles, meeting on mbarriers:
+// 256 + 32 s (a column's 128 words, K = 128 bits as e4m3, read by the MMAs from tensor memory, so
+// the shared-memory port carries only the strips). Roles, meeting on mbarriers:
 //   lane 0 of warp 2 (loader): per column, once the MMAs of the column that used the slot RING
 //     columns earlier are done (sfree), two bulk copies into slot c % RING (the column's strips,
-//     7168 bytes, and the block's 128 words, 2048 bytes) completing on wfull[slot];
+//     6656 bytes, and the block's 128 words, 2048 bytes) completing on wfull[slot];
 //   warps 3-18 (producers; warp w holds tensor-memory lanes 32 (w % 4) .. +31 = words, and group
 //     g = (w - 3) / 4 takes the columns it = g mod 4, so stage g): per column wait until the stage is
 //     free (done[g] of the group's previous column) and the words landed, expand the words with
 //     tcgen05.st, arrive full[g]. Four groups keep four columns' expansions in flight, so the
 //     latency of one (barrier waits, tensor-memory stores) is not on the tensor core's path;
-//   lane 0 of warp r (issuer of range r = 0, 1): per column wait full[s], issue the range's 8 MMAs
+//   lane 0 of warp r (issuer of range r = 0, 1): per column wait full[s], issue the range's 4 MMAs
 //     (A from tensor memory, B = the range's strip through the Hankel descriptor), commit to done[s]
 //     and sfree[slot] (both count the two issuers). One thread issues an MMA of this size only
 //     about every 60 cycles, close to the tensor core's time for it, so each range has its own.
@@ -397,7 +406,7 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
-  const uint32_t id96 = tc::idesc_bf16_f32(128, FT_N) | (1u << 16);  // B MN-major
+  const uint32_t id96 = tc::idesc_e4m3_f32(128, FT_N);  // both K-major
   auto give_up = [&]() {
     if (!*abort_flag) {
       *abort_flag = 1;
@@ -408,7 +417,7 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   int last = -1;
   if (producer) {
     const int s = group;
-    const uint32_t tA = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + 256 + 64 * s;
+    const uint32_t tA = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + 256 + 32 * s;
     for (int it = group; it < ncols; it += FT_STAGES) {
       const int slot = it % FT_RING;
       bool ok = it < FT_STAGES || tc::mbar_wait(&done[s], ((it / FT_STAGES) - 1) & 1, abort_flag, FT_WAIT_CYCLES);
@@ -418,13 +427,10 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
         tc::fence_after_sync();
         const uint4 v = row < nw ? reinterpret_cast<const uint4*>(ring + slot * FT_SLOT + FT_STRIP)[row]
                                  : make_uint4(0, 0, 0, 0);
-        const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          uint32_t u[16];
-          fold_expand_quarter(xs[q], u);
-          tc::tmem_st_x16(tA + 16 * q, u);
-        }
+        uint32_t u[32];
+        fold_expand_word(v, u);
+        tc::tmem_st_x16(tA, *reinterpret_cast<const uint32_t(*)[16]>(u));
+        tc::tmem_st_x16(tA + 16, *reinterpret_cast<const uint32_t(*)[16]>(u + 16));
         tc::tmem_wait_st();
       }
       tc::fence_before_sync();
@@ -459,10 +465,10 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
         give_up();
       if (*abort_flag) break;
       tc::fence_after_sync();
-      const uint32_t a0 = tbase + 256 + 64 * s, b0 = tc::smem_u32(ring + slot * FT_SLOT) + boff;
+      const uint32_t a0 = tbase + 256 + 32 * s, b0 = tc::smem_u32(ring + slot * FT_SLOT) + boff;
 #pragma unroll
-      for (int kk = 0; kk < 8; ++kk)
-        tc::mma_bf16_ta(d, a0 + 8 * kk, tc::sdesc(b0 + (2 * kk) * 128, 128, 128), id96, (it | kk) ? 1u : 0u);
+      for (int kk = 0; kk < 4; ++kk)  // K = 32 x kk: k groups 2 kk, 2 kk + 1, so core e starts at 4 kk
+        tc::mma_e4m3_ta(d, a0 + 8 * kk, tc::sdesc(b0 + 4 * kk * 128, 256, 128), id96, (it | kk) ? 1u : 0u);
       tc::mma_commit(&done[s]);
       tc::mma_commit(&sfree[slot]);
       last = it;

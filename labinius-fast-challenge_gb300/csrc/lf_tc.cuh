@@ -174,6 +174,23 @@ __device__ __forceinline__ void mma_bf16_ta(uint32_t d_tmem, uint32_t a_tmem, ui
       "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
+// Instruction descriptor, kind::f8f6f4: e4m3 A and B (both K-major), f32 accumulator, M x N.
+__host__ __device__ constexpr uint32_t idesc_e4m3_f32(uint32_t m, uint32_t n) {
+  return (1u << 4) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+// D[tmem] (+)= A[tmem] * B[smem]^T with 8-bit operands, K = 32: A's row i in TMEM lane i, four K
+// elements per 32-bit column (K index 4 o + b in byte b of column o), 8 columns per instruction.
+__device__ __forceinline__ void mma_e4m3_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %3, p;\n"
+      "}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
 // The barrier receives one arrival when every MMA this thread issued before has completed.
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
