@@ -51,44 +51,74 @@ __global__ void k_eq_table_f162(const f162* __restrict__ ps, int n, f162* __rest
 // ---------------------------------------------------------------------------------------------
 // S blocks on the tensor cores: sblk[h][c] (16 bytes, bit b) = parity of
 //   count_h[c][b] = sum_{j < 4096} bit_c(pi0[4096 h + j]) bit_b(E_lo[j]),
-// an exact integer in f32. Both operands are the words expanded to bf16 rows
-// (tc::write_row), read MN-major: row = entry j (K), 128 bit positions along M (table word) or
-// N (E_lo). A block takes two h; the 4096 entries run in 32 k-tiles of 128 through two shared
-// memory stages, so the expansion of tile t + 1 overlaps the MMAs of tile t. Every block expands
-// the tile's E_lo rows itself from the 16-byte entries (2 KB per tile from L2, instead of 32 KB of
-// expanded rows); the words of both operands are loaded two tiles ahead. D for both h sits in TMEM
-// (2 x 128 columns). Set bits are bf16 2.0 in both operands, so D = 4 x count (<= 16384, exact);
-// the count's parity is bit 2 of the f32 mantissa after adding 2^23. Waits are bounded; a
-// timeout sets *status = 4.
+// an exact integer in f32. Operands are 8-bit floats (e4m3, kind::f8f6f4): every word is expanded
+// to a row of 128 bytes, byte i = 2.0 (0x40) when bit i is set, read MN-major (row = entry j = K).
+// A = E_lo's rows (M = b), B = the rows of two blocks h side by side (N = 256: 128 h + c), so one
+// MMA of K = 32 covers both blocks and D = 128 lanes (b) x 256 columns, 4 x count (<= 16384, exact);
+// the count's parity is bit 2 of the f32 mantissa after adding 2^23. The 4096 entries run in 32
+// k-tiles of 128 through four shared-memory stages. Roles, on mbarriers:
+//   lane 0 of warp 1 (loader): per k-tile three bulk copies of 2048 bytes (E_lo's entries and the
+//     two blocks' entries 128 t .. +127) into ring slot t % SBT_RING, completing on wfull[slot],
+//     once the producers have read the slot's previous k-tile (cfree);
+//   warps 2-25 (producers, two groups of 384 threads, one row each: E_lo, block 0, block 1; group g
+//     takes the k-tiles t = g mod 2): wait until stage t % 4 is free (done, the MMAs of k-tile
+//     t - 4) and the words landed, read their word (arrive cfree), expand it, arrive full;
+//   lane 0 of warp 0 (issuer): per k-tile wait full, issue 4 MMAs, commit to done.
+// Epilogue: warps 0-7 read D (lane quarter w % 4, block w / 4) and assemble each c's 128 parity
+// bits with one ballot per 32 b. Every wait is bounded; a timeout sets *status = 4.
 // ---------------------------------------------------------------------------------------------
-constexpr int SBT_PRODUCERS = 256;                           // warps 0-7 expand; warp 8 issues
-constexpr int SBT_THREADS = SBT_PRODUCERS + 32;
-constexpr int SBT_TILE = 128 * 128 * 2;                       // 128 entries x 128 bits, bf16
-constexpr int SBT_SMEM = 2 * SBT_TILE + 2 * 2 * SBT_TILE + 64;  // [B0][B1][A0: 2 h][A1: 2 h][barriers]
+constexpr int SBT_GROUPS = 2;
+constexpr int SBT_ROWS = 3 * 128;                             // a k-tile's rows: E_lo, block 0, block 1
+constexpr int SBT_PRODUCERS = SBT_GROUPS * SBT_ROWS;          // warps 2-25
+constexpr int SBT_THREADS = SBT_PRODUCERS + 64;
+constexpr int SBT_OPA = 128 * 128;                            // E_lo rows: 128 entries x 128 bytes
+constexpr int SBT_STAGE = 3 * SBT_OPA;                        // [A][B: 128 entries x 256 bytes]
+constexpr int SBT_STAGES = 4;
+constexpr int SBT_RING = 4;
+constexpr int SBT_SLOT = 3 * 2048;                            // a k-tile's words: E_lo, block 0, block 1
+constexpr int SBT_BARS = SBT_STAGES * SBT_STAGE + SBT_RING * SBT_SLOT;
+constexpr int SBT_SMEM = SBT_BARS + (2 * SBT_STAGES + 2 * SBT_RING) * 8 + 16;
 constexpr long long SBT_WAIT_CYCLES = 2000000000LL;
+
+// A 128-bit word -> row r of an MN-major e4m3 tile (8-row x 16-byte core matrices, cores adjacent
+// along the row 128 bytes apart, 8-row groups `kstride` apart): byte i = 0x40 when bit i is set.
+__device__ __forceinline__ void sblock_write_row(uint8_t* tile, int r, int kstride, uint4 v) {
+  const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
+  uint8_t* dst = tile + (r >> 3) * kstride + (r & 7) * 16;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {  // bits 16 q .. 16 q + 15 -> core q
+    const uint32_t x = xs[q >> 1] >> (16 * (q & 1));
+    uint32_t u[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) u[t] = (((x >> (4 * t)) & 0xFu) * 0x08102040u) & 0x40404040u;
+    *reinterpret_cast<uint4*>(dst + q * 128) = make_uint4(u[0], u[1], u[2], u[3]);
+  }
+}
 
 __global__ void __launch_bounds__(SBT_THREADS, 1)
     k_sblock_tc(const uint4* __restrict__ table, uint64_t nblocks, const uint4* __restrict__ elo,
                 uint8_t* __restrict__ sblk, int* status) {
   extern __shared__ __align__(1024) uint8_t sbs[];
-  uint8_t* sB = sbs;                  // stage s at sB + s * SBT_TILE (E_lo rows of the k-tile)
-  uint8_t* sA = sbs + 2 * SBT_TILE;   // stage s, block hb at sA + (2 s + hb) * SBT_TILE
-  uint64_t* done = reinterpret_cast<uint64_t*>(sbs + 6 * SBT_TILE);  // [2] MMAs of a stage done
-  uint64_t* full = done + 2;                                          // [2] a stage written
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(full + 2);
+  uint8_t* ring = sbs + SBT_STAGES * SBT_STAGE;                       // [SBT_RING][SBT_SLOT]
+  uint64_t* done = reinterpret_cast<uint64_t*>(sbs + SBT_BARS);      // [SBT_STAGES] MMAs of a stage done
+  uint64_t* full = done + SBT_STAGES;                                 // [SBT_STAGES] a stage written
+  uint64_t* wfull = full + SBT_STAGES;                                // [SBT_RING] a slot's copies landed
+  uint64_t* cfree = wfull + SBT_RING;                                 // [SBT_RING] a slot's words read
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(cfree + SBT_RING);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint64_t h0 = 2 * (uint64_t)blockIdx.x;
-  const int hb = tid >> 7, j = tid & 127;
-  const bool producer = tid < SBT_PRODUCERS;
-  const bool live = producer && h0 + hb < nblocks;
-  const uint4* src = table + (h0 + hb) * 4096 + j;  // entry 128 t + j of block h0 + hb
+  const bool two = h0 + 1 < nblocks;  // the block's second h exists
   if (tid == 0) {
     *abort_flag = 0;
-    tc::mbar_init(&done[0], 1);
-    tc::mbar_init(&done[1], 1);
-    tc::mbar_init(&full[0], SBT_PRODUCERS);
-    tc::mbar_init(&full[1], SBT_PRODUCERS);
+    for (int i = 0; i < SBT_STAGES; ++i) {
+      tc::mbar_init(&done[i], 1);
+      tc::mbar_init(&full[i], SBT_ROWS);
+    }
+    for (int i = 0; i < SBT_RING; ++i) {
+      tc::mbar_init(&wfull[i], 1);
+      tc::mbar_init(&cfree[i], SBT_ROWS);
+    }
     tc::mbar_init_fence();
   }
   if (warp == 0) tc::tmem_alloc(tslot, 256);
@@ -96,94 +126,111 @@ __global__ void __launch_bounds__(SBT_THREADS, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
-  const uint32_t idesc = tc::idesc_bf16_f32(128, 128) | (1u << 15) | (1u << 16);  // A and B MN-major
-  auto wait_all = [&](uint64_t* bar, uint32_t parity) {
-    const bool r = tc::mbar_wait(bar, parity, abort_flag, SBT_WAIT_CYCLES);
-    return __all_sync(0xffffffffu, r);
+  // A and B MN-major, M = 128, N = 256
+  const uint32_t idesc = tc::idesc_e4m3_f32(128, 256) | (1u << 15) | (1u << 16);
+  auto give_up = [&]() {
+    if (!*abort_flag) {
+      *abort_flag = 1;
+      atomicExch(status, 4);
+    }
   };
 
-  // The k-tile's operands are expanded here from 16-byte words (the block's table entries and the
-  // E_lo entries 128 t .. 128 t + 127, which every block shares from L2); the words are loaded two
-  // k-tiles ahead. Threads 0-127 also expand one E_lo row each. The producers (warps 0-7) and the
-  // issuer (lane 0 of warp 8) meet only at the stage barriers: full[s] once a stage is written,
-  // done[s] once its MMAs have read it; every wait is bounded and gives up at once after an abort.
   int last = -1;  // k-tile of the issuer's last commit
-  if (producer) {
-    uint4 w = live ? src[0] : make_uint4(0, 0, 0, 0);
-    uint4 w1 = live ? src[128] : make_uint4(0, 0, 0, 0);
-    uint4 e = tid < 128 ? elo[tid] : make_uint4(0, 0, 0, 0);
-    uint4 e1 = tid < 128 ? elo[128 + tid] : make_uint4(0, 0, 0, 0);
-    for (int t = 0; t < 32; ++t) {
-      const int s = t & 1;
-      if (t >= 2 && !wait_all(&done[s], ((t >> 1) - 1) & 1) && !*abort_flag) {
-        *abort_flag = 1;
-        atomicExch(status, 4);
-      }
-      if (!*abort_flag) {
-        tc::write_row(sA + (2 * s + hb) * SBT_TILE, j, w);
-        if (tid < 128) tc::write_row(sB + s * SBT_TILE, tid, e);
-      }
-      w = w1, e = e1;
-      if (t + 2 < 32) {
-        w1 = live ? src[(t + 2) * 128] : make_uint4(0, 0, 0, 0);
-        if (tid < 128) e1 = elo[(t + 2) * 128 + tid];
-      }
+  if (warp >= 2) {
+    const int p = tid - 64, group = p / SBT_ROWS, op = (p % SBT_ROWS) >> 7, j = p & 127;
+    const bool live = op < 2 || two;
+    // E_lo: A tile, 8-row groups 1024 bytes apart; block op - 1: B tile cores 8 (op - 1) .. + 7,
+    // 8-row groups 2048 bytes apart
+    const int kstride = op == 0 ? 1024 : 2048;
+    const int at = op == 0 ? 0 : SBT_OPA + (op - 1) * 8 * 128;
+    for (int t = group; t < 32; t += SBT_GROUPS) {
+      const int s = t % SBT_STAGES, slot = t % SBT_RING;
+      bool ok = t < SBT_STAGES ||
+                tc::mbar_wait(&done[s], ((t / SBT_STAGES) - 1) & 1, abort_flag, SBT_WAIT_CYCLES);
+      ok = ok && tc::mbar_wait(&wfull[slot], (t / SBT_RING) & 1, abort_flag, SBT_WAIT_CYCLES);
+      if (!__all_sync(0xffffffffu, ok)) give_up();
+      const uint4 w = live && !*abort_flag ? reinterpret_cast<const uint4*>(ring + slot * SBT_SLOT)[128 * op + j]
+                                           : make_uint4(0, 0, 0, 0);
+      if (!*abort_flag) sblock_write_row(sbs + s * SBT_STAGE + at, j, kstride, w);
+      // The proxy fence orders this thread's generic accesses before the async proxy's: the stage
+      // writes before the MMAs read them, and the word's read from the ring before the next bulk
+      // copy overwrites it (a release on the barrier alone does not order the copy engine's write;
+      // without the fence a word was at times read after its slot was refilled).
       tc::fence_proxy_async();
+      tc::mbar_arrive(&cfree[slot]);
       tc::mbar_arrive(&full[s]);
     }
-  } else if (tid == SBT_PRODUCERS) {
+  } else if (tid == 32) {  // loader
+    int issued = 0;
+    for (int t = 0; t < 32 && !*abort_flag; ++t, ++issued) {
+      const int slot = t % SBT_RING;
+      if (t >= SBT_RING && !tc::mbar_wait(&cfree[slot], ((t / SBT_RING) - 1) & 1, abort_flag, SBT_WAIT_CYCLES)) {
+        give_up();
+        break;
+      }
+      uint8_t* dst = ring + slot * SBT_SLOT;
+      tc::mbar_expect_tx(&wfull[slot], two ? 3 * 2048 : 2 * 2048);
+      tc::bulk_load(dst, elo + 128 * t, 2048, &wfull[slot]);
+      tc::bulk_load(dst + 2048, table + h0 * 4096 + 128 * t, 2048, &wfull[slot]);
+      if (two) tc::bulk_load(dst + 4096, table + (h0 + 1) * 4096 + 128 * t, 2048, &wfull[slot]);
+    }
+    // the copies in flight land before the block leaves or reuses the ring
+    for (int t = issued > SBT_RING ? issued - SBT_RING : 0; t < issued; ++t) {
+      const long long t0 = clock64();
+      while (!tc::mbar_try_wait(&wfull[t % SBT_RING], (t / SBT_RING) & 1) && clock64() - t0 < SBT_WAIT_CYCLES) {
+      }
+    }
+  } else if (tid == 0) {
     for (int t = 0; t < 32; ++t) {
-      const int s = t & 1;
-      if (!tc::mbar_wait(&full[s], (t >> 1) & 1, abort_flag, SBT_WAIT_CYCLES) && !*abort_flag) {
-        *abort_flag = 1;
-        atomicExch(status, 4);
-      }
-      if (*abort_flag) continue;
+      const int s = t % SBT_STAGES;
+      if (!tc::mbar_wait(&full[s], (t / SBT_STAGES) & 1, abort_flag, SBT_WAIT_CYCLES)) give_up();
+      if (*abort_flag) break;
       tc::fence_after_sync();
-      const uint32_t b0 = tc::smem_u32(sB + s * SBT_TILE);
+      const uint32_t a0 = tc::smem_u32(sbs + s * SBT_STAGE), b0 = a0 + SBT_OPA;
 #pragma unroll
-      for (int h2 = 0; h2 < 2; ++h2) {
-        const uint32_t a0 = tc::smem_u32(sA + (2 * s + h2) * SBT_TILE);
-#pragma unroll
-        for (int kk = 0; kk < 8; ++kk)
-          tc::mma_bf16(tbase + 128 * h2, tc::sdesc(a0 + kk * 4096, 2048, 128), tc::sdesc(b0 + kk * 4096, 2048, 128),
-                       idesc, (t | kk) ? 1u : 0u);
-      }
+      for (int kk = 0; kk < 4; ++kk)  // K = 32: four 8-row groups
+        tc::mma_e4m3(tbase, tc::sdesc(a0 + kk * 4096, 1024, 128), tc::sdesc(b0 + kk * 8192, 2048, 128), idesc,
+                     (t | kk) ? 1u : 0u);
       tc::mma_commit(&done[s]);
       last = t;
     }
     // Drain: the issuer's last commit covers every MMA it issued (also after an abort).
     if (last >= 0) {
       const long long t0 = clock64();
-      while (!tc::mbar_try_wait(&done[last & 1], (last >> 1) & 1) && clock64() - t0 < SBT_WAIT_CYCLES) {
+      while (!tc::mbar_try_wait(&done[last % SBT_STAGES], (last / SBT_STAGES) & 1) &&
+             clock64() - t0 < SBT_WAIT_CYCLES) {
       }
     }
   }
-  // The last commit (k-tile 31, stage 1, its 16th) covers every MMA of the block.
-  bool ok = !*abort_flag && wait_all(&done[1], 1);
+  // The last commit (k-tile 31, stage 3, its 8th) covers every MMA of the block.
+  bool ok = !*abort_flag;
+  if (ok) ok = __all_sync(0xffffffffu, tc::mbar_wait(&done[31 % SBT_STAGES], (31 / SBT_STAGES) & 1, abort_flag,
+                                                     SBT_WAIT_CYCLES));
   ok = __syncthreads_and(ok);
   tc::fence_after_sync();
-  if (ok && producer) {  // warps 0-7: TMEM lanes 32 (w % 4) .. + 31 of block h0 + w / 4
-    const int h2 = warp >> 2, qd = warp & 3;
-    if (h0 + h2 < nblocks) {
-      const int m = 32 * qd + lane, c = tc::row_bit(m);
-      uint32_t out[4] = {0, 0, 0, 0};
+  if (ok && warp < 8) {  // TMEM lanes 32 (w % 4) .. + 31 = bits b, columns 128 (w / 4) + c
+    const int qd = warp & 3, hh = warp >> 2;
+    if (h0 + hh < nblocks) {
+      uint32_t* out = reinterpret_cast<uint32_t*>(sblk + (h0 + hh) * 128 * 16) + qd;
+#pragma unroll 1
+      for (int c0 = 0; c0 < 128; c0 += 32) {
+        uint32_t mine = 0;
 #pragma unroll
-      for (int n0 = 0; n0 < 128; n0 += 16) {
-        uint32_t v[16];
-        tc::tmem_ld_x16(tbase + ((uint32_t)(32 * qd) << 16) + 128 * h2 + n0, v);
-        tc::tmem_wait_ld(v);
+        for (int n0 = 0; n0 < 32; n0 += 16) {
+          uint32_t v[16];
+          tc::tmem_ld_x16(tbase + ((uint32_t)(32 * qd) << 16) + 128 * hh + c0 + n0, v);
+          tc::tmem_wait_ld(v);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const int b = tc::row_bit(n0 + i);
-          // both operands hold set bits as 2.0: D = 4 x count, so the count's parity is bit 2
-          const uint32_t par = (__float_as_uint(__uint_as_float(v[i]) + 8388608.0f) >> 2) & 1u;
-          out[b >> 5] |= par << (b & 31);
+          for (int i = 0; i < 16; ++i) {
+            // both operands hold set bits as 2.0: D = 4 x count, so the count's parity is bit 2
+            const uint32_t bal = __ballot_sync(0xffffffffu, (__float_as_uint(__uint_as_float(v[i]) + 8388608.0f) >> 2) & 1u);
+            if (lane == n0 + i) mine = bal;
+          }
         }
+        out[4 * (c0 + lane)] = mine;  // word qd of c = c0 + lane: bits b = 32 qd + lane'
       }
-      *reinterpret_cast<uint4*>(sblk + ((h0 + h2) * 128 + c) * 16) = make_uint4(out[0], out[1], out[2], out[3]);
     }
-  } else if (tid == 0) {
+  } else if (!ok && tid == 0) {
     atomicExch(status, 4);
   }
   tc::fence_before_sync();
