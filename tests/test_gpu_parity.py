@@ -117,6 +117,25 @@ def test_repeatable(prover, oracle):
     assert prover.prove(seed, table, log_vars) == prover.prove(seed, table, log_vars)
 
 
+@pytest.mark.parametrize("log_vars", [27, 29])
+def test_repeatable_over_several_waves(prover, log_vars):
+    # Grids of several waves of blocks per SM (2^28 bits and up for the partial sums) start their
+    # blocks at staggered times, the schedule under which a missing ordering between a ring slot's
+    # read and its refill once changed the partial sums from one proof to the next: six proofs of
+    # one device table, byte-identical.
+    seed = SEEDS[0]
+    dev = prover.alloc((1 << log_vars) // 8)
+    try:
+        prover.write_table_device(seed, log_vars, dev)
+        proofs = set()
+        for _ in range(6):
+            proof, plen = prover.prove_device(seed, dev, log_vars)
+            proofs.add(bytes(proof[:plen]))
+    finally:
+        prover.free(dev)
+    assert len(proofs) == 1
+
+
 @pytest.mark.parametrize("prefix", [b"", b"lfchk", bytes(range(256)) * 13], ids=["empty", "short", "3328B"])
 def test_device_challenges_match_oracle(prover, oracle, prefix):
     want = oracle.short_challenges("labinius/test/batch", prefix, 64)
