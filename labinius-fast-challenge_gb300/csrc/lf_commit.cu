@@ -631,8 +631,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     for (int e = 0; e < nelem; ++e) {
       int iok = 1;
       if (lane == 0) {
-        iok = tc::mbar_wait(&full[k], e & 1, abort_flag, TC_WAIT_CYCLES) &&
-              (e == 0 || tc::mbar_wait(&dfree[k], (e - 1) & 1, abort_flag, TC_WAIT_CYCLES));
+        iok = tc::mbar_wait_fast(&full[k], e & 1, abort_flag, TC_WAIT_CYCLES) &&
+              (e == 0 || tc::mbar_wait_fast(&dfree[k], (e - 1) & 1, abort_flag, TC_WAIT_CYCLES));
         if (iok) {
           tc::fence_after_sync();
           tc::mma_bf16(st + 64, adesc_c, bdesc_c, idesc, 0u);

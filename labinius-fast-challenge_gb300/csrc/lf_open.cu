@@ -290,13 +290,14 @@ constexpr int FT_WORDS = 128 * 16;              // a column's 128 table words of
 constexpr int FT_SLOT = FT_STRIP + FT_WORDS;    // one column's bulk copies
 constexpr int FT_STAGES = 4;                    // A stages in tensor memory, 32 columns each
 constexpr int FT_RING = 12;                     // column slots: the loader runs up to 12 columns ahead
-constexpr int FT_PRODUCERS = 512;               // four groups of 128 (a word each): warps 3-18
-constexpr int FT_THREADS = FT_PRODUCERS + 96;   // warps 0 and 1 issue the MMAs, lane 0 of warp 2 loads
+constexpr int FT_PRODUCERS = 512;               // four groups of 128 (a word each): warps 5-20
+constexpr int FT_ISSUERS = 4;                   // lane 0 of warps 0-3 issue the MMAs
+constexpr int FT_THREADS = FT_PRODUCERS + 160;  // + the issuers' warps and the loader's (lane 0 of warp 4)
 constexpr int FT_FIN = 128 * (N162 + 1) * 4;    // the epilogue's coefficients per row (reuses the ring)
 constexpr int FT_BARS = FT_RING * FT_SLOT > FT_FIN ? FT_RING * FT_SLOT : FT_FIN;
 // More than half of an SM's shared memory, so one block holds the SM's 512 tensor-memory columns.
 constexpr int FT_SMEM = 120 * 1024;
-static_assert(FT_BARS + (2 * FT_STAGES + 2 * FT_RING) * 8 + 16 <= FT_SMEM, "fold shared memory");
+static_assert(FT_BARS + (FT_STAGES + 2 * FT_RING) * 8 + 16 <= FT_SMEM, "fold shared memory");
 constexpr long long FT_WAIT_CYCLES = 2000000000LL;
 
 // e4m3 code of a sum of up to three +-0.5: 0, +-0.5 (0x30), +-1 (0x38) or +-1.5 (0x3C).
@@ -351,38 +352,37 @@ __device__ __forceinline__ void fold_expand_word(uint4 v, uint32_t (&u)[32]) {
 // Block = 128 table words (32 ring elements) x a run of columns; out: part[split][m][4 y + k]
 // for the block's elements, the column run's share of the fold.
 //
-// Tensor memory (512 columns): D = columns 0..191 (two ranges of N = 96), A stages s = 0..3 at
-// 256 + 32 s (a column's 128 words, K = 128 bits as e4m3, read by the MMAs from tensor memory, so
-// the shared-memory port carries only the strips). Roles, meeting on mbarriers:
-//   lane 0 of warp 2 (loader): per column, once the MMAs of the column that used the slot RING
-//     columns earlier are done (sfree), two bulk copies into slot c % RING (the column's strips,
-//     6656 bytes, and the block's 128 words, 2048 bytes) completing on wfull[slot];
-//   warps 3-18 (producers; warp w holds tensor-memory lanes 32 (w % 4) .. +31 = words, and group
-//     g = (w - 3) / 4 takes the columns it = g mod 4, so stage g): per column wait until the stage is
-//     free (done[g] of the group's previous column) and the words landed, expand the words with
-//     tcgen05.st, arrive full[g]. Four groups keep four columns' expansions in flight, so the
-//     latency of one (barrier waits, tensor-memory stores) is not on the tensor core's path;
-//   lane 0 of warp r (issuer of range r = 0, 1): per column wait full[s], issue the range's 4 MMAs
-//     (A from tensor memory, B = the range's strip through the Hankel descriptor), commit to done[s]
-//     and sfree[slot] (both count the two issuers). One thread issues an MMA of this size only
-//     about every 60 cycles, close to the tensor core's time for it, so each range has its own.
+// Tensor memory (512 columns): D = columns 0..191 (two ranges of N = 96, zeroed before the first
+// MMA), A stages s = 0..3 at 256 + 32 s (a column's 128 words, K = 128 bits as e4m3, read by the
+// MMAs from tensor memory, so the shared-memory port carries only the strips). Roles, meeting on
+// mbarriers:
+//   lane 0 of warp 4 (loader): per column c, once the MMAs of the column that used its ring slot
+//     FT_RING columns earlier are done (done[slot]), two bulk copies into slot c % FT_RING (the
+//     column's strips, 6656 bytes, and the block's 128 words, 2048 bytes) completing on wfull[slot];
+//   warps 5-20 (producers; warp w holds tensor-memory lanes 32 (w % 4) .. +31 = words, and group
+//     g = (w - 5) / 4 takes the columns it = g mod 4, so stage g): per column wait until the stage is
+//     free (done of the group's previous column) and the words landed, expand the words with
+//     tcgen05.st, arrive full[g]. Four groups keep four columns' expansions in flight;
+//   lane 0 of warp i < 4 (issuer of range i % 2, K half i / 2): per column wait full[s], issue its
+//     2 MMAs (A from tensor memory, B = the range's strip through the Hankel descriptor) and commit
+//     to done[slot], which counts the four issuers. One thread issues a tcgen05 operation only
+//     about every 100 cycles, so the column's 8 MMAs come from four threads.
 // Every wait is bounded; a timeout sets *status = 5 and the abort flag, on which every role leaves
 // its loop. The loader waits for its own copies in flight before the block reuses the ring, and
-// tensor memory is freed only after the issuer's last commit drained.
+// tensor memory is freed only after the issuers' last commits drained.
 __global__ void __launch_bounds__(FT_THREADS, 1)
     k_fold_tc(const uint4* __restrict__ table, int rl, uint64_t ring_elements, const uint8_t* __restrict__ strips,
               int cols_per_split, int32_t* __restrict__ part, int* status) {
   extern __shared__ __align__(1024) uint8_t fsm[];
   uint8_t* ring = fsm;                                                  // [FT_RING][FT_SLOT]: strips, words
-  uint64_t* done = reinterpret_cast<uint64_t*>(fsm + FT_BARS);          // [FT_STAGES] MMAs of a stage done
-  uint64_t* full = done + FT_STAGES;                                    // [FT_STAGES] a stage written
+  uint64_t* done = reinterpret_cast<uint64_t*>(fsm + FT_BARS);          // [FT_RING] a slot's column's MMAs done
+  uint64_t* full = done + FT_RING;                                      // [FT_STAGES] a stage written
   uint64_t* wfull = full + FT_STAGES;                                   // [FT_RING] a slot's copies landed
-  uint64_t* sfree = wfull + FT_RING;                                    // [FT_RING] a slot's MMAs done
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(sfree + FT_RING);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(wfull + FT_RING);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const bool producer = warp >= 3;
-  const int row = 32 * (warp & 3) + lane, group = (warp - 3) >> 2;  // producers: word (A row), group
+  const bool producer = warp >= 5;
+  const int row = 32 * (warp & 3) + lane, group = (warp - 5) >> 2;  // producers: word (A row), group
   const uint64_t words = 4 * ring_elements;
   const uint64_t w0 = (uint64_t)blockIdx.x * 128;  // first word (row) of the block
   const int nw = (int)min((uint64_t)128, words - w0);
@@ -391,14 +391,11 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   const int ncols = c_end - c_begin;
   if (tid == 0) {
     *abort_flag = 0;
-    for (int i = 0; i < FT_STAGES; ++i) {
-      tc::mbar_init(&done[i], 2);
-      tc::mbar_init(&full[i], FT_PRODUCERS / FT_STAGES);
-    }
     for (int i = 0; i < FT_RING; ++i) {
+      tc::mbar_init(&done[i], FT_ISSUERS);
       tc::mbar_init(&wfull[i], 1);
-      tc::mbar_init(&sfree[i], 2);
     }
+    for (int i = 0; i < FT_STAGES; ++i) tc::mbar_init(&full[i], FT_PRODUCERS / FT_STAGES);
     tc::mbar_init_fence();
   }
   if (warp == 0) tc::tmem_alloc(tslot, 512);
@@ -406,6 +403,17 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
+  if (warp < 4) {  // D = 0: every MMA accumulates, in whatever order the issuers' MMAs arrive
+    uint32_t z[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) z[i] = 0;
+#pragma unroll
+    for (int n0 = 0; n0 < 2 * FT_N; n0 += 16) tc::tmem_st_x16(tbase + ((uint32_t)(32 * warp) << 16) + n0, z);
+    tc::tmem_wait_st();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
   const uint32_t id96 = tc::idesc_e4m3_f32(128, FT_N);  // both K-major
   auto give_up = [&]() {
     if (!*abort_flag) {
@@ -420,8 +428,9 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
     const uint32_t tA = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + 256 + 32 * s;
     for (int it = group; it < ncols; it += FT_STAGES) {
       const int slot = it % FT_RING;
-      bool ok = it < FT_STAGES || tc::mbar_wait(&done[s], ((it / FT_STAGES) - 1) & 1, abort_flag, FT_WAIT_CYCLES);
-      ok = ok && tc::mbar_wait(&wfull[slot], (it / FT_RING) & 1, abort_flag, FT_WAIT_CYCLES);
+      bool ok = it < FT_STAGES || tc::mbar_wait_fast(&done[(it - FT_STAGES) % FT_RING],
+                                                     ((it - FT_STAGES) / FT_RING) & 1, abort_flag, FT_WAIT_CYCLES);
+      ok = ok && tc::mbar_wait_fast(&wfull[slot], (it / FT_RING) & 1, abort_flag, FT_WAIT_CYCLES);
       if (!__all_sync(0xffffffffu, ok)) give_up();
       if (!*abort_flag) {
         tc::fence_after_sync();
@@ -436,11 +445,11 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
       tc::fence_before_sync();
       tc::mbar_arrive(&full[s]);
     }
-  } else if (tid == 64) {  // loader
+  } else if (tid == 128) {  // loader
     int issued = 0;
     for (int it = 0; it < ncols && !*abort_flag; ++it, ++issued) {
       const int slot = it % FT_RING;
-      if (it >= FT_RING && !tc::mbar_wait(&sfree[slot], ((it / FT_RING) - 1) & 1, abort_flag, FT_WAIT_CYCLES)) {
+      if (it >= FT_RING && !tc::mbar_wait(&done[slot], ((it / FT_RING) - 1) & 1, abort_flag, FT_WAIT_CYCLES)) {
         give_up();
         break;
       }
@@ -456,33 +465,35 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
       while (!tc::mbar_try_wait(&wfull[it % FT_RING], (it / FT_RING) & 1) && clock64() - t0 < FT_WAIT_CYCLES) {
       }
     }
-  } else if (lane == 0) {  // issuer of range warp (0: low, 1: high)
-    const uint32_t d = tbase + FT_N * warp, boff = FT_RCORES * 128 * warp;
+  } else if (warp < FT_ISSUERS && lane == 0) {  // issuer: range warp % 2, MMAs kk = 2 (warp / 2) + 0, 1
+    const int range = warp & 1, kh = warp >> 1;
+    const uint32_t d = tbase + FT_N * range, boff = FT_RCORES * 128 * range;
     for (int it = 0; it < ncols; ++it) {
       const int s = it % FT_STAGES, slot = it % FT_RING;
-      if (!tc::mbar_wait(&full[s], (it / FT_STAGES) & 1, abort_flag, FT_WAIT_CYCLES) ||
+      if (!tc::mbar_wait_fast(&full[s], (it / FT_STAGES) & 1, abort_flag, FT_WAIT_CYCLES) ||
           !tc::mbar_wait_fast(&wfull[slot], (it / FT_RING) & 1, abort_flag, FT_WAIT_CYCLES))
         give_up();
       if (*abort_flag) break;
       tc::fence_after_sync();
       const uint32_t a0 = tbase + 256 + 32 * s, b0 = tc::smem_u32(ring + slot * FT_SLOT) + boff;
 #pragma unroll
-      for (int kk = 0; kk < 4; ++kk)  // K = 32 x kk: k groups 2 kk, 2 kk + 1, so core e starts at 4 kk
-        tc::mma_e4m3_ta(d, a0 + 8 * kk, tc::sdesc(b0 + 4 * kk * 128, 256, 128), id96, (it | kk) ? 1u : 0u);
-      tc::mma_commit(&done[s]);
-      tc::mma_commit(&sfree[slot]);
+      for (int k2 = 0; k2 < 2; ++k2) {  // K = 32 kk: k groups 2 kk, 2 kk + 1, so core e starts at 4 kk
+        const int kk = 2 * kh + k2;
+        tc::mma_e4m3_ta(d, a0 + 8 * kk, tc::sdesc(b0 + 4 * kk * 128, 256, 128), id96, 1u);
+      }
+      tc::mma_commit(&done[slot]);
       last = it;
     }
-    if (last >= 0) {  // drain: the last commit covers every MMA
+    if (last >= 0) {  // drain: the last commits cover every MMA
       const long long t0 = clock64();
-      while (!tc::mbar_try_wait(&done[last % FT_STAGES], (last / FT_STAGES) & 1) && clock64() - t0 < FT_WAIT_CYCLES) {
+      while (!tc::mbar_try_wait(&done[last % FT_RING], (last / FT_RING) & 1) && clock64() - t0 < FT_WAIT_CYCLES) {
       }
     }
   }
   bool ok = !*abort_flag;
   if (ok && ncols > 0) {
     const int lt = ncols - 1;
-    ok = __all_sync(0xffffffffu, tc::mbar_wait(&done[lt % FT_STAGES], (lt / FT_STAGES) & 1, abort_flag,
+    ok = __all_sync(0xffffffffu, tc::mbar_wait(&done[lt % FT_RING], (lt / FT_RING) & 1, abort_flag,
                                                 FT_WAIT_CYCLES));
   }
   ok = __syncthreads_and(ok);
@@ -490,7 +501,7 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   // The coefficients per row into shared memory (the ring is free now): fin[row][i], i < 162.
   int32_t* fin = reinterpret_cast<int32_t*>(fsm);
   const int FS = N162 + 1;
-  if (tid < 128)
+  if (tid < 128 && !(ok && ncols > 0))  // (otherwise every coefficient is written below)
     for (int i = 0; i < N162; ++i) fin[tid * FS + i] = 0;
   if (ok && ncols > 0 && tid < 128) {  // warps 0-3: TMEM lanes 32 w .. 32 w + 31 = the block's rows
 #pragma unroll 1

@@ -146,8 +146,8 @@ __global__ void __launch_bounds__(SBT_THREADS, 1)
     for (int t = group; t < 32; t += SBT_GROUPS) {
       const int s = t % SBT_STAGES, slot = t % SBT_RING;
       bool ok = t < SBT_STAGES ||
-                tc::mbar_wait(&done[s], ((t / SBT_STAGES) - 1) & 1, abort_flag, SBT_WAIT_CYCLES);
-      ok = ok && tc::mbar_wait(&wfull[slot], (t / SBT_RING) & 1, abort_flag, SBT_WAIT_CYCLES);
+                tc::mbar_wait_fast(&done[s], ((t / SBT_STAGES) - 1) & 1, abort_flag, SBT_WAIT_CYCLES);
+      ok = ok && tc::mbar_wait_fast(&wfull[slot], (t / SBT_RING) & 1, abort_flag, SBT_WAIT_CYCLES);
       if (!__all_sync(0xffffffffu, ok)) give_up();
       const uint4 w = live && !*abort_flag ? reinterpret_cast<const uint4*>(ring + slot * SBT_SLOT)[128 * op + j]
                                            : make_uint4(0, 0, 0, 0);
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(SBT_THREADS, 1)
   } else if (tid == 0) {
     for (int t = 0; t < 32; ++t) {
       const int s = t % SBT_STAGES;
-      if (!tc::mbar_wait(&full[s], (t / SBT_STAGES) & 1, abort_flag, SBT_WAIT_CYCLES)) give_up();
+      if (!tc::mbar_wait_fast(&full[s], (t / SBT_STAGES) & 1, abort_flag, SBT_WAIT_CYCLES)) give_up();
       if (*abort_flag) break;
       tc::fence_after_sync();
       const uint32_t a0 = tc::smem_u32(sbs + s * SBT_STAGE), b0 = a0 + SBT_OPA;
