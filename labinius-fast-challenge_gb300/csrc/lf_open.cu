@@ -523,9 +523,10 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
     const uint64_t m0 = w0 / 4;
     const int nel = (int)min((uint64_t)32, ring_elements - m0);
     int32_t* dst = part + ((uint64_t)split * ring_elements + m0) * 648;
-    for (int idx = tid; idx < nel * 648; idx += FT_THREADS) {
-      const int m = idx / 648, cc = idx % 648;
-      dst[idx] = fin[(4 * m + (cc & 3)) * FS + (cc >> 2)];
+    static_assert(FT_THREADS >= 648, "one coefficient slot per thread");
+    if (tid < 648) {
+      const int* src = fin + (tid & 3) * FS + (tid >> 2);
+      for (int m = 0; m < nel; ++m) dst[m * 648 + tid] = src[4 * m * FS];
     }
   } else if (tid == 0) {
     atomicExch(status, 5);

@@ -53,31 +53,39 @@ __global__ void k_eq_table_f162(const f162* __restrict__ ps, int n, f162* __rest
 //   count_h[c][b] = sum_{j < 4096} bit_c(pi0[4096 h + j]) bit_b(E_lo[j]),
 // an exact integer in f32. Operands are 8-bit floats (e4m3, kind::f8f6f4): every word is expanded
 // to a row of 128 bytes, byte i = 2.0 (0x40) when bit i is set, read MN-major (row = entry j = K).
-// A = E_lo's rows (M = b), B = the rows of two blocks h side by side (N = 256: 128 h + c), so one
-// MMA of K = 32 covers both blocks and D = 128 lanes (b) x 256 columns, 4 x count (<= 16384, exact);
-// the count's parity is bit 2 of the f32 mantissa after adding 2^23. The 4096 entries run in 32
-// k-tiles of 128 through four shared-memory stages. Roles, on mbarriers:
+// A = E_lo's rows (M = b), B = the rows of a pair of blocks h side by side (N = 256: 128 h + c), so
+// one MMA of K = 32 covers both blocks and D = 128 lanes (b) x 256 columns, 4 x count (<= 16384,
+// exact); the count's parity is bit 2 of the f32 mantissa after adding 2^23.
+//
+// Persistent: one CTA per SM walks the pairs p = blockIdx.x + q gridDim.x, each pair 32 k-tiles of
+// 128 entries, as one continuous stream of k-tiles T = 32 q + t through four shared-memory stages,
+// with D double-buffered in tensor memory (pair q in columns 256 (q % 2) ..), so the next pair's
+// copies, expansion and MMAs overlap the previous pair's read-out. Roles, on mbarriers:
 //   lane 0 of warp 1 (loader): per k-tile three bulk copies of 2048 bytes (E_lo's entries and the
-//     two blocks' entries 128 t .. +127) into ring slot t % SBT_RING, completing on wfull[slot],
-//     once the producers have read the slot's previous k-tile (cfree);
+//     pair's entries 128 t .. +127) into ring slot T % SBT_RING, completing on wfull[slot], once the
+//     producers have read the slot's previous k-tile (cfree);
 //   warps 2-25 (producers, two groups of 384 threads, one row each: E_lo, block 0, block 1; group g
-//     takes the k-tiles t = g mod 2): wait until stage t % 4 is free (done, the MMAs of k-tile
-//     t - 4) and the words landed, read their word (arrive cfree), expand it, arrive full;
-//   lane 0 of warp 0 (issuer): per k-tile wait full, issue 4 MMAs, commit to done.
-// Epilogue: warps 0-7 read D (lane quarter w % 4, block w / 4) and assemble each c's 128 parity
-// bits with one ballot per 32 b. Every wait is bounded; a timeout sets *status = 4.
+//     takes the k-tiles T = g mod 2): wait until stage T % 4 is free (done, the MMAs of k-tile T - 4)
+//     and the words landed, read their word, expand it, fence, arrive cfree and full;
+//   lane 0 of warp 0 (issuer): per k-tile wait full, issue 4 MMAs, commit to done; before a pair's
+//     first k-tile wait until its D buffer was read out (dfree), after its last commit to dfull;
+//   warps 26-29 (epilogue; lane quarter w % 4): per pair wait dfull, read D (bits b of the quarter,
+//     256 columns), assemble each c's parity word from one ballot per 32 b, arrive dfree.
+// Every wait is bounded; a timeout sets *status = 4 and the abort flag, on which every role leaves
+// its loop; tensor memory is freed after the issuer's last commit drained.
 // ---------------------------------------------------------------------------------------------
 constexpr int SBT_GROUPS = 2;
 constexpr int SBT_ROWS = 3 * 128;                             // a k-tile's rows: E_lo, block 0, block 1
 constexpr int SBT_PRODUCERS = SBT_GROUPS * SBT_ROWS;          // warps 2-25
-constexpr int SBT_THREADS = SBT_PRODUCERS + 64;
+constexpr int SBT_EPI_WARP = 2 + SBT_PRODUCERS / 32;          // warps 26-29 read D out
+constexpr int SBT_THREADS = SBT_PRODUCERS + 64 + 128;
 constexpr int SBT_OPA = 128 * 128;                            // E_lo rows: 128 entries x 128 bytes
 constexpr int SBT_STAGE = 3 * SBT_OPA;                        // [A][B: 128 entries x 256 bytes]
 constexpr int SBT_STAGES = 4;
 constexpr int SBT_RING = 4;
 constexpr int SBT_SLOT = 3 * 2048;                            // a k-tile's words: E_lo, block 0, block 1
 constexpr int SBT_BARS = SBT_STAGES * SBT_STAGE + SBT_RING * SBT_SLOT;
-constexpr int SBT_SMEM = SBT_BARS + (2 * SBT_STAGES + 2 * SBT_RING) * 8 + 16;
+constexpr int SBT_SMEM = SBT_BARS + (2 * SBT_STAGES + 2 * SBT_RING + 4) * 8 + 16;
 constexpr long long SBT_WAIT_CYCLES = 2000000000LL;
 
 // A 128-bit word -> row r of an MN-major e4m3 tile (8-row x 16-byte core matrices, cores adjacent
@@ -104,11 +112,15 @@ __global__ void __launch_bounds__(SBT_THREADS, 1)
   uint64_t* full = done + SBT_STAGES;                                 // [SBT_STAGES] a stage written
   uint64_t* wfull = full + SBT_STAGES;                                // [SBT_RING] a slot's copies landed
   uint64_t* cfree = wfull + SBT_RING;                                 // [SBT_RING] a slot's words read
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(cfree + SBT_RING);
+  uint64_t* dfull = cfree + SBT_RING;                                 // [2] a D buffer's pair complete
+  uint64_t* dfree = dfull + 2;                                        // [2] a D buffer read out
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(dfree + 2);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint64_t h0 = 2 * (uint64_t)blockIdx.x;
-  const bool two = h0 + 1 < nblocks;  // the block's second h exists
+  const uint64_t npairs = (nblocks + 1) / 2;
+  const int nq = blockIdx.x < npairs ? (int)((npairs - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  const int ntiles = 32 * nq;
+  auto pair_h0 = [&](int q) { return 2 * ((uint64_t)blockIdx.x + (uint64_t)q * gridDim.x); };
   if (tid == 0) {
     *abort_flag = 0;
     for (int i = 0; i < SBT_STAGES; ++i) {
@@ -119,9 +131,13 @@ __global__ void __launch_bounds__(SBT_THREADS, 1)
       tc::mbar_init(&wfull[i], 1);
       tc::mbar_init(&cfree[i], SBT_ROWS);
     }
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&dfull[i], 1);
+      tc::mbar_init(&dfree[i], 128);
+    }
     tc::mbar_init_fence();
   }
-  if (warp == 0) tc::tmem_alloc(tslot, 256);
+  if (warp == 0) tc::tmem_alloc(tslot, 512);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -135,19 +151,18 @@ __global__ void __launch_bounds__(SBT_THREADS, 1)
     }
   };
 
-  int last = -1;  // k-tile of the issuer's last commit
-  if (warp >= 2) {
+  if (warp >= 2 && warp < SBT_EPI_WARP) {
     const int p = tid - 64, group = p / SBT_ROWS, op = (p % SBT_ROWS) >> 7, j = p & 127;
-    const bool live = op < 2 || two;
     // E_lo: A tile, 8-row groups 1024 bytes apart; block op - 1: B tile cores 8 (op - 1) .. + 7,
     // 8-row groups 2048 bytes apart
     const int kstride = op == 0 ? 1024 : 2048;
     const int at = op == 0 ? 0 : SBT_OPA + (op - 1) * 8 * 128;
-    for (int t = group; t < 32; t += SBT_GROUPS) {
-      const int s = t % SBT_STAGES, slot = t % SBT_RING;
-      bool ok = t < SBT_STAGES ||
-                tc::mbar_wait_fast(&done[s], ((t / SBT_STAGES) - 1) & 1, abort_flag, SBT_WAIT_CYCLES);
-      ok = ok && tc::mbar_wait_fast(&wfull[slot], (t / SBT_RING) & 1, abort_flag, SBT_WAIT_CYCLES);
+    for (int T = group; T < ntiles; T += SBT_GROUPS) {
+      const int s = T % SBT_STAGES, slot = T % SBT_RING;
+      const bool live = op < 2 || pair_h0(T / 32) + 1 < nblocks;
+      bool ok = T < SBT_STAGES ||
+                tc::mbar_wait_fast(&done[s], ((T / SBT_STAGES) - 1) & 1, abort_flag, SBT_WAIT_CYCLES);
+      ok = ok && tc::mbar_wait_fast(&wfull[slot], (T / SBT_RING) & 1, abort_flag, SBT_WAIT_CYCLES);
       if (!__all_sync(0xffffffffu, ok)) give_up();
       const uint4 w = live && !*abort_flag ? reinterpret_cast<const uint4*>(ring + slot * SBT_SLOT)[128 * op + j]
                                            : make_uint4(0, 0, 0, 0);
@@ -162,37 +177,43 @@ __global__ void __launch_bounds__(SBT_THREADS, 1)
     }
   } else if (tid == 32) {  // loader
     int issued = 0;
-    for (int t = 0; t < 32 && !*abort_flag; ++t, ++issued) {
-      const int slot = t % SBT_RING;
-      if (t >= SBT_RING && !tc::mbar_wait(&cfree[slot], ((t / SBT_RING) - 1) & 1, abort_flag, SBT_WAIT_CYCLES)) {
+    for (int T = 0; T < ntiles && !*abort_flag; ++T, ++issued) {
+      const int slot = T % SBT_RING, t = T % 32;
+      if (T >= SBT_RING && !tc::mbar_wait(&cfree[slot], ((T / SBT_RING) - 1) & 1, abort_flag, SBT_WAIT_CYCLES)) {
         give_up();
         break;
       }
+      const uint64_t h0 = pair_h0(T / 32);
+      const bool two = h0 + 1 < nblocks;
       uint8_t* dst = ring + slot * SBT_SLOT;
       tc::mbar_expect_tx(&wfull[slot], two ? 3 * 2048 : 2 * 2048);
       tc::bulk_load(dst, elo + 128 * t, 2048, &wfull[slot]);
       tc::bulk_load(dst + 2048, table + h0 * 4096 + 128 * t, 2048, &wfull[slot]);
       if (two) tc::bulk_load(dst + 4096, table + (h0 + 1) * 4096 + 128 * t, 2048, &wfull[slot]);
     }
-    // the copies in flight land before the block leaves or reuses the ring
-    for (int t = issued > SBT_RING ? issued - SBT_RING : 0; t < issued; ++t) {
+    // the copies in flight land before the block leaves
+    for (int T = issued > SBT_RING ? issued - SBT_RING : 0; T < issued; ++T) {
       const long long t0 = clock64();
-      while (!tc::mbar_try_wait(&wfull[t % SBT_RING], (t / SBT_RING) & 1) && clock64() - t0 < SBT_WAIT_CYCLES) {
+      while (!tc::mbar_try_wait(&wfull[T % SBT_RING], (T / SBT_RING) & 1) && clock64() - t0 < SBT_WAIT_CYCLES) {
       }
     }
-  } else if (tid == 0) {
-    for (int t = 0; t < 32; ++t) {
-      const int s = t % SBT_STAGES;
-      if (!tc::mbar_wait_fast(&full[s], (t / SBT_STAGES) & 1, abort_flag, SBT_WAIT_CYCLES)) give_up();
+  } else if (tid == 0) {  // issuer
+    int last = -1;  // k-tile of the last commit
+    for (int T = 0; T < ntiles; ++T) {
+      const int s = T % SBT_STAGES, t = T % 32, q = T / 32, buf = q & 1;
+      if (t == 0 && q >= 2 && !tc::mbar_wait(&dfree[buf], ((q >> 1) - 1) & 1, abort_flag, SBT_WAIT_CYCLES))
+        give_up();
+      if (!tc::mbar_wait_fast(&full[s], (T / SBT_STAGES) & 1, abort_flag, SBT_WAIT_CYCLES)) give_up();
       if (*abort_flag) break;
       tc::fence_after_sync();
       const uint32_t a0 = tc::smem_u32(sbs + s * SBT_STAGE), b0 = a0 + SBT_OPA;
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk)  // K = 32: four 8-row groups
-        tc::mma_e4m3(tbase, tc::sdesc(a0 + kk * 4096, 1024, 128), tc::sdesc(b0 + kk * 8192, 2048, 128), idesc,
-                     (t | kk) ? 1u : 0u);
+        tc::mma_e4m3(tbase + 256 * buf, tc::sdesc(a0 + kk * 4096, 1024, 128), tc::sdesc(b0 + kk * 8192, 2048, 128),
+                     idesc, (t | kk) ? 1u : 0u);
       tc::mma_commit(&done[s]);
-      last = t;
+      if (t == 31) tc::mma_commit(&dfull[buf]);
+      last = T;
     }
     // Drain: the issuer's last commit covers every MMA it issued (also after an abort).
     if (last >= 0) {
@@ -201,42 +222,46 @@ __global__ void __launch_bounds__(SBT_THREADS, 1)
              clock64() - t0 < SBT_WAIT_CYCLES) {
       }
     }
-  }
-  // The last commit (k-tile 31, stage 3, its 8th) covers every MMA of the block.
-  bool ok = !*abort_flag;
-  if (ok) ok = __all_sync(0xffffffffu, tc::mbar_wait(&done[31 % SBT_STAGES], (31 / SBT_STAGES) & 1, abort_flag,
-                                                     SBT_WAIT_CYCLES));
-  ok = __syncthreads_and(ok);
-  tc::fence_after_sync();
-  if (ok && warp < 8) {  // TMEM lanes 32 (w % 4) .. + 31 = bits b, columns 128 (w / 4) + c
-    const int qd = warp & 3, hh = warp >> 2;
-    if (h0 + hh < nblocks) {
-      uint32_t* out = reinterpret_cast<uint32_t*>(sblk + (h0 + hh) * 128 * 16) + qd;
-#pragma unroll 1
-      for (int c0 = 0; c0 < 128; c0 += 32) {
-        uint32_t mine = 0;
-#pragma unroll
-        for (int n0 = 0; n0 < 32; n0 += 16) {
-          uint32_t v[16];
-          tc::tmem_ld_x16(tbase + ((uint32_t)(32 * qd) << 16) + 128 * hh + c0 + n0, v);
-          tc::tmem_wait_ld(v);
-#pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            // both operands hold set bits as 2.0: D = 4 x count, so the count's parity is bit 2
-            const uint32_t bal = __ballot_sync(0xffffffffu, (__float_as_uint(__uint_as_float(v[i]) + 8388608.0f) >> 2) & 1u);
-            if (lane == n0 + i) mine = bal;
-          }
-        }
-        out[4 * (c0 + lane)] = mine;  // word qd of c = c0 + lane: bits b = 32 qd + lane'
+  } else if (warp >= SBT_EPI_WARP) {  // TMEM lanes 32 (w % 4) .. + 31 = bits b
+    const int qd = warp & 3;
+    for (int q = 0; q < nq; ++q) {
+      const int buf = q & 1;
+      if (!__all_sync(0xffffffffu, tc::mbar_wait(&dfull[buf], (q >> 1) & 1, abort_flag, SBT_WAIT_CYCLES))) {
+        give_up();
+        break;
       }
+      tc::fence_after_sync();
+      const uint64_t h0 = pair_h0(q);
+      for (int hh = 0; hh < 2 && h0 + hh < nblocks; ++hh) {
+        uint32_t* out = reinterpret_cast<uint32_t*>(sblk + (h0 + hh) * 128 * 16) + qd;
+#pragma unroll 1
+        for (int c0 = 0; c0 < 128; c0 += 32) {
+          uint32_t mine = 0;
+#pragma unroll
+          for (int n0 = 0; n0 < 32; n0 += 16) {
+            uint32_t v[16];
+            tc::tmem_ld_x16(tbase + ((uint32_t)(32 * qd) << 16) + 256 * buf + 128 * hh + c0 + n0, v);
+            tc::tmem_wait_ld(v);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              // both operands hold set bits as 2.0: D = 4 x count, so the count's parity is bit 2
+              const uint32_t bal =
+                  __ballot_sync(0xffffffffu, (__float_as_uint(__uint_as_float(v[i]) + 8388608.0f) >> 2) & 1u);
+              if (lane == n0 + i) mine = bal;
+            }
+          }
+          out[4 * (c0 + lane)] = mine;  // word qd of c = c0 + lane: bits b = 32 qd + lane'
+        }
+      }
+      tc::fence_before_sync();
+      tc::mbar_arrive(&dfree[buf]);
     }
-  } else if (!ok && tid == 0) {
-    atomicExch(status, 4);
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 0) tc::tmem_dealloc(tbase, 256);
+  if (*abort_flag && tid == 0) atomicExch(status, 4);
+  if (warp == 0) tc::tmem_dealloc(tbase, 512);
 }
 
 // v[c] = sum_h E_hi[h] * S_h[c]: block of 128 threads (one per c) over a run of h.
@@ -636,7 +661,15 @@ void launch_sblock(const uint4* table, uint64_t nblocks, const b128* elo, uint8_
                    cudaStream_t s) {
   static std::atomic<unsigned long long> attr{0};
   smem_limit(k_sblock_tc, SBT_SMEM, attr);
-  k_sblock_tc<<<(unsigned)((nblocks + 1) / 2), SBT_THREADS, SBT_SMEM, s>>>(
+  static int sms = 0;  // one CTA per SM (the kernel walks its pairs)
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  const uint64_t npairs = (nblocks + 1) / 2;
+  k_sblock_tc<<<(unsigned)std::min<uint64_t>(npairs, (uint64_t)sms), SBT_THREADS, SBT_SMEM, s>>>(
       table, nblocks, reinterpret_cast<const uint4*>(elo), sblk, status);
 }
 void launch_partials_combine(const b128* ehi, const uint8_t* sblk, int nblocks, unsigned long long* v, cudaStream_t s) {
