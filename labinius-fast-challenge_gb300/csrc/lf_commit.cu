@@ -659,9 +659,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int reduce_every = (int)pcs[pi].reduce_every;
     uint4 cum[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
     const uint32_t tl = tbase + ((uint32_t)(32 * (warp - 24)) << 16);
-    int ready_part = -1;  // the table is known to be in device memory up to this part
+    // The table is known to be in device memory below element next_wait (the end of the last
+    // part waited for): one compare per element, the division only when a new part begins (an
+    // integer division per element slowed every block of a streamed proof by 5 %).
+    int next_wait = 0;
     auto fetch = [&](int e) {  // element e's words (this column) and key rows t, t + 128 into ring slot e % 3
-      if (e < nelem && ready && (m_begin + e) / part_elems > ready_part) {
+      if (e < nelem && ready && m_begin + e >= next_wait) {
         // The table is still arriving: part (m_begin + e) / part_elems is there once the copy
         // stream has written the proof's epoch into its flag (after the part's copy).
         const int part = (m_begin + e) / part_elems;
@@ -676,7 +679,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           }
           __nanosleep(256);
         }
-        ready_part = part;
+        next_wait = (part + 1) * part_elems;
       }
       if (e < nelem && !*abort_flag) {
         const size_t m = (size_t)(m_begin + e);
