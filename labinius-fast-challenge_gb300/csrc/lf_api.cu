@@ -305,8 +305,9 @@ struct lf_ctx {
 
 namespace {
 
-constexpr int TABLE_PARTS = 16;       // parts of a page-locked host table (lf_prove)
-constexpr int TABLE_FIRST_PARTS = 2;  // queued before the commitment's launch
+constexpr int TABLE_PARTS = 64;       // at most this many parts of a page-locked host table (lf_prove)
+constexpr int TABLE_MIN_PARTS = 16;   // a host table streams when its columns have this many elements
+constexpr int TABLE_FIRST_PARTS = 3;  // queued before the commitment's launch
 
 int fail(lf_ctx* c, int code, const std::string& msg) {
   if (c) {
@@ -625,15 +626,19 @@ struct TableStream {
   const uint8_t* host;  // the page-locked table
   size_t pitch;         // bytes of one column
   uint64_t elements;    // ring elements per column
-  int next;             // parts not yet queued: [next, TABLE_PARTS)
+  int next;             // parts not yet queued: order[next .. nparts)
   int withhold;         // a part whose flag is left unset (test hook), else -1
   long long wait;       // SM cycles the commitment waits for a part (0: its default)
+  int nparts;           // parts of part_elems elements (the last one shorter)
+  uint8_t order[TABLE_PARTS];  // the copy order of the parts (order_table_parts)
 };
 
-// Queues parts [ts->next, end) of a streamed table on the copy stream, each followed by its ready
-// flag; once every part is queued, `done` (and the upload's end) is recorded after them.
+// Queues parts order[ts->next .. end) of a streamed table on the copy stream, each followed by its
+// ready flag; once every part is queued, `done` (and the upload's end) is recorded after them.
 int enqueue_table_parts(lf_ctx* ctx, TableStream* ts, int end) {
-  for (int i = ts->next; i < end; ++i) {
+  end = std::min(end, ts->nparts);
+  for (int n = ts->next; n < end; ++n) {
+    const int i = ts->order[n];
     const uint64_t m0 = (uint64_t)i * ts->part_elems, m1 = std::min<uint64_t>(ts->elements, m0 + ts->part_elems);
     if (m0 < m1)
       CK(cudaMemcpy2DAsync(ctx->table.as<uint8_t>() + 64 * m0, ts->pitch, ts->host + 64 * m0, ts->pitch, 64 * (m1 - m0),
@@ -644,7 +649,7 @@ int enqueue_table_parts(lf_ctx* ctx, TableStream* ts, int end) {
       return fail(ctx, LF_E_CUDA, "stream write of a table part's ready flag failed");
   }
   if (end > ts->next) ts->next = end;
-  if (ts->next >= TABLE_PARTS) {
+  if (ts->next >= ts->nparts) {
     CK(cudaEventRecord(ctx->uploaded[0], ctx->upload_stream));
     CK(cudaEventRecord(ctx->up_t1, ctx->upload_stream));
   }
@@ -697,6 +702,31 @@ cudaError_t read_round_message(lf_ctx* ctx, cudaStream_t st, f162 m[2]) {
   return cudaSuccess;
 }
 
+// The copy order of a streamed table's parts: by when the commitment's blocks first read them.
+// The commitment's grid runs its element splits in order, blocks_per_split blocks each, about sms
+// blocks at a time, and a block reads its split's elements in order at a steady rate, so element m
+// of split z is first read about wave(z) + (m - m0(z)) / per waves after the launch. Parts go up
+// in the order of their first element's time (part 0 first, already queued): the first wave's
+// blocks, which start at several places in the table, all find their first parts early.
+void order_table_parts(TableStream* ts, int splits, int blocks_per_split, int sms) {
+  const int n = ts->nparts;
+  const uint64_t E = ts->elements, per = (E + splits - 1) / splits;
+  std::vector<double> need(n, 1e300);
+  for (int z = 0; z < splits; ++z) {
+    const uint64_t m0 = (uint64_t)z * per, m1 = std::min<uint64_t>(E, m0 + per);
+    if (m0 >= m1) continue;
+    const double wave = std::floor((double)z * blocks_per_split / std::max(1, sms));
+    for (uint64_t p = m0 / ts->part_elems; p < (uint64_t)n && p * ts->part_elems < m1; ++p) {
+      const uint64_t e = std::max<uint64_t>(m0, p * ts->part_elems);
+      need[p] = std::min(need[p], wave + (double)(e - m0) / (double)per);
+    }
+  }
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  std::stable_sort(idx.begin() + ts->next, idx.end(), [&](int a, int b) { return need[a] < need[b]; });
+  for (int i = ts->next; i < n; ++i) ts->order[i] = (uint8_t)idx[i];
+}
+
 // table_ready (may be null): an event the prover's stream waits for before the first kernel that
 // reads the table. With ts, the commitment starts before the table is complete (table_ready is
 // then unused). touch: `proof` is host memory that may need touch_proof_buffer (done while the
@@ -734,11 +764,13 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
   // host table arrives, cost it its wave balance: 4 launches of about 5 splits each ran 1.4 ms
   // longer than one launch at 2^31 bits.)
   if (ts) {
+    order_table_parts(ts, splits, commit_blocks_per_split(mp), ctx->sms);
+    if ((rc = enqueue_table_parts(ctx, ts, TABLE_FIRST_PARTS))) return rc;
     launch_commit(mp, sh, table, ctx->key->key.as<uint32_t>(), ctx->key->btiles.as<uint16_t>(),
                   ctx->partial.as<uint32_t>(), splits, ctx->status.as<int>(), st, 0, -1, ts->ready, ts->epoch,
                   ts->part_elems, ts->wait);
     // the parts after the first few are queued only now, off the commitment's critical path
-    if ((rc = enqueue_table_parts(ctx, ts, TABLE_PARTS))) return rc;
+    if ((rc = enqueue_table_parts(ctx, ts, ts->nparts))) return rc;
     CK(cudaStreamWaitEvent(st, ts->done, 0));  // every later kernel reads the whole table
   } else {
     if (table_ready) CK(cudaStreamWaitEvent(st, table_ready, 0));
@@ -988,12 +1020,12 @@ double ms_between(clk::time_point a, clk::time_point b) { return std::chrono::du
 
 // One job with the context lock held; table_dev is the job's table already on the device.
 // Starts the copy of a host table into ctx->table on ctx's copy stream. A page-locked table goes up
-// in TABLE_PARTS element ranges of every column (one 2-D copy each), each followed by a stream
-// write of the proof's epoch into its ready flag, and *ts describes them (streamed = true): the
-// commitment reads a range as soon as it has arrived. The first TABLE_FIRST_PARTS are queued here,
-// the rest by prove_device right after it launches the commitment (so the host's queueing of them
-// does not delay that launch). Any other table goes up in one copy whose completion is
-// ctx->uploaded[0].
+// in up to TABLE_PARTS element ranges of every column (one 2-D copy each), each followed by a
+// stream write of the proof's epoch into its ready flag, and *ts describes them (streamed = true):
+// the commitment reads a range as soon as it has arrived. Part 0 is queued here; prove_device
+// orders the rest by when the commitment's blocks reach them (order_table_parts), queues the next
+// few, launches the commitment and then queues the others (so the host's queueing of them does not
+// delay that launch). Any other table goes up in one copy whose completion is ctx->uploaded[0].
 int start_table_upload(lf_ctx* ctx, const void* table, size_t table_bytes, const Shape& sh, TableStream* ts,
                        bool* streamed) {
   int rc = side_streams(ctx);
@@ -1003,13 +1035,16 @@ int start_table_upload(lf_ctx* ctx, const void* table, size_t table_bytes, const
   cudaPointerAttributes ta{};
   const bool locked = cudaPointerGetAttributes(&ta, table) == cudaSuccess && ta.type == cudaMemoryTypeHost;
   cudaGetLastError();  // plain host memory leaves an error behind on some drivers
-  *streamed = locked && ctx->write_value && sh.ring_elements >= (uint64_t)TABLE_PARTS;
+  *streamed = locked && ctx->write_value && sh.ring_elements >= (uint64_t)TABLE_MIN_PARTS;
   if (*streamed) {
     const uint32_t epoch = ++ctx->epoch == 0 ? ++ctx->epoch : ctx->epoch;  // never 0, the flags' initial value
-    const int part_elems = (int)((sh.ring_elements + TABLE_PARTS - 1) / TABLE_PARTS);
+    const uint64_t want = std::min<uint64_t>(TABLE_PARTS, sh.ring_elements);
+    const int part_elems = (int)((sh.ring_elements + want - 1) / want);
     *ts = TableStream{ctx->ready, epoch, part_elems, ctx->uploaded[0], static_cast<const uint8_t*>(table),
-                      (size_t)16 << sh.rl, sh.ring_elements, 0, ctx->test_withhold, ctx->test_ready_wait};
-    return enqueue_table_parts(ctx, ts, TABLE_FIRST_PARTS);  // the rest after the commitment's launch
+                      (size_t)16 << sh.rl, sh.ring_elements, 0, ctx->test_withhold, ctx->test_ready_wait,
+                      (int)((sh.ring_elements + part_elems - 1) / part_elems), {}};
+    for (int i = 0; i < ts->nparts; ++i) ts->order[i] = (uint8_t)i;
+    return enqueue_table_parts(ctx, ts, 1);  // the rest once the commitment's layout is known
   }
   CK(cudaMemcpyAsync(ctx->table.p, table, table_bytes, cudaMemcpyHostToDevice, ctx->upload_stream));
   CK(cudaEventRecord(ctx->uploaded[0], ctx->upload_stream));
@@ -1040,7 +1075,7 @@ int run_job(lf_ctx* ctx, const lf_job& j, size_t* proof_len) {
   ctx->test_ready_wait = 0;
   rc = prove_device(ctx, j.seed, q, sh, ctx->table.as<uint4>(), j.proof, proof_len, ctx->uploaded[0], true,
                     streamed ? &ts : nullptr);
-  if (streamed && ts.next < TABLE_PARTS) enqueue_table_parts(ctx, &ts, TABLE_PARTS);  // (an early failure)
+  if (streamed && ts.next < ts.nparts) enqueue_table_parts(ctx, &ts, ts.nparts);  // (an early failure)
   // (a proof that failed early may not have waited for the side streams)
   cudaStreamSynchronize(ctx->upload_stream);
   cudaStreamSynchronize(ctx->touch_stream);
@@ -1686,7 +1721,7 @@ int lf_prove(lf_ctx* ctx, const uint8_t seed[32], const uint8_t q_le[16], uint32
   ctx->test_ready_wait = 0;
   rc = prove_device(ctx, seed, q, sh, ctx->table.as<uint4>(), proof, proof_len, ctx->uploaded[0], true,
                     streamed ? &tstream : nullptr);
-  if (streamed && tstream.next < TABLE_PARTS) enqueue_table_parts(ctx, &tstream, TABLE_PARTS);  // (an early failure)
+  if (streamed && tstream.next < tstream.nparts) enqueue_table_parts(ctx, &tstream, tstream.nparts);  // (an early failure)
   // (a proof that failed early may not have waited for the side streams)
   cudaStreamSynchronize(ctx->upload_stream);
   cudaStreamSynchronize(ctx->touch_stream);

@@ -907,6 +907,8 @@ void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, c
                                                  ready_wait > 0 ? ready_wait : TC_WAIT_CYCLES);
 }
 
+int commit_blocks_per_split(const ModulusPlan& mp) { return mp.nprimes * 3 * (COLUMNS / TC_COLS); }
+
 // Element range [m0, m1) of split range [s0, s1): the part of every column those splits read.
 void commit_split_elements(uint64_t elements, int splits, int s0, int s1, uint64_t& m0, uint64_t& m1) {
   const uint64_t per = (elements + splits - 1) / splits;

@@ -189,6 +189,8 @@ void launch_commit(const ModulusPlan& mp, const Shape& sh, const uint4* table, c
                    int split_begin = 0, int split_end = -1, const uint32_t* ready = nullptr, uint32_t epoch = 0,
                    int part_elems = 0, long long ready_wait = 0);
 void commit_split_elements(uint64_t elements, int splits, int s0, int s1, uint64_t& m0, uint64_t& m1);
+// Blocks of the commitment's grid per element split (they run one split after another).
+int commit_blocks_per_split(const ModulusPlan& mp);
 void launch_commit_finish(const ModulusPlan& mp, const Shape& sh, const uint32_t* partial, int splits, uint8_t* out,
                           cudaStream_t s, int ncols = COLUMNS);
 // Verifier pieces (lf_commit.cu): a_times_v into `out` (648 coefficients of `width` bytes) and

@@ -157,13 +157,13 @@ def test_degenerate_point_under_exact_lift(prover, oracle):
 
 
 def test_withheld_table_part_times_out_and_context_recovers(gpu_lib, oracle):
-    # A page-locked table is streamed into the running commitment in 16 element ranges, each
+    # A page-locked table is streamed into the running commitment in up to 64 element ranges, each
     # released by a flag the copy stream writes. With one flag withheld, the commitment's wait for
     # that range gives up after its limit (here about 10 ms of SM cycles), the kernel records the
     # timeout and leaves (tensor memory freed after its last MMAs drained), and the proof reports
     # LF_E_INTERNAL. The context then proves the next table, streamed again, correctly.
     torch = pytest.importorskip("torch")
-    log_vars = 24  # 64 ring elements per column: 16 parts of 4
+    log_vars = 24  # 64 ring elements per column: 64 parts of one
     table = oracle.write_table(SEED, log_vars)
     host = torch.empty(len(table), dtype=torch.uint8, pin_memory=True)
     host.numpy()[:] = bytearray(table)

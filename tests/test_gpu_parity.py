@@ -76,10 +76,11 @@ def test_device_table_writer_matches_oracle(prover, oracle):
 
 @pytest.mark.parametrize("log_vars", [23, 27, 31])
 def test_page_locked_table_streams_into_the_commitment(prover, oracle, log_vars):
-    # lf_prove from page-locked host memory copies the table in 16 element ranges while the
-    # commitment already runs, each block waiting for its range (tables of at least 16 ring
-    # elements per column: 2^23 bits and up): the proof is the one of the same table proven from
-    # device memory (and, at 2^23 bits, the oracle's).
+    # lf_prove from page-locked host memory copies the table in up to 64 element ranges, in the
+    # order the commitment's blocks reach them, while the commitment already runs, each block
+    # waiting for its range (tables of at least 16 ring elements per column: 2^23 bits and up):
+    # the proof is the one of the same table proven from device memory (and, at 2^23 bits, the
+    # oracle's).
     torch = pytest.importorskip("torch")
     seed = SEEDS[0]
     n = (1 << log_vars) // 8
