@@ -292,12 +292,10 @@ constexpr int FT_STAGES = 4;                    // A stages in tensor memory, 32
 constexpr int FT_RING = 12;                     // column slots: the loader runs up to 12 columns ahead
 constexpr int FT_PRODUCERS = 512;               // four groups of 128 (a word each): warps 5-20
 constexpr int FT_ISSUERS = 4;                   // lane 0 of warps 0-3 issue the MMAs
-constexpr int FT_THREADS = FT_PRODUCERS + 160;  // + the issuers' warps and the loader's (lane 0 of warp 4)
-constexpr int FT_FIN = 128 * (N162 + 1) * 4;    // the epilogue's coefficients per row (reuses the ring)
-constexpr int FT_BARS = FT_RING * FT_SLOT > FT_FIN ? FT_RING * FT_SLOT : FT_FIN;
+constexpr int FT_THREADS = FT_PRODUCERS + 288;  // + the issuers' warps, the loader's (lane 0 of warp 4), read-out
 // More than half of an SM's shared memory, so one block holds the SM's 512 tensor-memory columns.
 constexpr int FT_SMEM = 120 * 1024;
-static_assert(FT_BARS + (FT_STAGES + 2 * FT_RING) * 8 + 16 <= FT_SMEM, "fold shared memory");
+static_assert(FT_RING * FT_SLOT + (FT_STAGES + 2 * FT_RING + 4) * 8 + 16 <= FT_SMEM, "fold shared memory");
 constexpr long long FT_WAIT_CYCLES = 2000000000LL;
 
 // e4m3 code of a sum of up to three +-0.5: 0, +-0.5 (0x30), +-1 (0x38) or +-1.5 (0x3C).
@@ -349,46 +347,60 @@ __device__ __forceinline__ void fold_expand_word(uint4 v, uint32_t (&u)[32]) {
     for (int t = 0; t < 8; ++t) u[8 * q + t] = (((xs[q] >> (4 * t)) & 0xFu) * 0x08102040u) & 0x40404040u;
 }
 
-// Block = 128 table words (32 ring elements) x a run of columns; out: part[split][m][4 y + k]
-// for the block's elements, the column run's share of the fold.
+// Work unit = 128 table words (32 ring elements) x a run of columns; out: part[split][m][4 y + k]
+// for the unit's elements, the column run's share of the fold. Persistent: one CTA per SM takes the
+// units u = blockIdx.x + i gridDim.x (row block u % nbx, column run u / nbx) and runs their columns
+// as one stream T through the ring and the stages, with D double-buffered in tensor memory, so the
+// read-out of a unit overlaps the next unit's copies and MMAs.
 //
-// Tensor memory (512 columns): D = columns 0..191 (two ranges of N = 96, zeroed before the first
-// MMA), A stages s = 0..3 at 256 + 32 s (a column's 128 words, K = 128 bits as e4m3, read by the
-// MMAs from tensor memory, so the shared-memory port carries only the strips). Roles, meeting on
-// mbarriers:
-//   lane 0 of warp 4 (loader): per column c, once the MMAs of the column that used its ring slot
-//     FT_RING columns earlier are done (done[slot]), two bulk copies into slot c % FT_RING (the
-//     column's strips, 6656 bytes, and the block's 128 words, 2048 bytes) completing on wfull[slot];
+// Tensor memory (512 columns): D buffers b = 0, 1 at 192 b (two ranges of N = 96 each), A stages
+// s = 0..3 at 384 + 32 s (a column's 128 words, K = 128 bits as e4m3, read by the MMAs from tensor
+// memory, so the shared-memory port carries only the strips). Roles, meeting on mbarriers:
+//   lane 0 of warp 4 (loader): per column T, once the MMAs of the column that used its ring slot
+//     FT_RING columns earlier are done (done[slot]), two bulk copies into slot T % FT_RING (the
+//     column's strips, 6656 bytes, and the unit's 128 words, 2048 bytes) completing on wfull[slot];
 //   warps 5-20 (producers; warp w holds tensor-memory lanes 32 (w % 4) .. +31 = words, and group
-//     g = (w - 5) / 4 takes the columns it = g mod 4, so stage g): per column wait until the stage is
+//     g = (w - 5) / 4 takes the columns T = g mod 4, so stage g): per column wait until the stage is
 //     free (done of the group's previous column) and the words landed, expand the words with
 //     tcgen05.st, arrive full[g]. Four groups keep four columns' expansions in flight;
-//   lane 0 of warp i < 4 (issuer of range i % 2, K half i / 2): per column wait full[s], issue its
+//   lane 0 of warp i < 4 (issuer of range i % 2, K half i / 2): before a unit's first column wait
+//     until its D buffer was read out and cleared (dfree), then per column wait full[s], issue its
 //     2 MMAs (A from tensor memory, B = the range's strip through the Hankel descriptor) and commit
-//     to done[slot], which counts the four issuers. One thread issues a tcgen05 operation only
-//     about every 100 cycles, so the column's 8 MMAs come from four threads.
+//     to done[slot]; after the unit's last column commit to dfull. One thread issues a tcgen05
+//     operation only about every 100 cycles, so the column's 8 MMAs come from four threads;
+//   warps 21-24 (read-out; lane quarter w % 4 = the unit's rows): per unit wait dfull, read D and
+//     store each row's 162 coefficients, clear D (tcgen05.st) and arrive dfree.
 // Every wait is bounded; a timeout sets *status = 5 and the abort flag, on which every role leaves
-// its loop. The loader waits for its own copies in flight before the block reuses the ring, and
-// tensor memory is freed only after the issuers' last commits drained.
+// its loop. The loader waits for its own copies in flight before the block ends, and tensor memory
+// is freed only after the issuers' last commits drained.
+constexpr int FT_EPI_WARP = 5 + FT_PRODUCERS / 32;  // warps 21-24 read D out
+static_assert(FT_THREADS == 32 * FT_EPI_WARP + 128, "fold roles");
+
+struct FoldUnits {  // the CTA's units and their column runs
+  int nbx, cols_per_split;
+  uint64_t ring_elements;
+  __device__ int unit(int i) const { return blockIdx.x + i * gridDim.x; }
+  __device__ int c_begin(int u) const { return (u / nbx) * cols_per_split; }
+  __device__ int ncols(int u) const { return max(0, min(COLUMNS, c_begin(u) + cols_per_split) - c_begin(u)); }
+  __device__ uint64_t w0(int u) const { return (uint64_t)(u % nbx) * 128; }
+  __device__ int nw(int u) const { return (int)min((uint64_t)128, 4 * ring_elements - w0(u)); }
+};
+
 __global__ void __launch_bounds__(FT_THREADS, 1)
     k_fold_tc(const uint4* __restrict__ table, int rl, uint64_t ring_elements, const uint8_t* __restrict__ strips,
-              int cols_per_split, int32_t* __restrict__ part, int* status) {
+              int cols_per_split, int nunits, int32_t* __restrict__ part, int* status) {
   extern __shared__ __align__(1024) uint8_t fsm[];
   uint8_t* ring = fsm;                                                  // [FT_RING][FT_SLOT]: strips, words
-  uint64_t* done = reinterpret_cast<uint64_t*>(fsm + FT_BARS);          // [FT_RING] a slot's column's MMAs done
+  uint64_t* done = reinterpret_cast<uint64_t*>(fsm + FT_RING * FT_SLOT);  // [FT_RING] a slot's column's MMAs done
   uint64_t* full = done + FT_RING;                                      // [FT_STAGES] a stage written
   uint64_t* wfull = full + FT_STAGES;                                   // [FT_RING] a slot's copies landed
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(wfull + FT_RING);
+  uint64_t* dfull = wfull + FT_RING;                                    // [2] a D buffer's unit complete
+  uint64_t* dfree = dfull + 2;                                          // [2] a D buffer read out and cleared
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(dfree + 2);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const bool producer = warp >= 5;
-  const int row = 32 * (warp & 3) + lane, group = (warp - 5) >> 2;  // producers: word (A row), group
-  const uint64_t words = 4 * ring_elements;
-  const uint64_t w0 = (uint64_t)blockIdx.x * 128;  // first word (row) of the block
-  const int nw = (int)min((uint64_t)128, words - w0);
-  const int split = blockIdx.y;
-  const int c_begin = split * cols_per_split, c_end = min(COLUMNS, c_begin + cols_per_split);
-  const int ncols = c_end - c_begin;
+  const FoldUnits U{(int)((4 * ring_elements + 127) / 128), cols_per_split, ring_elements};
+  const int nu = blockIdx.x < nunits ? (nunits - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
   if (tid == 0) {
     *abort_flag = 0;
     for (int i = 0; i < FT_RING; ++i) {
@@ -396,6 +408,10 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
       tc::mbar_init(&wfull[i], 1);
     }
     for (int i = 0; i < FT_STAGES; ++i) tc::mbar_init(&full[i], FT_PRODUCERS / FT_STAGES);
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&dfull[i], FT_ISSUERS);
+      tc::mbar_init(&dfree[i], 128);
+    }
     tc::mbar_init_fence();
   }
   if (warp == 0) tc::tmem_alloc(tslot, 512);
@@ -403,12 +419,12 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
-  if (warp < 4) {  // D = 0: every MMA accumulates, in whatever order the issuers' MMAs arrive
-    uint32_t z[16];
+  uint32_t zero16[16];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) z[i] = 0;
-#pragma unroll
-    for (int n0 = 0; n0 < 2 * FT_N; n0 += 16) tc::tmem_st_x16(tbase + ((uint32_t)(32 * warp) << 16) + n0, z);
+  for (int i = 0; i < 16; ++i) zero16[i] = 0;
+  if (warp >= FT_EPI_WARP) {  // both D buffers = 0: every MMA accumulates, in any order of the issuers
+    for (int n0 = 0; n0 < 4 * FT_N; n0 += 16)
+      tc::tmem_st_x16(tbase + ((uint32_t)(32 * (warp & 3)) << 16) + n0, zero16);
     tc::tmem_wait_st();
   }
   tc::fence_before_sync();
@@ -422,114 +438,115 @@ __global__ void __launch_bounds__(FT_THREADS, 1)
     }
   };
 
-  int last = -1;
-  if (producer) {
-    const int s = group;
-    const uint32_t tA = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + 256 + 32 * s;
-    for (int it = group; it < ncols; it += FT_STAGES) {
-      const int slot = it % FT_RING;
-      bool ok = it < FT_STAGES || tc::mbar_wait_fast(&done[(it - FT_STAGES) % FT_RING],
-                                                     ((it - FT_STAGES) / FT_RING) & 1, abort_flag, FT_WAIT_CYCLES);
-      ok = ok && tc::mbar_wait_fast(&wfull[slot], (it / FT_RING) & 1, abort_flag, FT_WAIT_CYCLES);
+  if (warp >= 5 && warp < FT_EPI_WARP) {  // producers
+    const int group = (warp - 5) >> 2, s = group, row = 32 * (warp & 3) + lane;
+    const uint32_t tA = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + 384 + 32 * s;
+    int i = 0, it = group, T = group;  // unit, column within it, column of the stream
+    while (i < nu && it >= U.ncols(U.unit(i))) it -= U.ncols(U.unit(i)), ++i;
+    for (; i < nu; T += FT_STAGES) {
+      const int u = U.unit(i), slot = T % FT_RING;
+      bool ok = T < FT_STAGES || tc::mbar_wait_fast(&done[(T - FT_STAGES) % FT_RING],
+                                                    ((T - FT_STAGES) / FT_RING) & 1, abort_flag, FT_WAIT_CYCLES);
+      ok = ok && tc::mbar_wait_fast(&wfull[slot], (T / FT_RING) & 1, abort_flag, FT_WAIT_CYCLES);
       if (!__all_sync(0xffffffffu, ok)) give_up();
       if (!*abort_flag) {
         tc::fence_after_sync();
-        const uint4 v = row < nw ? reinterpret_cast<const uint4*>(ring + slot * FT_SLOT + FT_STRIP)[row]
-                                 : make_uint4(0, 0, 0, 0);
-        uint32_t u[32];
-        fold_expand_word(v, u);
-        tc::tmem_st_x16(tA, *reinterpret_cast<const uint32_t(*)[16]>(u));
-        tc::tmem_st_x16(tA + 16, *reinterpret_cast<const uint32_t(*)[16]>(u + 16));
+        const uint4 v = row < U.nw(u) ? reinterpret_cast<const uint4*>(ring + slot * FT_SLOT + FT_STRIP)[row]
+                                      : make_uint4(0, 0, 0, 0);
+        uint32_t w[32];
+        fold_expand_word(v, w);
+        tc::tmem_st_x16(tA, *reinterpret_cast<const uint32_t(*)[16]>(w));
+        tc::tmem_st_x16(tA + 16, *reinterpret_cast<const uint32_t(*)[16]>(w + 16));
         tc::tmem_wait_st();
       }
       tc::fence_before_sync();
       tc::mbar_arrive(&full[s]);
+      for (it += FT_STAGES; i < nu && it >= U.ncols(U.unit(i));) it -= U.ncols(U.unit(i)), ++i;
     }
   } else if (tid == 128) {  // loader
     int issued = 0;
-    for (int it = 0; it < ncols && !*abort_flag; ++it, ++issued) {
-      const int slot = it % FT_RING;
-      if (it >= FT_RING && !tc::mbar_wait(&done[slot], ((it / FT_RING) - 1) & 1, abort_flag, FT_WAIT_CYCLES)) {
-        give_up();
-        break;
+    for (int i = 0; i < nu && !*abort_flag; ++i) {
+      const int u = U.unit(i), nc = U.ncols(u), nw = U.nw(u), cb = U.c_begin(u);
+      const uint64_t w0 = U.w0(u);
+      for (int it = 0; it < nc && !*abort_flag; ++it, ++issued) {
+        const int T = issued, slot = T % FT_RING;
+        if (T >= FT_RING && !tc::mbar_wait(&done[slot], ((T / FT_RING) - 1) & 1, abort_flag, FT_WAIT_CYCLES)) {
+          give_up();
+          break;
+        }
+        uint8_t* dst = ring + slot * FT_SLOT;
+        tc::mbar_expect_tx(&wfull[slot], FT_STRIP + 16 * nw);
+        tc::bulk_load(dst, strips + (size_t)(cb + it) * FT_STRIP, FT_STRIP, &wfull[slot]);
+        tc::bulk_load(dst + FT_STRIP, table + ((uint64_t)(cb + it) << rl) + w0, 16 * nw, &wfull[slot]);
       }
-      const int c = c_begin + it;
-      uint8_t* dst = ring + slot * FT_SLOT;
-      tc::mbar_expect_tx(&wfull[slot], FT_STRIP + 16 * nw);
-      tc::bulk_load(dst, strips + (size_t)c * FT_STRIP, FT_STRIP, &wfull[slot]);
-      tc::bulk_load(dst + FT_STRIP, table + ((uint64_t)c << rl) + w0, 16 * nw, &wfull[slot]);
     }
-    // the copies in flight land before the block leaves or reuses the ring
-    for (int it = issued > FT_RING ? issued - FT_RING : 0; it < issued; ++it) {
+    // the copies in flight land before the block leaves
+    for (int T = issued > FT_RING ? issued - FT_RING : 0; T < issued; ++T) {
       const long long t0 = clock64();
-      while (!tc::mbar_try_wait(&wfull[it % FT_RING], (it / FT_RING) & 1) && clock64() - t0 < FT_WAIT_CYCLES) {
+      while (!tc::mbar_try_wait(&wfull[T % FT_RING], (T / FT_RING) & 1) && clock64() - t0 < FT_WAIT_CYCLES) {
       }
     }
   } else if (warp < FT_ISSUERS && lane == 0) {  // issuer: range warp % 2, MMAs kk = 2 (warp / 2) + 0, 1
     const int range = warp & 1, kh = warp >> 1;
-    const uint32_t d = tbase + FT_N * range, boff = FT_RCORES * 128 * range;
-    for (int it = 0; it < ncols; ++it) {
-      const int s = it % FT_STAGES, slot = it % FT_RING;
-      if (!tc::mbar_wait_fast(&full[s], (it / FT_STAGES) & 1, abort_flag, FT_WAIT_CYCLES) ||
-          !tc::mbar_wait_fast(&wfull[slot], (it / FT_RING) & 1, abort_flag, FT_WAIT_CYCLES))
-        give_up();
-      if (*abort_flag) break;
-      tc::fence_after_sync();
-      const uint32_t a0 = tbase + 256 + 32 * s, b0 = tc::smem_u32(ring + slot * FT_SLOT) + boff;
+    const uint32_t boff = FT_RCORES * 128 * range;
+    int T = 0, last = -1;
+    for (int i = 0; i < nu && !*abort_flag; ++i) {
+      const int buf = i & 1, nc = U.ncols(U.unit(i));
+      const uint32_t d = tbase + 2 * FT_N * buf + FT_N * range;
+      if (i >= 2 && !tc::mbar_wait(&dfree[buf], ((i >> 1) - 1) & 1, abort_flag, FT_WAIT_CYCLES)) give_up();
+      for (int it = 0; it < nc; ++it, ++T) {
+        const int s = T % FT_STAGES, slot = T % FT_RING;
+        if (!tc::mbar_wait_fast(&full[s], (T / FT_STAGES) & 1, abort_flag, FT_WAIT_CYCLES) ||
+            !tc::mbar_wait_fast(&wfull[slot], (T / FT_RING) & 1, abort_flag, FT_WAIT_CYCLES))
+          give_up();
+        if (*abort_flag) break;
+        tc::fence_after_sync();
+        const uint32_t a0 = tbase + 384 + 32 * s, b0 = tc::smem_u32(ring + slot * FT_SLOT) + boff;
 #pragma unroll
-      for (int k2 = 0; k2 < 2; ++k2) {  // K = 32 kk: k groups 2 kk, 2 kk + 1, so core e starts at 4 kk
-        const int kk = 2 * kh + k2;
-        tc::mma_e4m3_ta(d, a0 + 8 * kk, tc::sdesc(b0 + 4 * kk * 128, 256, 128), id96, 1u);
+        for (int k2 = 0; k2 < 2; ++k2) {  // K = 32 kk: k groups 2 kk, 2 kk + 1, so core e starts at 4 kk
+          const int kk = 2 * kh + k2;
+          tc::mma_e4m3_ta(d, a0 + 8 * kk, tc::sdesc(b0 + 4 * kk * 128, 256, 128), id96, 1u);
+        }
+        tc::mma_commit(&done[slot]);
+        last = T;
       }
-      tc::mma_commit(&done[slot]);
-      last = it;
+      if (!*abort_flag) tc::mma_commit(&dfull[buf]);
     }
     if (last >= 0) {  // drain: the last commits cover every MMA
       const long long t0 = clock64();
       while (!tc::mbar_try_wait(&done[last % FT_RING], (last / FT_RING) & 1) && clock64() - t0 < FT_WAIT_CYCLES) {
       }
     }
-  }
-  bool ok = !*abort_flag;
-  if (ok && ncols > 0) {
-    const int lt = ncols - 1;
-    ok = __all_sync(0xffffffffu, tc::mbar_wait(&done[lt % FT_RING], (lt / FT_RING) & 1, abort_flag,
-                                                FT_WAIT_CYCLES));
-  }
-  ok = __syncthreads_and(ok);
-  tc::fence_after_sync();
-  // The coefficients per row into shared memory (the ring is free now): fin[row][i], i < 162.
-  int32_t* fin = reinterpret_cast<int32_t*>(fsm);
-  const int FS = N162 + 1;
-  if (tid < 128 && !(ok && ncols > 0))  // (otherwise every coefficient is written below)
-    for (int i = 0; i < N162; ++i) fin[tid * FS + i] = 0;
-  if (ok && ncols > 0 && tid < 128) {  // warps 0-3: TMEM lanes 32 w .. 32 w + 31 = the block's rows
-#pragma unroll 1
-    for (int n0 = 0; n0 < 2 * FT_N; n0 += 16) {
-      uint32_t v[16];
-      tc::tmem_ld_x16(tbase + ((uint32_t)(32 * warp) << 16) + n0, v);
-      tc::tmem_wait_ld(v);
-#pragma unroll
-      for (int t = 0; t < 16; ++t) {
-        const int n = n0 + t, high = n >= FT_N, nn = high ? n - FT_N : n;
-        if (nn >= 81) continue;  // padding columns of a range
-        fin[tid * FS + (high ? 161 - nn : 80 - nn)] = (int32_t)__float2int_rn(__uint_as_float(v[t]));
+  } else if (warp >= FT_EPI_WARP) {  // read-out: row r = 4 m + k of the unit = TMEM lane r
+    const int qd = warp & 3, r = 32 * qd + lane;
+    for (int i = 0; i < nu; ++i) {
+      const int u = U.unit(i), buf = i & 1;
+      if (!__all_sync(0xffffffffu, tc::mbar_wait(&dfull[buf], (i >> 1) & 1, abort_flag, FT_WAIT_CYCLES))) {
+        give_up();
+        break;
       }
+      tc::fence_after_sync();
+      const uint64_t m0 = U.w0(u) / 4;
+      const int nel = (int)min((uint64_t)32, ring_elements - m0), m = r >> 2, k = r & 3;
+      // part[split][(m0 + m) * 648 + 4 i + k]: four rows of an element fill 16 consecutive bytes
+      int32_t* dst = part + ((uint64_t)(u / U.nbx) * ring_elements + m0 + m) * 648 + k;
+      const uint32_t tb = tbase + ((uint32_t)(32 * qd) << 16) + 2 * FT_N * buf;
+#pragma unroll 1
+      for (int n0 = 0; n0 < 2 * FT_N; n0 += 16) {
+        uint32_t v[16];
+        tc::tmem_ld_x16(tb + n0, v);
+        tc::tmem_wait_ld(v);
+#pragma unroll
+        for (int t = 0; t < 16; ++t) {
+          const int n = n0 + t, high = n >= FT_N, nn = high ? n - FT_N : n;
+          if (nn < 81 && m < nel) dst[4 * (high ? 161 - nn : 80 - nn)] = (int32_t)__float2int_rn(__uint_as_float(v[t]));
+        }
+        tc::tmem_st_x16(tb + n0, zero16);  // cleared for the unit after next
+      }
+      tc::tmem_wait_st();
+      tc::fence_before_sync();
+      tc::mbar_arrive(&dfree[buf]);
     }
-  }
-  __syncthreads();
-  if (ok) {
-    // row = 4 m + k; part[split][(w0 / 4 + m) * 648 + 4 i + k], coalesced over the block's elements
-    const uint64_t m0 = w0 / 4;
-    const int nel = (int)min((uint64_t)32, ring_elements - m0);
-    int32_t* dst = part + ((uint64_t)split * ring_elements + m0) * 648;
-    static_assert(FT_THREADS >= 648, "one coefficient slot per thread");
-    if (tid < 648) {
-      const int* src = fin + (tid & 3) * FS + (tid >> 2);
-      for (int m = 0; m < nel; ++m) dst[m * 648 + tid] = src[4 * m * FS];
-    }
-  } else if (tid == 0) {
-    atomicExch(status, 5);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -566,9 +583,17 @@ void launch_fold(const uint4* table, int rl, uint64_t ring_elements, const Chall
   static std::atomic<unsigned long long> attr{0};
   smem_limit(k_fold_tc, FT_SMEM, attr);
   k_fold_cores<<<COLUMNS, 128, 0, s>>>(ch, strips);
-  const unsigned blocks = (unsigned)((4 * ring_elements + 127) / 128);
+  static int sms = 0;  // one CTA per SM (the kernel walks its units)
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  const int units = (int)((4 * ring_elements + 127) / 128) * splits;
   const int per = (COLUMNS + splits - 1) / splits;
-  k_fold_tc<<<dim3(blocks, splits), FT_THREADS, FT_SMEM, s>>>(table, rl, ring_elements, strips, per, part, status);
+  k_fold_tc<<<(unsigned)std::min(units, sms), FT_THREADS, FT_SMEM, s>>>(table, rl, ring_elements, strips, per, units,
+                                                                        part, status);
   k_fold_sum<<<1024, 256, 0, s>>>(part, splits, ring_elements * 648, out, status);
 }
 
