@@ -73,6 +73,23 @@ constexpr int WEIGHT = 28;
 constexpr int PHASE_LANES = 88;
 constexpr uint64_t MAX_ATTEMPTS = 1ull << 22;
 
+// Per draw i of an attempt (n = 162 - i candidates): the rejection limit (65536 / n) * n and the
+// multiplier (2^32 / n) + 1 whose high product word is r / n for every r < 2^16, tabulated so that
+// no draw divides.
+struct DrawConsts {
+  uint32_t limit[WEIGHT], magic[WEIGHT];
+};
+constexpr DrawConsts make_draw_consts() {
+  DrawConsts d{};
+  for (int i = 0; i < WEIGHT; ++i) {
+    const uint32_t n = (uint32_t)(N162 - i);
+    d.limit[i] = (65536u / n) * n;
+    d.magic[i] = (uint32_t)((1ull << 32) / n + 1);
+  }
+  return d;
+}
+__constant__ DrawConsts kDraw = make_draw_consts();
+
 struct ChWarp {
   uint8_t buf[XOF_BUF];
   uint8_t perm[176];
@@ -138,8 +155,8 @@ __global__ void __launch_bounds__(32 * CH_WARPS) k_challenges(const bk::Hasher* 
     __syncwarp();
     for (int i = 0; i < WEIGHT; ++i) {
       const uint32_t nn = (uint32_t)(N162 - i);
-      const uint32_t limit = (65536u / nn) * nn;
-      const uint64_t magic = (1ull << 32) / nn + 1;
+      const uint32_t limit = kDraw.limit[i];
+      const uint64_t magic = kDraw.magic[i];
       uint32_t r;
       do {
         uint32_t lo = byte();
@@ -187,14 +204,21 @@ __global__ void __launch_bounds__(32 * CH_WARPS) k_challenges(const bk::Hasher* 
     // Inside that window (rare) the lane repeats the reference's f64 sequence exactly.
     const float bound_f = (float)bound_sq;
     bool over = false;
+    // The attempt's 28 table rows, then all 56 loads of a lane's phase at once (one load latency
+    // per phase lane instead of 28 dependent ones: the loop ran 26 us per attempt rolled).
+    int rowoff[WEIGHT];
+#pragma unroll
+    for (int t = 0; t < WEIGHT; ++t) rowoff[t] = sorted[wid][t] * PHASE_LANES;
     for (int k = lane; k < 81; k += 32) {
+      float pr[WEIGHT], pi[WEIGHT];
+#pragma unroll
+      for (int t = 0; t < WEIGHT; ++t) pr[t] = __ldg(re32 + rowoff[t] + k), pi[t] = __ldg(im32 + rowoff[t] + k);
       float fr = 0.0f, fi = 0.0f;
+#pragma unroll
       for (int t = 0; t < WEIGHT; ++t) {
-        const int b = sorted[wid][t] * PHASE_LANES + k;
-        const float pr = re32[b], pi = im32[b];
         const bool neg = (signs >> t) & 1;
-        fr += neg ? -pr : pr;
-        fi += neg ? -pi : pi;
+        fr += neg ? -pr[t] : pr[t];
+        fi += neg ? -pi[t] : pi[t];
       }
       const float m2f = fr * fr + fi * fi;
       const bool traced = trace && attempt == 0 && k == 0;  // the diagnostic records the f64 values
