@@ -90,20 +90,23 @@ constexpr DrawConsts make_draw_consts() {
 }
 __constant__ DrawConsts kDraw = make_draw_consts();
 
-struct ChWarp {
+struct __align__(16) ChWarp {
   uint8_t buf[XOF_BUF];
   uint8_t perm[176];
   uint32_t root[27];
 };
 
-__device__ __forceinline__ void xof_refill(ChWarp& s, const bk::Pending& root, uint64_t& next_block, int lane) {
-  __syncwarp();  // every lane has read the previous buffer before any lane overwrites it
-  uint32_t w[16];
-  root.root_block(next_block + lane, w);
-  uint32_t* dst = reinterpret_cast<uint32_t*>(s.buf + 64 * lane);
+// The XOF output as a ring of 32 blocks of 64 bytes: blocks [lo, lo + 32) of the stream sit in
+// slots block % 32. xof_blocks(first, count): lanes < count produce blocks first + lane.
+__device__ __forceinline__ void xof_blocks(ChWarp& s, const bk::Pending& root, uint64_t first, int count, int lane) {
+  __syncwarp();  // every lane has read the slots before any lane overwrites them
+  if (lane < count) {
+    uint32_t w[16];
+    root.root_block(first + lane, w);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(s.buf + 64 * ((first + lane) % 32));
 #pragma unroll
-  for (int i = 0; i < 16; ++i) dst[i] = w[i];
-  next_block += 32;
+    for (int i = 0; i < 16; ++i) dst[i] = w[i];
+  }
   __syncwarp();
 }
 
@@ -138,57 +141,66 @@ __global__ void __launch_bounds__(32 * CH_WARPS) k_challenges(const bk::Hasher* 
   root.t = s.root[24];
   root.len = s.root[25];
   root.flags = s.root[26];
-  uint64_t next_block = 0;
-  int pos = XOF_BUF;
+  // The byte stream: the next byte is at A (even: every draw reads two), the ring holds blocks
+  // [lo, lo + 32). An attempt starts with at least 160 bytes ahead (56 without rejected draws).
+  uint64_t lo = 0, A = 0;
+  xof_blocks(s, root, 0, 32, lane);
   const bool trace = dbg != nullptr && ci == 0;
   if (trace && lane == 0)
     for (int i = 0; i < 27; ++i) dbg[i] = s.root[i];
-  auto byte = [&]() -> uint32_t {
-    if (pos == XOF_BUF) {
-      xof_refill(s, root, next_block, lane);
-      pos = 0;
-    }
-    return s.buf[pos++];
+  auto advance = [&]() {  // the oldest 16 blocks (read) make room for the next 16
+    xof_blocks(s, root, lo + 32, 16, lane);
+    lo += 16;
   };
   for (uint64_t attempt = 0; attempt < MAX_ATTEMPTS; ++attempt) {
+    if (A + 160 > (lo + 32) * 64) advance();
     for (int i = lane; i < N162; i += 32) s.perm[i] = (uint8_t)i;
     __syncwarp();
-    for (int i = 0; i < WEIGHT; ++i) {
-      const uint32_t nn = (uint32_t)(N162 - i);
-      const uint32_t limit = kDraw.limit[i];
-      const uint64_t magic = kDraw.magic[i];
-      uint32_t r;
-      do {
-        uint32_t lo = byte();
-        uint32_t hi = byte();
-        r = lo | (hi << 8);
-      } while (r >= limit);
-      uint32_t q = (uint32_t)(((uint64_t)r * magic) >> 32);
-      int j = i + (int)(r - q * nn);
+    // Lane 0 alone runs the partial Fisher-Yates (no warp barrier per draw): draw i reads a
+    // little-endian u16, rejects it above the largest multiple of n = 162 - i, and swaps slot i
+    // with slot i + r mod n.
+    for (int i = 0;;) {
       if (lane == 0) {
-        uint8_t t = s.perm[i];
-        s.perm[i] = s.perm[j];
-        s.perm[j] = t;
+        while (i < WEIGHT && A + 2 <= (lo + 32) * 64) {
+          const uint32_t r = *reinterpret_cast<const uint16_t*>(s.buf + (A % XOF_BUF));
+          A += 2;
+          if (r >= kDraw.limit[i]) continue;
+          const uint32_t nn = (uint32_t)(N162 - i);
+          const uint32_t q = (uint32_t)(((uint64_t)r * kDraw.magic[i]) >> 32);
+          const int j = i + (int)(r - q * nn);
+          const uint8_t t = s.perm[i];
+          s.perm[i] = s.perm[j];
+          s.perm[j] = t;
+          ++i;
+        }
       }
-      __syncwarp();
+      i = __shfl_sync(0xffffffffu, i, 0);
+      A = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(A >> 32), 0) << 32) | __shfl_sync(0xffffffffu, (uint32_t)A, 0);
+      if (i == WEIGHT) break;
+      advance();  // (more than 52 rejected draws in one attempt)
     }
+    __syncwarp();
     // Sorted positions: lane l < 28 places perm[l] by its rank.
     uint32_t mine = lane < WEIGHT ? s.perm[lane] : 255;
     int rank = 0;
     for (int t = 0; t < WEIGHT; ++t) rank += (int)(s.perm[t] < mine);
     __syncwarp();
-    __shared__ uint8_t sorted[CH_WARPS][32];
+    __shared__ __align__(4) uint8_t sorted[CH_WARPS][32];
+    static_assert(WEIGHT % 4 == 0, "positions fill whole message words");
     if (lane < WEIGHT) sorted[wid][rank] = (uint8_t)mine;
     __syncwarp();
     // Signs: derive-key hash of (weight as u64 LE || positions), first four bytes LE.
     uint32_t signs = 0;
     if (lane == 0) {
-      uint8_t blk[64];
-      for (int i = 0; i < 64; ++i) blk[i] = 0;
-      blk[0] = (uint8_t)WEIGHT;
-      for (int i = 0; i < WEIGHT; ++i) blk[8 + i] = sorted[wid][i];
+      // the block (weight as u64 LE || the 28 positions) as message words, straight from the
+      // sorted positions (4 per word, little-endian) without a byte array in local memory
       uint32_t m[16], o[16];
-      bk::load_words(blk, m, 16);
+      const uint32_t* sp = reinterpret_cast<const uint32_t*>(sorted[wid]);
+      m[0] = (uint32_t)WEIGHT, m[1] = 0;
+#pragma unroll
+      for (int q = 0; q < WEIGHT / 4; ++q) m[2 + q] = sp[q];
+#pragma unroll
+      for (int q = 2 + WEIGHT / 4; q < 16; ++q) m[q] = 0;
       bk::compress16(sign_key_node.h, m, 0, 8 + WEIGHT, sign_key_node.flags | bk::F_ROOT, o);
       signs = o[0] & ((1u << WEIGHT) - 1);
     }
