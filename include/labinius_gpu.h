@@ -236,7 +236,7 @@ int lf_sample_challenges_noalloc(int device, const char* domain, const uint8_t* 
  * a pending point. LF_E_ARGS from the proof if n does not match its shape.
  *
  * lf_test_withhold_table_part: if that proof streams a page-locked table (lf_prove), the ready flag
- * of element range `part` (0..63; a table is streamed in min(64, ring elements per column) ranges) is not written, and the commitment kernel gives up waiting for it
+ * of element range `part` (0..63; a table is streamed in min(64, ring elements per column / 16) ranges, at least one) is not written, and the commitment kernel gives up waiting for it
  * after wait_cycles SM cycles (0 = its default of about a second): the proof returns LF_E_INTERNAL
  * and the context stays usable. */
 int lf_test_set_point(lf_ctx* ctx, const uint8_t* r_hi, uint32_t n);

@@ -163,7 +163,7 @@ def test_withheld_table_part_times_out_and_context_recovers(gpu_lib, oracle):
     # timeout and leaves (tensor memory freed after its last MMAs drained), and the proof reports
     # LF_E_INTERNAL. The context then proves the next table, streamed again, correctly.
     torch = pytest.importorskip("torch")
-    log_vars = 24  # 64 ring elements per column: 64 parts of one
+    log_vars = 27  # 256 ring elements per column: 16 parts of 16
     table = oracle.write_table(SEED, log_vars)
     host = torch.empty(len(table), dtype=torch.uint8, pin_memory=True)
     host.numpy()[:] = bytearray(table)
