@@ -562,7 +562,10 @@ def main():
     tuned = None
     if not args.no_tune:  # lf_tune: the commitment's split count measured on this GPU (proofs unchanged)
         sp, tms, cand = prover.tune(log_vars, tables[0].data_ptr())
-        tuned = {"commit_splits": sp, "commit_ms": round(tms, 3), "candidates": cand}
+        lt = prover.last_tune
+        tuned = {"commit_splits": sp, "commit_ms": round(tms, 3), "candidates": cand,
+                 "fold_splits": lt["fold_splits"], "fold_ms": round(lt["fold_ms"], 3),
+                 "fold_candidates": lt["fold_candidates"]}
     nt = len(ss)
     warm = max(3, args.warmup)
     for i in range(warm):

@@ -158,11 +158,17 @@ int lf_submit(lf_ctx* ctx, const lf_job* job, uint64_t* ticket);
  * is measured on this device for the shape, using table_dev (a device table of the shape: the
  * result does not depend on its content), over the candidates whose last wave is at least 3/4
  * full; the fastest is kept for this shape and modulus on every lane of the context (the proof
- * bytes do not depend on it). Without tuning a wave-balance heuristic chooses. */
+ * bytes do not depend on it). The fold's column-run count (its persistent kernel walks row blocks
+ * x runs work units over the SMs) is measured the same way, over the counts whose last round of
+ * units fills at least 3/4 of the SMs, and kept for the shape. Without tuning wave-balance
+ * heuristics choose both. */
 typedef struct lf_tune_result {
-  int commit_splits;  /* the count kept */
-  float commit_ms;    /* its measured commitment time */
-  int candidates;     /* counts measured */
+  int commit_splits;   /* the count kept */
+  float commit_ms;     /* its measured commitment time */
+  int candidates;      /* counts measured */
+  int fold_splits;     /* the fold's column-run count kept */
+  float fold_ms;       /* its measured fold time (strips, product, sum of the runs) */
+  int fold_candidates; /* run counts measured */
 } lf_tune_result;
 int lf_tune(lf_ctx* ctx, const uint8_t q_le[16], uint32_t log_vars, const void* table_dev, lf_tune_result* out);
 

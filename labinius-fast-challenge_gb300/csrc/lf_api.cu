@@ -254,6 +254,12 @@ struct lf_ctx {
     auto it = tuned_splits.find({sh.log_vars, nprimes});
     return it != tuned_splits.end() ? it->second : commit_splits(sh.ring_elements, nprimes, sms);
   }
+  // column runs of the fold per log_vars chosen by lf_tune; the wave-balance heuristic otherwise
+  std::map<int, int> tuned_fold;
+  int fold_split_for(const Shape& sh) const {
+    auto it = tuned_fold.find(sh.log_vars);
+    return it != tuned_fold.end() ? it->second : fold_splits(sh.ring_elements, sms);
+  }
   // switch rounds: msg (device) accumulates a round's message, msg_out (page-locked, mapped) receives
   // it from the last block of the round's kernel
   unsigned long long* msg_out = nullptr;
@@ -940,7 +946,7 @@ int prove_device(lf_ctx* ctx, const uint8_t seed[32], u128 q, const Shape& sh, c
 
   // ---- fold (reference.rs:72-133), straight into the proof's i32 region ----
   CK(ctx->fold.ensure(fold_bytes));
-  const int fsplits = fold_splits(sh.ring_elements, ctx->sms);
+  const int fsplits = ctx->fold_split_for(sh);
   CK(ctx->fold_strips.ensure(COLUMNS * FOLD_STRIP_BYTES));
   CK(ctx->fold_part.ensure((size_t)fsplits * fold_bytes));
   launch_fold(table, sh.rl, sh.ring_elements, ctx->chal.as<Challenge>(), ctx->fold_strips.as<uint8_t>(),
@@ -1968,14 +1974,55 @@ int lf_tune(lf_ctx* ctx, const uint8_t q_le[16], uint32_t log_vars, const void* 
   CK(cudaMemcpy(&status, ctx->status.p, 4, cudaMemcpyDeviceToHost));
   if (status) return fail(ctx, LF_E_INTERNAL, "the commitment kernel failed while tuning");
   ctx->tuned_splits[{sh.log_vars, mp.nprimes}] = best;
+
+  // The fold's column-run count: the persistent kernel walks nbx x runs work units over the SMs,
+  // so counts whose units fill the SMs' last round at least 3/4 are timed (the whole fold: strips,
+  // the product and the runs' sum). Challenges of all-zero positions stand in for the proof's own
+  // (the time does not depend on the values).
+  const size_t fold_bytes = 4 * RING_N * sh.ring_elements;
+  const long nbx = (long)((4 * sh.ring_elements + 127) / 128);
+  int fbest = fold_splits(sh.ring_elements, ctx->sms), ftried = 0;
+  float fbest_ms = 1e30f;
+  CK(ctx->chal.ensure(COLUMNS * sizeof(Challenge)));
+  CK(cudaMemsetAsync(ctx->chal.p, 0, COLUMNS * sizeof(Challenge), st));
+  CK(ctx->fold.ensure(fold_bytes));
+  CK(ctx->fold_strips.ensure(COLUMNS * FOLD_STRIP_BYTES));
+  CK(cudaMemsetAsync(ctx->status.p, 0, 16, st));
+  for (int sp = 1; sp <= 32; ++sp) {
+    const long units = nbx * sp, rounds = (units + ctx->sms - 1) / ctx->sms;
+    if ((double)units / (double)(rounds * ctx->sms) < 0.75 && sp != fbest) continue;
+    CK(ctx->fold_part.ensure((size_t)sp * fold_bytes));
+    float ms = 0;
+    for (int rep = 0; rep < 2; ++rep) {  // the second run is timed
+      cudaEventRecord(ctx->ev[12], st);
+      launch_fold(table, sh.rl, sh.ring_elements, ctx->chal.as<Challenge>(), ctx->fold_strips.as<uint8_t>(),
+                  ctx->fold_part.as<int32_t>(), sp, ctx->fold.as<int32_t>(), ctx->status.as<int>(), st);
+      cudaEventRecord(ctx->ev[13], st);
+      CKL("tuning the fold");
+      CK(cudaEventSynchronize(ctx->ev[13]));
+      cudaEventElapsedTime(&ms, ctx->ev[12], ctx->ev[13]);
+    }
+    ++ftried;
+    if (ms < fbest_ms) fbest_ms = ms, fbest = sp;
+  }
+  CK(cudaMemcpy(&status, ctx->status.p, 4, cudaMemcpyDeviceToHost));
+  if (status) return fail(ctx, LF_E_INTERNAL, "the fold kernel failed while tuning");
+  ctx->tuned_fold[sh.log_vars] = fbest;
   for (lf_ctx* l : lanes) {
     std::lock_guard<std::mutex> gl(l->mu);
     l->tuned_splits[{sh.log_vars, mp.nprimes}] = best;
+    l->tuned_fold[sh.log_vars] = fbest;
+    cudaSetDevice(l->device);
+    if (l->fold_part.ensure((size_t)fbest * fold_bytes) != cudaSuccess)  // no lane grows it inside a proof
+      return fail(ctx, LF_E_OOM, "fold run buffer of a lane");
   }
   if (out) {
     out->commit_splits = best;
     out->commit_ms = best_ms;
     out->candidates = tried;
+    out->fold_splits = fbest;
+    out->fold_ms = fbest_ms;
+    out->fold_candidates = ftried;
   }
   return LF_OK;
 }

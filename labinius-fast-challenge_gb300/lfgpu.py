@@ -41,7 +41,8 @@ class LfError(RuntimeError):
 
 
 class TuneResult(ctypes.Structure):
-    _fields_ = [("commit_splits", ctypes.c_int), ("commit_ms", ctypes.c_float), ("candidates", ctypes.c_int)]
+    _fields_ = [("commit_splits", ctypes.c_int), ("commit_ms", ctypes.c_float), ("candidates", ctypes.c_int),
+                ("fold_splits", ctypes.c_int), ("fold_ms", ctypes.c_float), ("fold_candidates", ctypes.c_int)]
 
 
 class Config(ctypes.Structure):
@@ -278,9 +279,11 @@ class Prover:
         return self.lib.lf_request_footprint(self.ctx, q_bytes(q), log_vars, 1 if host_table else 0)
 
     def tune(self, log_vars, table_dev, q=BASELINE_Q):
-        """lf_tune: the commitment's split count measured for this shape; (splits, ms, candidates)."""
+        """lf_tune: the commitment's split count and the fold's column-run count measured for this
+        shape; returns (commit splits, commit ms, candidates), the whole result in self.last_tune."""
         r = TuneResult()
         self._check(self.lib.lf_tune(self.ctx, q_bytes(q), log_vars, ctypes.c_void_p(table_dev), ctypes.byref(r)))
+        self.last_tune = {f: getattr(r, f) for f, _ in TuneResult._fields_}
         return r.commit_splits, r.commit_ms, r.candidates
 
     def ring_mul(self, q, n, a_dev, b_dev, c_dev):

@@ -154,7 +154,8 @@ def test_many_device_challenges_match_oracle(prover, oracle, prefix):
 
 
 def test_tuned_split_count_keeps_the_proof(gpu_lib, oracle):
-    # lf_tune changes only the commitment's grid depth; the proof must stay the oracle's
+    # lf_tune changes only the commitment's grid depth and the fold's column-run count; the proof
+    # must stay the oracle's
     seed = SEEDS[0]
     log_vars = 21
     table = oracle.write_table(seed, log_vars)
@@ -164,6 +165,8 @@ def test_tuned_split_count_keeps_the_proof(gpu_lib, oracle):
             p.h2d(dev, table)
             splits, ms, tried = p.tune(log_vars, dev)
             assert splits >= 1 and ms > 0 and tried >= 1
+            assert p.last_tune["fold_splits"] >= 1 and p.last_tune["fold_ms"] > 0
+            assert p.last_tune["fold_candidates"] >= 1
             got = p.prove(seed, table, log_vars)
         finally:
             p.free(dev)
