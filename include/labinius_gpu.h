@@ -246,6 +246,11 @@ int lf_sample_challenges_noalloc(int device, const char* domain, const uint8_t* 
  * after wait_cycles SM cycles (0 = its default of about a second): the proof returns LF_E_INTERNAL
  * and the context stays usable. */
 int lf_test_set_point(lf_ctx* ctx, const uint8_t* r_hi, uint32_t n);
+/* lf_test_table_part_order (host only): the copy order of a streamed table's parts for a
+ * commitment grid of `splits` element splits of blocks_per_split blocks each on `sms` SMs, as
+ * lf_prove uses it; order receives *nparts part indices (at most 64). */
+int lf_test_table_part_order(uint64_t ring_elements, int splits, int blocks_per_split, int sms, uint8_t* order,
+                             int* nparts);
 int lf_test_withhold_table_part(lf_ctx* ctx, int part, uint64_t wait_cycles);
 
 const char* lf_strerror(int code);

@@ -639,6 +639,15 @@ struct TableStream {
   uint8_t order[TABLE_PARTS];  // the copy order of the parts (order_table_parts)
 };
 
+// The parts of a streamed table of `elements` ring elements per column: up to TABLE_PARTS ranges of
+// at least 16 elements (1 KB rows of the 2-D copy; shorter rows copy slowly and cost a batch of
+// small tables 13 % of its throughput), the last one shorter.
+void table_parts(uint64_t elements, int* part_elems, int* nparts) {
+  const uint64_t want = std::max<uint64_t>(1, std::min<uint64_t>(TABLE_PARTS, elements / 16));
+  *part_elems = (int)((elements + want - 1) / want);
+  *nparts = (int)((elements + *part_elems - 1) / *part_elems);
+}
+
 // Queues parts order[ts->next .. end) of a streamed table on the copy stream, each followed by its
 // ready flag; once every part is queued, `done` (and the upload's end) is recorded after them.
 int enqueue_table_parts(lf_ctx* ctx, TableStream* ts, int end) {
@@ -1044,13 +1053,11 @@ int start_table_upload(lf_ctx* ctx, const void* table, size_t table_bytes, const
   *streamed = locked && ctx->write_value && sh.ring_elements >= (uint64_t)TABLE_MIN_PARTS;
   if (*streamed) {
     const uint32_t epoch = ++ctx->epoch == 0 ? ++ctx->epoch : ctx->epoch;  // never 0, the flags' initial value
-    // parts of at least 16 elements (1 KB rows of the 2-D copy; shorter rows copy slowly and
-    // cost a batch of small tables 13 % of its throughput), at most TABLE_PARTS
-    const uint64_t want = std::max<uint64_t>(1, std::min<uint64_t>(TABLE_PARTS, sh.ring_elements / 16));
-    const int part_elems = (int)((sh.ring_elements + want - 1) / want);
+    int part_elems = 0, nparts = 0;
+    table_parts(sh.ring_elements, &part_elems, &nparts);
     *ts = TableStream{ctx->ready, epoch, part_elems, ctx->uploaded[0], static_cast<const uint8_t*>(table),
                       (size_t)16 << sh.rl, sh.ring_elements, 0, ctx->test_withhold, ctx->test_ready_wait,
-                      (int)((sh.ring_elements + part_elems - 1) / part_elems), {}};
+                      nparts, {}};
     for (int i = 0; i < ts->nparts; ++i) ts->order[i] = (uint8_t)i;
     return enqueue_table_parts(ctx, ts, 1);  // the rest once the commitment's layout is known
   }
@@ -2214,6 +2221,20 @@ int lf_test_withhold_table_part(lf_ctx* ctx, int part, uint64_t wait_cycles) {
   std::lock_guard<std::mutex> g(ctx->mu);
   ctx->test_withhold = part;
   ctx->test_ready_wait = (long long)std::min<uint64_t>(wait_cycles, (uint64_t)1 << 40);
+  return LF_OK;
+}
+
+int lf_test_table_part_order(uint64_t ring_elements, int splits, int blocks_per_split, int sms, uint8_t* order,
+                             int* nparts) {
+  if (!order || !nparts || ring_elements < 1 || splits < 1 || blocks_per_split < 1 || sms < 1) return LF_E_ARGS;
+  TableStream ts{};
+  ts.elements = ring_elements;
+  table_parts(ring_elements, &ts.part_elems, &ts.nparts);
+  for (int i = 0; i < ts.nparts; ++i) ts.order[i] = (uint8_t)i;
+  ts.next = 1;  // part 0 goes up first, before the commitment's layout is known
+  order_table_parts(&ts, splits, blocks_per_split, sms);
+  for (int i = 0; i < ts.nparts; ++i) order[i] = ts.order[i];
+  *nparts = ts.nparts;
   return LF_OK;
 }
 

@@ -30,7 +30,7 @@ EXPORTS = [
     "lf_last_profile", "lf_strerror", "lf_last_error", "lf_last_challenges",
     "lf_sample_challenges", "lf_sample_challenges_noalloc", "lf_prove_batch", "lf_submit", "lf_poll",
     "lf_verify", "lf_verify_device", "lf_request_footprint", "lf_ring_mul", "lf_ghash_mul", "lf_ajtai_matrix_device",
-    "lf_a_times_v", "lf_tune", "lf_test_set_point", "lf_test_withhold_table_part",
+    "lf_a_times_v", "lf_tune", "lf_test_set_point", "lf_test_withhold_table_part", "lf_test_table_part_order",
 ]
 
 
@@ -123,6 +123,8 @@ def load(path=LIB_PATH):
                                                  u8p, p]
     lib.lf_test_set_point.argtypes = [p, ctypes.c_char_p, ctypes.c_uint32]
     lib.lf_test_withhold_table_part.argtypes = [p, ctypes.c_int, ctypes.c_uint64]
+    lib.lf_test_table_part_order.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, u8p,
+                                             ctypes.POINTER(ctypes.c_int)]
     _lib = lib
     return lib
 
@@ -144,6 +146,17 @@ def sample_challenges_noalloc(domain, prefix, n, device=0, stream=None):
     if rc != LF_OK:
         raise LfError(rc, load().lf_strerror(rc).decode())
     return _parse_challenges(bytes(buf), n)
+
+
+def table_part_order(ring_elements, splits, blocks_per_split, sms):
+    """lf_test_table_part_order (host only): the copy order lf_prove gives a streamed table's parts."""
+    lib = load()
+    buf = (ctypes.c_uint8 * 64)()
+    n = ctypes.c_int()
+    rc = lib.lf_test_table_part_order(ring_elements, splits, blocks_per_split, sms, buf, ctypes.byref(n))
+    if rc != LF_OK:
+        raise LfError(rc, "table part order")
+    return list(buf[:n.value])
 
 
 def q_bytes(q):

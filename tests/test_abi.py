@@ -72,3 +72,22 @@ def test_test_hooks_check_their_arguments(gpu_lib):
     lib = gpu_lib.load()
     assert lib.lf_test_set_point(None, b"", 0) == -1
     assert lib.lf_test_withhold_table_part(None, 0, 0) == -1
+    assert lib.lf_test_table_part_order(0, 1, 1, 1, None, None) == -1
+
+
+def test_streamed_table_parts_go_up_in_the_order_the_commitment_reads_them(gpu_lib):
+    # 2^31 bits: 4096 ring elements per column in 64 parts of 64; the commitment's grid runs 21
+    # element splits of 196 elements, 72 blocks each (3 primes x 3 leaf thirds x 8 column groups),
+    # 152 at a time. Splits 0, 1 and 2 start in the first wave at elements 0, 196 and 392 (parts 0,
+    # 3 and 6); then each part by when a split's blocks reach it (448, 256, 64: parts 7, 4, 1).
+    order = gpu_lib.table_part_order(4096, 21, 72, 152)
+    assert sorted(order) == list(range(64))
+    assert order[:3] == [0, 3, 6]
+    assert order[3:6] == [7, 4, 1]
+    # parts of at least 16 elements: a 2^24-bit table (64 elements) goes up in 4 parts, 2^23 in 2,
+    # a table of fewer than 32 elements in one
+    assert sorted(gpu_lib.table_part_order(64, 4, 72, 152)) == [0, 1, 2, 3]
+    assert gpu_lib.table_part_order(32, 1, 72, 152) == [0, 1]
+    assert gpu_lib.table_part_order(20, 1, 72, 152) == [0]
+    # one split, one wave: the parts in index order
+    assert gpu_lib.table_part_order(1024, 1, 72, 152) == list(range(64))
