@@ -842,7 +842,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
 // B tiles of K1 on the tensor cores, per (prime, third): row 8 g + i = leaf 9 g + i of the third
 // for i < 8, row 48 + g = leaf 9 g + 8 (rows 54..63 zero); K position kappa < 128 carries the low limb of bit j(kappa),
-// kappa >= 128 the high limb of bit j(kappa - 128), j in the K order of tc::write_row; bf16 in
+// kappa >= 128 the high limb of bit j(kappa - 128), j = tc::row_bit (the expansion's order); bf16 in
 // the no-swizzle K-major core-matrix layout (8 x 16 B cores, K-adjacent 128 B apart, 8-row
 // groups 4096 B apart).
 static void fill_btiles(const PrimePlan& pl, const PrimeConst& c, uint16_t* out /* 3 x TC_B_BYTES/2 */) {

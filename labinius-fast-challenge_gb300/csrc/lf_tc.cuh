@@ -209,28 +209,9 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                : "memory");
 }
 
-// ---- bf16 bit expansion ----
-// One 128-bit word -> 128 bf16 values (2.0 for a set bit, else 0) in row `r` of a 128-row tile of
-// 8-row x 16-byte core matrices (cores adjacent along the row 128 B apart, 8-row groups 2048 B
-// apart). u32 o = 16 w + t of the row holds bits 32 w + t (low half) and 32 w + t + 16 (high
-// half) of the word; the other operand of the product uses the same order. Read as K-major
-// (row = M or N index) with lbo 128 / sbo 2048, or as MN-major (row = K index) with lbo 2048 /
-// sbo 128.
-__device__ __forceinline__ void write_row(uint8_t* tile, int r, uint4 v) {
-  const uint32_t xs[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    const uint32_t x = xs[q >> 2];
-    uint32_t u[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int t = (q & 3) * 4 + i;
-      u[i] = t < 15 ? (x << (14 - t)) & 0x40004000u : (x >> 1) & 0x40004000u;
-    }
-    *reinterpret_cast<uint4*>(tile + (r >> 3) * 2048 + q * 128 + (r & 7) * 16) = make_uint4(u[0], u[1], u[2], u[3]);
-  }
-}
-// Bit of the word held by position e (0..127) of an expanded row.
+// ---- the bf16 bit order of K1's expanded words ----
+// An expanded word's position e (0..127; u32 o = 16 w + t holds positions 2 o and 2 o + 1) holds
+// bit 32 w + t (low half) or 32 w + t + 16 (high half) of the word: the bit of position e.
 __host__ __device__ constexpr int row_bit(int e) { return 32 * (e >> 5) + ((e >> 1) & 15) + 16 * (e & 1); }
 
 // ---- bulk copies (the tensor memory accelerator, no tensor map) ----
